@@ -1,0 +1,390 @@
+#!/usr/bin/env python
+"""MDAS throughput on one GB300: Msamples/s of the sampler on the 4-D
+depth-of-field workload (1024x1024, 16 spp, bitsPerDim 1, extraImgBits 8,
+alpha 0.25, 4 candidates; 256 seeded discs behind a thin lens, f = 4,
+aperture 0.1).
+
+A step is one complete MDAS render through the reference's call sequence:
+InitialSampling, integrand, then `while N < budget`: SamplingPass + integrand
+for the new samples, then Integrate.
+
+metric: final sample count / (initial sampling + errors + adaptive sampling +
+integrate time): the reference's `total_mdas_time` (SDK/data/Scripts/
+parse_logs.py:148-154), integrand excluded.  Stage times are CUDA events on the
+grid's stream.
+
+e2e: the same metric through the host-buffer C-ABI call (mdas_render_host:
+scene primitives uploaded from host memory, float4 image copied back), timed by
+the host clock around each call, integrand included.
+
+--impl reference: the CPU restatement of the reference's MDAS step (the
+reference has no CPU implementation of its own) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "MDAS Msamples/s"
+UNIT = "Msamples/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="dof1024")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-cuda", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    return ap.parse_args()
+
+
+# ---- clocks during the timed region ------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        for r in rows:
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                               r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ---- traffic accounting -------------------------------------------------------------
+def stage_bytes(D: int, W: int, H: int, L0: int, passes: list, N_final: int, L_final: int) -> dict:
+    """Algorithmic (compulsory) DRAM bytes of each stage over one render.
+
+    init     : per initial leaf 4 samples * D floats + node 16 + box 8D + error 4 + seed 4 = 24D + 24
+    errors   : error read 4 per leaf; per recomputed leaf error write 4 + node 16 + box 8D
+               + its sample values (12 B each; 4 per leaf on the first pass, 5 per split pair after)
+    adaptive : error + seed read and seed write, 12 per leaf; per accepted leaf node 16 + box 8D +
+               new coordinate 4D + node write 16 (append) + 4D per gathered sample coordinate;
+               per split: left + right node 32 + left box coordinate 4 + right box 8D +
+               two errors 8 + right seed 4, minus the append's node write
+    integrate: per leaf node 16 + box 8D, 12 per sample value, pixels cleared and written 32 per pixel
+    """
+    init = L0 * (24 * D + 24)
+    err = adap = 0
+    for k, p in enumerate(passes):
+        L, R = p["L"], p["recomputed"]
+        V = 4 * R if k == 0 else (5 * R) // 2
+        err += 4 * L + R * (4 + 16 + 8 * D) + 12 * V
+        S, P, G = p["selected"], p["splits"], p["gathered"]
+        adap += 12 * L + S * (16 + 8 * D + 4 * D + 16) + 4 * D * G + P * (48 + 8 * D - 16)
+    integ = L_final * (16 + 8 * D) + 12 * N_final + 32 * W * H
+    return {"init": init, "errors": err, "adaptive": adap, "integrate": integ}
+
+
+# ---- the GB300 arm ------------------------------------------------------------------
+def run_gb300(args, rank: int, world: int, local_rank: int):
+    import numpy as np
+    import torch
+
+    import pmdas_gb300 as P
+    from pmdas_gb300.workloads import WORKLOADS
+
+    torch.cuda.set_device(local_rank)
+    wl = WORKLOADS[args.workload]
+    D, W, H = wl.dim, wl.width, wl.height
+    grid = P.KDGrid(D, wl.maxSamples, wl.candidatesNum, wl.bitsPerDim, wl.extraImgBits, wl.alpha, wl.scaleX,
+                    wl.scaleY, arith=P.ARITH_REFERENCE)
+    # replicas: each rank renders its own scene (independent images, no exchange)
+    scene = P.Scene(wl.scene_kind, wl.scene_seed + rank, wl.scene_count, wl.scaleX, wl.scaleY, W, H)
+    pixels = torch.zeros(H, W, 4, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+    grid.set_timing(True)
+
+    def one_render(record: bool):
+        grid.stage_times(reset=True)
+        grid.InitialSampling()
+        L0 = grid.GetNumberOfNodes()
+        scene.evaluate(grid, 0, grid.GetNumberOfSamples())
+        passes = []
+        while True:
+            n, _, l, _ = grid._counts()
+            if n >= wl.budget or n + l > wl.maxSamples:
+                break
+            grid.SamplingPass()
+            if record:
+                ps = grid.pass_stats()
+                ps["L"] = l
+                passes.append(ps)
+            n2, nn, _, _ = grid._counts()
+            scene.evaluate(grid, n2 - nn, nn)
+        grid.Integrate(pixels, W, H)
+        t = grid.stage_times(reset=True)
+        n, _, l, _ = grid._counts()
+        return n, l, L0, t, passes
+
+    for _ in range(args.warmup):
+        one_render(False)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches0 = grid.launch_count()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    time.sleep(0.2)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    stage_ms = [0.0] * 5
+    results = []
+    for _ in range(args.steps):
+        flush.zero_()  # L2 flushed between steps (outside the stage events)
+        n, l, L0, t, passes = one_render(record=not results)
+        for i in range(5):
+            stage_ms[i] += t[i]
+        results.append((n, l, L0, passes))
+    ev1.record()
+    torch.cuda.synchronize()
+    wall_ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    launches = grid.launch_count() - launches0
+
+    mdas_ms = sum(stage_ms[:4])
+    n_final, l_final, L0, passes = results[0]
+    total_samples = sum(r[0] for r in results)
+    # max over ranks of the time, sum of the work
+    if world > 1:
+        t = torch.tensor([mdas_ms, wall_ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        mdas_ms, wall_ms = t.tolist()
+        s = torch.tensor([total_samples], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(s)
+        total_samples = int(s.item())
+    value = total_samples / (mdas_ms / 1e3) / 1e6
+
+    # roofline of the dominant kernel
+    by = stage_bytes(D, W, H, L0, passes, n_final, l_final)
+    names = ["init", "errors", "adaptive", "integrate"]
+    dom = max(range(4), key=lambda i: stage_ms[i])
+    launches_of = {0: 1, 1: len(passes), 2: len(passes), 3: 1}[dom]
+    per_launch_bytes = by[names[dom]] / max(launches_of, 1)
+    per_launch_ms = stage_ms[dom] / args.steps / max(launches_of, 1)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
+    all_bytes = sum(by.values())
+    overall_gbs = all_bytes * args.steps / (mdas_ms / 1e3) / 1e9
+
+    # e2e through the host-buffer C-ABI call
+    e2e = None
+    if args.e2e_steps > 0:
+        host_px = np.zeros((H, W, 4), np.float32)
+        prims = scene.export().prims
+        grid.set_timing(False)
+        P.render_host(grid, scene, wl.budget, host_px, W, H, host_prims=prims)  # warm
+        times = []
+        for _ in range(args.e2e_steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st = P.render_host(grid, scene, wl.budget, host_px, W, H, host_prims=prims)
+            times.append(time.perf_counter() - t0)
+        e2e_s = statistics.median(times)
+        if world > 1:
+            t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_s = t.item()
+        e2e = {"value": round(st.numberOfSamples * world / e2e_s / 1e6, 3), "unit": UNIT,
+               "h2d_bytes_per_step": int(prims.nbytes),
+               "d2h_bytes_per_step": int(W * H * 16 + 56 * (st.passes + 1)),
+               "ms_per_step": round(e2e_s * 1e3, 3), "includes": "integrand, host syncs per pass, copies"}
+
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(mdas_ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded analytic integrand)",
+        "config": {"workload": f"{wl.name}: {D}-D {W}x{H}, {wl.spp:g} spp, bitsPerDim {wl.bitsPerDim}, "
+                               f"extraImgBits {wl.extraImgBits}, alpha {wl.alpha}, {wl.candidatesNum} candidates, "
+                               f"{wl.scene_count} discs",
+                   "final_samples": n_final, "final_leaves": l_final, "initial_leaves": L0,
+                   "passes": len(passes), "maxSamples": wl.maxSamples, "arith": "reference (fast-math)",
+                   "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
+        "stage_ms_per_step": {k: round(stage_ms[i] / args.steps, 4)
+                              for i, k in enumerate(["init", "errors", "adaptive", "integrate", "integrand"])},
+        "wall_ms_per_step": round(wall_ms / args.steps, 3),
+        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "algorithmic_bytes_per_launch": int(per_launch_bytes), "launches_per_step": launches_of,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s",
+                     "all_stages_gbs": round(overall_gbs, 1)},
+        "stage_bytes_per_step": by,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    return line, wl
+
+
+def cpu_baseline(wl, threads: int, budget_s: float = 30.0) -> dict:
+    """The oracle (CPU restatement of the reference's MDAS step) on the host cores."""
+    import pmdas_gb300 as P
+    from oracle import pyoracle as O
+    scene = P.Scene(wl.scene_kind, wl.scene_seed, wl.scene_count, wl.scaleX, wl.scaleY, wl.width, wl.height).export()
+    _, n, l, passes, t, wall = O.render(wl.dim, wl.bitsPerDim, wl.extraImgBits, wl.candidatesNum, wl.alpha,
+                                        wl.scaleX, wl.scaleY, wl.budget, wl.maxSamples, scene, wl.width, wl.height,
+                                        threads=threads)
+    mdas_s = sum(t[:4]) / 1e3
+    return {"value": round(n / mdas_s / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"one full {wl.name} render ({n} samples, {passes} passes); integrand "
+                      f"{t[4] / 1e3:.2f} s excluded", "wall_s": round(wall, 2)}
+
+
+def reference_cuda(wl, steps: int = 2) -> dict | None:
+    """The reference's own CUDA kernels (oracle/_ref, patched copy of SDK/lib/mdas/kdgrid.cu)
+    on the same GPU, same workload, same integrand; per-stage CUDA events."""
+    import torch
+
+    import pmdas_gb300 as P
+    from oracle import pyoracle as O
+    if not O.RefGrid.available():
+        return None
+    lib = O.RefGrid.lib()
+    ref = O.RefGrid(wl.dim, wl.maxSamples, wl.candidatesNum, wl.bitsPerDim, wl.extraImgBits, wl.alpha, wl.scaleX,
+                    wl.scaleY)
+    scene = P.Scene(wl.scene_kind, wl.scene_seed, wl.scene_count, wl.scaleX, wl.scaleY, wl.width, wl.height)
+    pixels = torch.zeros(wl.height, wl.width, 4, device="cuda")
+    coords, values = ref.ptr(0), ref.ptr(1)
+    s0 = torch.cuda.default_stream()
+
+    def timed(fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s0)
+        rc = fn()
+        b.record(s0)
+        assert rc == 0, rc
+        return a, b
+
+    totals = []
+    n = 0
+    for it in range(steps + 1):
+        evs = []
+        evs.append(timed(lambda: lib.ref_initial_sampling_async(ref.h)))
+        n, _, l, _ = ref.counts()
+        scene.evaluate_buffers(coords, values, wl.dim, 0, n)
+        while n < wl.budget and n + l <= wl.maxSamples:
+            evs.append(timed(lambda: lib.ref_compute_errors_async(ref.h)))
+            evs.append(timed(lambda: lib.ref_adaptive_sampling_async(ref.h)))
+            n, nn, l, _ = ref.counts()
+            scene.evaluate_buffers(coords, values, wl.dim, n - nn, nn)
+        evs.append(timed(lambda: lib.ref_integrate_async(ref.h, pixels.data_ptr(), wl.width, wl.height)))
+        torch.cuda.synchronize()
+        if it > 0:
+            totals.append(sum(a.elapsed_time(b) for a, b in evs))
+    ref.close()
+    ms = statistics.median(totals)
+    return {"value": round(n / (ms / 1e3) / 1e6, 3), "unit": UNIT, "ms_per_step": round(ms, 3),
+            "source": "SDK/lib/mdas/kdgrid.cu (four CUDA-13 edits), --use_fast_math, sm_103a, managed memory"}
+
+
+def run_reference_arm(args):
+    from pmdas_gb300.workloads import WORKLOADS
+    wl = WORKLOADS[args.workload]
+    threads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(wl, threads)
+        if i >= args.warmup:
+            vals.append(r)
+    value = statistics.median(v["value"] for v in vals)
+    n = vals[0]
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded analytic integrand)", "impl": "reference",
+            "config": {"workload": wl.name},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": n["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference_arm(args)), flush=True)
+        return
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    from pmdas_gb300 import build as B  # noqa: F401  (the library must already be built)
+    line, wl = run_gb300(args, rank, world, local_rank)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            try:
+                line["cpu_baseline"] = cpu_baseline(wl, os.cpu_count() or 1)
+            except Exception as e:  # reported, never fatal
+                line["cpu_baseline"] = {"error": str(e)}
+        if not args.no_reference_cuda and world == 1:
+            try:
+                line["reference_cuda"] = reference_cuda(wl)
+            except Exception as e:
+                line["reference_cuda"] = {"error": str(e)}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,228 @@
+/* mdas.h — C ABI of the GB300-native MDAS sampler (libpmdas_gb300.so).
+ *
+ * Drop-in for the reference's sampler class template
+ *   mdas::KDGrid<PointN<D>>           SDK/lib/mdas/kdgrid.h:10-107
+ * whose methods are implemented in     SDK/lib/mdas/kdgrid.cu:600-961.
+ * The point dimension D (3..6, SDK/lib/mdas/point.h:196-199) is a runtime
+ * argument instead of a template parameter.
+ *
+ * Conventions
+ *   - Every function returns an int status (MDAS_OK == 0) unless stated;
+ *     nothing throws across the ABI.  The reference prints CUDA errors and
+ *     continues (SDK/lib/mdas/buffer.h:6-16); this library returns them.
+ *   - The grid owns its device buffers (device memory, not managed memory).
+ *     Callers own the pixel buffers they pass in.
+ *   - All work is queued on the grid's stream (default: the legacy default
+ *     stream, like the reference).  Calls that must report counts to the host
+ *     (mdas_adaptive_sampling, mdas_sampling_pass) synchronise that stream,
+ *     as the reference does with cudaMemcpyFromSymbol (kdgrid.cu:753-759).
+ *   - Device pointers are plain `float*`; a float3 buffer is 3 floats per
+ *     sample, a float4 pixel buffer 4 floats per pixel.
+ */
+#ifndef PMDAS_GB300_MDAS_H
+#define PMDAS_GB300_MDAS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mdas_grid mdas_grid;
+typedef struct mdas_scene mdas_scene;
+
+#define MDAS_OK 0
+#define MDAS_ERR_INVALID 1   /* bad argument or configuration */
+#define MDAS_ERR_CUDA 2      /* a CUDA call failed */
+#define MDAS_ERR_CAPACITY 3  /* a pass could write past maxSamples / 2*maxSamples-1 leaves */
+#define MDAS_ERR_TIMEOUT 4   /* a bounded device-side wait gave up */
+#define MDAS_ERR_ALLOC 5     /* device or host allocation failed */
+#define MDAS_ERR_STATE 6     /* call out of order (e.g. a pass before InitialSampling) */
+
+/* Arithmetic of the float work.
+ * REFERENCE: the reference's own build flags (--use_fast_math); results match
+ *            the reference's CUDA kernels bit for bit.
+ * IEEE:      correctly rounded binary32 without contraction and a reproducible
+ *            pow; results match a CPU restatement bit for bit. */
+#define MDAS_ARITH_REFERENCE 0
+#define MDAS_ARITH_IEEE 1
+
+/* Replaces KDGrid::KDGrid(maxSamples, candidatesNum, bitsPerDim, extraImgBits,
+ * alpha, scaleX, scaleY, std::ofstream* log)   (kdgrid.h:42-51, kdgrid.cu:600-631).
+ * logPath may be NULL; otherwise the per-stage keys of the reference's log
+ * (INITIAL SAMPLES, INITIAL SAMPLING TIME, COMPUTE ERRORS TIME, SAMPLES,
+ * ADAPTIVE SAMPLING TIME, TOTAL SAMPLES, INTEGRATE TIME) are appended to it. */
+int mdas_create(mdas_grid** out, int dim, int maxSamples, int candidatesNum, int bitsPerDim, int extraImgBits,
+                float alpha, float scaleX, float scaleY, const char* logPath);
+
+/* mdas_create with the arithmetic mode and a CUDA stream (cudaStream_t, may be NULL). */
+int mdas_create_ex(mdas_grid** out, int dim, int maxSamples, int candidatesNum, int bitsPerDim, int extraImgBits,
+                   float alpha, float scaleX, float scaleY, const char* logPath, int arith, void* stream);
+
+/* Replaces KDGrid::~KDGrid (buffers freed, buffer.h:37-38). */
+int mdas_destroy(mdas_grid* g);
+
+/* Changes the stream later calls queue their work on. */
+int mdas_set_stream(mdas_grid* g, void* stream);
+
+/* Replaces KDGrid::InitialSampling (kdgrid.cu:633-674). */
+int mdas_initial_sampling(mdas_grid* g);
+
+/* Replaces KDGrid::ComputeErrors (kdgrid.cu:676-716). */
+int mdas_compute_errors(mdas_grid* g);
+
+/* Replaces KDGrid::AdaptiveSampling (kdgrid.cu:718-773).  Returns
+ * MDAS_ERR_CAPACITY instead of writing out of bounds when N + L > maxSamples
+ * or 2L > 2*maxSamples-1. */
+int mdas_adaptive_sampling(mdas_grid* g);
+
+/* Replaces KDGrid::SamplingPass (kdgrid.cu:775-779). */
+int mdas_sampling_pass(mdas_grid* g);
+
+/* Replaces KDGrid::Integrate(float4* pixels, int width, int height)
+ * (kdgrid.cu:781-820); pixels is a device float4 buffer of width*height. */
+int mdas_integrate(mdas_grid* g, float* pixels, int width, int height);
+
+/* Replaces KDGrid::ConvertToBytes(float4*, uchar4*, w, h) (kdgrid.cu:839-846);
+ * both are device buffers. */
+int mdas_convert_to_bytes(mdas_grid* g, const float* pixels, unsigned char* bytes, int width, int height);
+
+/* Replaces KDGrid::SamplingDensity(float4* pixels, w, h) (kdgrid.cu:822-837);
+ * pixels is a HOST float4 buffer, as in the reference. */
+int mdas_sampling_density(mdas_grid* g, float* hostPixels, int width, int height);
+
+/* Same result into a device float4 buffer. */
+int mdas_sampling_density_device(mdas_grid* g, float* pixels, int width, int height);
+
+/* Replaces KDGrid::Validate (kdgrid.cu:848-961): *valid = 1 if every sample
+ * lies in its leaf, the leaf volumes add up to scaleX*scaleY within 1%, and
+ * every sample is referenced exactly once; *valid = 0 otherwise. */
+int mdas_validate(mdas_grid* g, int* valid);
+
+/* Replace GetSampleCoordinates().Data() / GetSampleValues().Data()
+ * (kdgrid.h:65-66): device buffers the caller's integrand reads (AoS, dim
+ * floats per sample) and writes (3 floats per sample) in place. */
+float* mdas_sample_coordinates(mdas_grid* g);
+float* mdas_sample_values(mdas_grid* g);
+
+/* Replace GetNumberOfSamples / GetNewSamples / GetNumberOfNodes / GetNewNodes
+ * (kdgrid.h:69-72). */
+int mdas_get_counts(mdas_grid* g, int* numberOfSamples, int* newSamples, int* numberOfNodes, int* newNodes);
+
+/* Replace GetCandidatesNum / GetMaxNodeSize / GetMaxSamples / GetScaleX / GetScaleY
+ * (kdgrid.h:67-76), plus the dimension and arithmetic mode. */
+int mdas_get_info(mdas_grid* g, int* dim, int* maxSamples, int* candidatesNum, int* maxNodeSize, float* scaleX,
+                  float* scaleY, int* arith);
+
+/* g_error of the last ComputeErrors (the __device__ float of kdgrid.cu:21). */
+int mdas_get_gerror(mdas_grid* g, float* gError);
+
+/* Copy the complete sampler state to host buffers: coords [N*dim], values [N*3],
+ * nodes [L*4], boxes [L*2*dim], errors [L], seeds [L] (any may be NULL). */
+int mdas_dump_state(mdas_grid* g, float* coords, float* values, int* nodes, float* boxes, float* errors,
+                    uint32_t* seeds);
+
+/* Load a complete state from host buffers (a checkpoint, or a parity case). */
+int mdas_load_state(mdas_grid* g, int numberOfSamples, int numberOfNodes, const float* coords, const float* values,
+                    const int* nodes, const float* boxes, const float* errors, const uint32_t* seeds);
+
+/* Per-stage CUDA-event times accumulated since the last reset, in ms:
+ * [0] initial sampling, [1] compute errors, [2] adaptive sampling,
+ * [3] integrate, [4] integrand.  Timing is off until mdas_set_timing(g, 1). */
+int mdas_set_timing(mdas_grid* g, int on);
+int mdas_get_stage_times(mdas_grid* g, double* ms5, int reset);
+
+/* Tallies of the last sampling pass (for traffic accounting): leaves whose error
+ * was recomputed, leaves accepted, leaves split, and sample coordinates the
+ * adaptive pass read.  Valid after mdas_adaptive_sampling returns. */
+int mdas_get_pass_stats(mdas_grid* g, int* recomputed, int* selected, int* splits, int64_t* gathered);
+
+/* Number of kernels this grid has launched (all of them this library's own). */
+int mdas_get_launch_count(mdas_grid* g, uint64_t* launches);
+
+const char* mdas_status_string(int status);
+
+/* ---- analytic integrand (stands in for the OptiX ray-generation programs,
+ *      SDK/cuda/whitted.cu:164-293, SDK/cuda/direct.cu:116-152) ---- */
+#define MDAS_SCENE_DISCS_MB 0     /* (x, y, t)       */
+#define MDAS_SCENE_DISCS_DOF 1    /* (x, y, u, v)    */
+#define MDAS_SCENE_DISCS_MBDOF 2  /* (x, y, t, u, v) */
+#define MDAS_SCENE_DIRECT_LIGHT 3 /* (x, y, u, v)    */
+
+/* Seeded scene: kind, seed, primitive count, the grid's scaleX/scaleY and the image size. */
+int mdas_scene_create(mdas_scene** out, int kind, uint64_t seed, int count, float scaleX, float scaleY, int width,
+                      int height);
+int mdas_scene_destroy(mdas_scene* s);
+/* Copy the scene descriptor (descBytes >= mdas_scene_desc_size()) and its
+ * primitives (12 floats each) to host memory. */
+int mdas_scene_desc_size(void);
+int mdas_scene_export(mdas_scene* s, void* desc, int descBytes, float* prims, int maxPrims, int* dim, int* count);
+
+/* Evaluate samples [offset, offset+count) of the grid in place — the
+ * reference's launchSubframe with sample_offset/sample_count
+ * (optixMotionBlur.cpp:420-470).  count < 0 evaluates the samples the last
+ * adaptive pass added. */
+int mdas_evaluate(mdas_grid* g, mdas_scene* s, int offset, int count);
+
+/* The same integrand over any device buffers: coords AoS with `dim` floats per
+ * sample (dim >= the scene's dimension), values 3 floats per sample. */
+int mdas_scene_evaluate(mdas_scene* s, const float* coords, float* values, int dim, int offset, int count,
+                        void* stream);
+
+/* ---- the headless budget loop of the sample apps (optixMotionBlur.cpp:768-793) ----
+ * initial sampling, integrand, then while N < budget: sampling pass + integrand
+ * for the new samples, then integrate into a device float4 image.  Stops early
+ * (like the interactive loop's guard, optixMotionBlur.cpp:723-724) when the
+ * next pass could overrun the buffers. */
+typedef struct mdas_render_stats {
+    int numberOfSamples;
+    int numberOfNodes;
+    int passes;
+    int reserved;
+    double stageMs[5];  /* as mdas_get_stage_times, when timing is on */
+} mdas_render_stats;
+
+int mdas_render(mdas_grid* g, mdas_scene* s, int budget, float* pixels, int width, int height,
+                mdas_render_stats* stats);
+
+/* mdas_render with HOST input and output: the scene primitives are uploaded
+ * from `hostPrims` (12 floats each, may be NULL to keep the scene's) and the
+ * float4 image is copied back into `hostPixels`. */
+int mdas_render_host(mdas_grid* g, mdas_scene* s, const float* hostPrims, int budget, float* hostPixels, int width,
+                     int height, mdas_render_stats* stats);
+
+/* ---- env configuration (SDK/sutil/Environment.{h,cpp}; the options the MDAS
+ *      apps register, optixMotionBlur.cpp:104-137) ---- */
+typedef struct mdas_config {
+    int mdas;            /* Sampler.mdas        (bool, default 0)    */
+    float samples;       /* Sampler.samples     (float, default 1)   */
+    float scaleFactor;   /* Mdas.scaleFactor    (float, default 1.0) */
+    float alpha;         /* Mdas.alpha          (float, default 0.25)*/
+    int bitsPerDim;      /* Mdas.bitsPerDim     (int, default 0)     */
+    int extraImgBits;    /* Mdas.extraImgBits   (int, default 8)     */
+    int candidatesNum;   /* Mdas.candidatesNum  (int, default 4)     */
+    int width;           /* Film.width          (int, default 1024)  */
+    int height;          /* Film.height         (int, default 768)   */
+    float focalDistance; /* Camera.focalDistance (float, default 0)  */
+    float lensRadius;    /* Camera.lensRadius   (float, default 0)   */
+    float fovy;          /* Camera.fovy         (float, default 45)  */
+    int sceneKind;       /* Scene.kind (this library's synthetic scenes, default -1 = unset) */
+    int sceneCount;      /* Scene.count   (int, default 0)  */
+    int64_t sceneSeed;   /* Scene.seed    (int, default 0)  */
+    char filmFilename[256]; /* Film.filename */
+} mdas_config;
+
+/* Defaults of the registered options. */
+int mdas_config_defaults(mdas_config* cfg);
+
+/* Parse an .env file with the reference's rules (blocks `Name { key value }`,
+ * '#' comments, unknown keys are an error, numbers round-tripped through
+ * std::to_string, the first occurrence of a key wins).  `err` receives a
+ * message on failure. */
+int mdas_config_read(const char* path, mdas_config* cfg, char* err, int errBytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PMDAS_GB300_MDAS_H */

@@ -1,0 +1,154 @@
+// ref_harness.cu — C entry points around the reference's own mdas::KDGrid,
+// compiled from the reference's sources (SDK/lib/mdas/kdgrid.cu and its
+// headers) after the four mechanical CUDA-13 edits that oracle/build.py applies
+// in oracle/_ref/src (texture reference -> pointer + __ldg, `typename`,
+// cudaBindTexture -> cudaMemcpyToSymbol).
+//
+// TEST INFRASTRUCTURE ONLY: this is the checker that pins the oracle and the
+// GPU kernels to the reference on a GB300.  It drives the reference's own host
+// methods (InitialSampling, ComputeErrors, AdaptiveSampling, Integrate,
+// ConvertToBytes, SamplingDensity); state is read and written through the
+// reference's managed-memory buffers so that a pass can start from any state.
+//
+// Built with the reference's flags: --use_fast_math -lineinfo (sm_103a).
+
+// Standard and CUDA headers first, so that the access override below only
+// reaches the reference's own class.
+#include <cuda_runtime.h>
+#include <vector_types.h>
+#include <vector_functions.h>
+#include <cmath>
+#include <cstdlib>
+#include <cstdio>
+#include <cstring>
+#include <cfloat>
+#include <float.h>
+#include <stack>
+#include <vector>
+#include <algorithm>
+#include <iostream>
+#include <fstream>
+#include <sstream>
+#include <string>
+
+#define private public
+#include "mdas/kdgrid.cu"
+#undef private
+
+namespace {
+
+struct RefBase {
+    virtual ~RefBase() {}
+    virtual void initial() = 0;
+    virtual void errors() = 0;
+    virtual void adaptive() = 0;
+    virtual void integrate(float4* p, int w, int h) = 0;
+    virtual void bytes(float4* p, uchar4* b, int w, int h) = 0;
+    virtual void density(float4* p, int w, int h) = 0;
+    virtual void counts(int* N, int* nN, int* L, int* nL) = 0;
+    virtual void set_counts(int N, int L) = 0;
+    virtual void* ptr(int which) = 0;
+    virtual int dim() = 0;
+};
+
+template <class P>
+struct Ref : RefBase {
+    mdas::KDGrid<P> g;
+    Ref(int maxSamples, int cand, int bpd, int eib, float alpha, float sx, float sy)
+        : g(maxSamples, cand, bpd, eib, alpha, sx, sy, nullptr) {
+        g.newSamples = 0;
+        g.newNodes = 0;
+    }
+    void initial() override { g.InitialSampling(); }
+    void errors() override { g.ComputeErrors(); }
+    void adaptive() override { g.AdaptiveSampling(); }
+    void integrate(float4* p, int w, int h) override { g.Integrate(p, w, h); }
+    void bytes(float4* p, uchar4* b, int w, int h) override { g.ConvertToBytes(p, b, w, h); }
+    void density(float4* p, int w, int h) override { g.SamplingDensity(p, w, h); }
+    void counts(int* N, int* nN, int* L, int* nL) override {
+        *N = g.numberOfSamples;
+        *nN = g.newSamples;
+        *L = g.numberOfNodes;
+        *nL = g.newNodes;
+    }
+    void set_counts(int N, int L) override {
+        g.numberOfSamples = N;
+        g.numberOfNodes = L;
+    }
+    void* ptr(int which) override {
+        switch (which) {
+            case 0: return g.sampleCoordinates.Data();
+            case 1: return g.sampleValues.Data();
+            case 2: return g.nodes.Data();
+            case 3: return g.nodeBoxes.Data();
+            case 4: return g.nodeErrors.Data();
+            case 5: return g.seeds.Data();
+        }
+        return nullptr;
+    }
+    int dim() override { return P::DIM; }
+};
+
+}  // namespace
+
+extern "C" {
+
+void* ref_create(int dim, int maxSamples, int cand, int bpd, int eib, float alpha, float sx, float sy) {
+    switch (dim) {
+        case 3: return new Ref<mdas::Point3>(maxSamples, cand, bpd, eib, alpha, sx, sy);
+        case 4: return new Ref<mdas::Point4>(maxSamples, cand, bpd, eib, alpha, sx, sy);
+        case 5: return new Ref<mdas::Point5>(maxSamples, cand, bpd, eib, alpha, sx, sy);
+        case 6: return new Ref<mdas::Point6>(maxSamples, cand, bpd, eib, alpha, sx, sy);
+    }
+    return nullptr;
+}
+
+int ref_destroy(void* h) {
+    cudaDeviceSynchronize();
+    delete (RefBase*)h;
+    return 0;
+}
+
+int ref_sync() { return (int)cudaDeviceSynchronize(); }
+int ref_initial_sampling(void* h) { ((RefBase*)h)->initial(); return (int)cudaDeviceSynchronize(); }
+int ref_compute_errors(void* h) { ((RefBase*)h)->errors(); return (int)cudaDeviceSynchronize(); }
+int ref_adaptive_sampling(void* h) { ((RefBase*)h)->adaptive(); return (int)cudaDeviceSynchronize(); }
+
+// Unsynchronised variants, for timing with events on the legacy default stream.
+int ref_initial_sampling_async(void* h) { ((RefBase*)h)->initial(); return (int)cudaGetLastError(); }
+int ref_compute_errors_async(void* h) { ((RefBase*)h)->errors(); return (int)cudaGetLastError(); }
+int ref_adaptive_sampling_async(void* h) { ((RefBase*)h)->adaptive(); return (int)cudaGetLastError(); }
+int ref_integrate_async(void* h, float* pixels, int w, int hgt) {
+    ((RefBase*)h)->integrate((float4*)pixels, w, hgt);
+    return (int)cudaGetLastError();
+}
+
+int ref_integrate(void* h, float* pixels, int w, int hgt) {
+    ((RefBase*)h)->integrate((float4*)pixels, w, hgt);
+    return (int)cudaDeviceSynchronize();
+}
+int ref_convert_to_bytes(void* h, float* pixels, unsigned char* bytes, int w, int hgt) {
+    ((RefBase*)h)->bytes((float4*)pixels, (uchar4*)bytes, w, hgt);
+    return (int)cudaDeviceSynchronize();
+}
+int ref_sampling_density(void* h, float* hostPixels, int w, int hgt) {
+    cudaDeviceSynchronize();
+    ((RefBase*)h)->density((float4*)hostPixels, w, hgt);
+    return 0;
+}
+int ref_get_counts(void* h, int* N, int* nN, int* L, int* nL) {
+    ((RefBase*)h)->counts(N, nN, L, nL);
+    return 0;
+}
+int ref_set_counts(void* h, int N, int L) {
+    ((RefBase*)h)->set_counts(N, L);
+    return 0;
+}
+float ref_get_gerror() {
+    float v = 0.0f;
+    cudaMemcpyFromSymbol(&v, mdas::g_error, sizeof(float));
+    return v;
+}
+void* ref_ptr(void* h, int which) { return ((RefBase*)h)->ptr(which); }
+
+}  // extern "C"

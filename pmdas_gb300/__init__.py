@@ -1,0 +1,13 @@
+"""pmdas_gb300 — GB300-native MDAS (multidimensional adaptive sampling).
+
+The compute path is libpmdas_gb300.so (hand-written sm_103a CUDA kernels
+behind the C ABI of include/mdas.h); this package is its host-side mirror of
+the reference's ``mdas::KDGrid`` interface.
+"""
+from ._native import (ARITH_IEEE, ARITH_REFERENCE, MdasError, SCENE_DIRECT_LIGHT, SCENE_DISCS_DOF,
+                      SCENE_DISCS_MB, SCENE_DISCS_MBDOF, load)
+from .kdgrid import KDGrid, Scene, render, render_host
+from .workloads import WORKLOADS, Workload
+
+__all__ = ["KDGrid", "Scene", "render", "render_host", "load", "MdasError", "ARITH_REFERENCE", "ARITH_IEEE",
+           "SCENE_DISCS_MB", "SCENE_DISCS_DOF", "SCENE_DISCS_MBDOF", "SCENE_DIRECT_LIGHT", "WORKLOADS", "Workload"]

@@ -1,0 +1,684 @@
+// capi.cu — host side of libpmdas_gb300: the C ABI declared in include/mdas.h.
+//
+// Mirrors the host drivers of mdas::KDGrid (SDK/lib/mdas/kdgrid.cu:600-961)
+// and the headless budget loop of the sample apps
+// (SDK/optixMotionBlur/optixMotionBlur.cpp:768-793), over device memory and a
+// caller-chosen stream.  The kernels live in kdgrid_fast.cu (the reference's
+// arithmetic) and kdgrid_ieee.cu (strict IEEE); a grid picks one at creation.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+#include <math.h>
+#include <fstream>
+#include <string>
+#include <vector>
+#include <new>
+
+#include "../../include/mdas.h"
+#include "grid_types.h"
+#include "scene.h"
+
+namespace {
+
+__global__ void k_set_counts(MdasCounts* c, int N, int L) {
+    c->N = N;
+    c->L = L;
+    c->newN = 0;
+    c->newL = 0;
+    c->gerr = 0u;
+    c->recomputed = 0;
+    c->status = 0;
+    c->selected = 0;
+    c->passes = 0;
+    c->gathered = 0u;
+}
+
+struct PendingTiming {
+    int stage;
+    cudaEvent_t a, b;
+};
+
+}  // namespace
+
+struct mdas_grid {
+    MdasDeviceGrid dg{};
+    int arith = MDAS_ARITH_REFERENCE;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    int numSMs = 1;
+    int occ[4] = {1, 1, 1, 1};
+    int N = 0, L = 0, newN = 0, newL = 0;
+    bool initialized = false;
+    MdasCounts* hcounts = nullptr;  // pinned mirror of the device counters
+    std::ofstream* log = nullptr;
+    bool timing = false;
+    double stageMs[5] = {0, 0, 0, 0, 0};
+    uint64_t launches = 0;
+    float* scratch = nullptr;  // density / host-render image
+    size_t scratchBytes = 0;
+    std::vector<cudaEvent_t> eventPool;
+    std::vector<PendingTiming> pending;
+};
+
+namespace {
+
+int status_of(cudaError_t e) { return e == cudaSuccess ? MDAS_OK : MDAS_ERR_CUDA; }
+
+cudaEvent_t pool_get(mdas_grid* g) {
+    if (!g->eventPool.empty()) {
+        cudaEvent_t e = g->eventPool.back();
+        g->eventPool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void flush_timing(mdas_grid* g) {
+    for (const PendingTiming& p : g->pending) {
+        float ms = 0.0f;
+        if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess)
+            g->stageMs[p.stage] += ms;
+        g->eventPool.push_back(p.a);
+        g->eventPool.push_back(p.b);
+    }
+    g->pending.clear();
+}
+
+// Runs `launch` between two events of the given stage when timing is on.
+template <class F>
+int timed(mdas_grid* g, int stage, F&& launch) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (g->timing) {
+        a = pool_get(g);
+        b = pool_get(g);
+        cudaEventRecord(a, g->stream);
+    }
+    const cudaError_t e = launch();
+    if (g->timing) {
+        cudaEventRecord(b, g->stream);
+        g->pending.push_back({stage, a, b});
+    }
+    return status_of(e);
+}
+
+// Time of the most recent pending event pair of `stage` (syncs), for the log.
+double last_stage_ms(mdas_grid* g, int stage) {
+    double before = g->stageMs[stage];
+    flush_timing(g);
+    return g->stageMs[stage] - before;
+}
+
+int grid_for(mdas_grid* g, int which, int64_t items) {
+    const int64_t want = (items + 255) / 256;
+    const int64_t cap = (int64_t)g->numSMs * (g->occ[which] > 0 ? g->occ[which] : 1);
+    int64_t n = want < cap ? want : cap;
+    return (int)(n < 1 ? 1 : n);
+}
+
+cudaError_t launch_initial(mdas_grid* g, int L) {
+    return g->arith == MDAS_ARITH_IEEE ? mdas_ieee::initial_sampling(g->dg, L, g->stream)
+                                       : mdas_fast::initial_sampling(g->dg, L, g->stream);
+}
+cudaError_t launch_errors(mdas_grid* g, int grid) {
+    return g->arith == MDAS_ARITH_IEEE ? mdas_ieee::compute_errors(g->dg, grid, g->stream)
+                                       : mdas_fast::compute_errors(g->dg, grid, g->stream);
+}
+cudaError_t launch_adaptive(mdas_grid* g, int grid) {
+    return g->arith == MDAS_ARITH_IEEE ? mdas_ieee::adaptive_sampling(g->dg, grid, g->stream)
+                                       : mdas_fast::adaptive_sampling(g->dg, grid, g->stream);
+}
+cudaError_t launch_integrate(mdas_grid* g, int grid, float* pixels, int W, int H) {
+    return g->arith == MDAS_ARITH_IEEE ? mdas_ieee::integrate(g->dg, grid, pixels, W, H, g->stream)
+                                       : mdas_fast::integrate(g->dg, grid, pixels, W, H, g->stream);
+}
+
+int ensure_scratch(mdas_grid* g, size_t bytes) {
+    if (g->scratchBytes >= bytes) return MDAS_OK;
+    if (g->scratch) cudaFree(g->scratch);
+    g->scratch = nullptr;
+    g->scratchBytes = 0;
+    if (cudaMalloc(&g->scratch, bytes) != cudaSuccess) return MDAS_ERR_ALLOC;
+    g->scratchBytes = bytes;
+    return MDAS_OK;
+}
+
+int read_counts(mdas_grid* g) {
+    cudaError_t e = cudaMemcpyAsync(g->hcounts, g->dg.counts, sizeof(MdasCounts), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    g->N = g->hcounts->N;
+    g->L = g->hcounts->L;
+    g->newN = g->hcounts->newN;
+    g->newL = g->hcounts->newL;
+    return g->hcounts->status ? g->hcounts->status : MDAS_OK;
+}
+
+void free_grid(mdas_grid* g) {
+    if (!g) return;
+    flush_timing(g);
+    for (cudaEvent_t e : g->eventPool) cudaEventDestroy(e);
+    cudaFree(g->dg.coords);
+    cudaFree(g->dg.values);
+    cudaFree(g->dg.nodes);
+    cudaFree(g->dg.boxes);
+    cudaFree(g->dg.errors);
+    cudaFree(g->dg.seeds);
+    cudaFree(g->dg.counts);
+    cudaFree(g->dg.ctl);
+    cudaFree(g->dg.tiles);
+    if (g->scratch) cudaFree(g->scratch);
+    if (g->hcounts) cudaFreeHost(g->hcounts);
+    delete g->log;
+    delete g;
+}
+
+int scene_upload(mdas_scene* s, cudaStream_t stream) {
+    if (s->d_prims) return MDAS_OK;
+    const size_t bytes = sizeof(float) * (s->prims.size() ? s->prims.size() : 1);
+    if (cudaMalloc(&s->d_prims, bytes) != cudaSuccess) {
+        s->d_prims = nullptr;
+        return MDAS_ERR_ALLOC;
+    }
+    if (!s->prims.empty() && cudaMemcpyAsync(s->d_prims, s->prims.data(), sizeof(float) * s->prims.size(),
+                                             cudaMemcpyHostToDevice, stream) != cudaSuccess)
+        return MDAS_ERR_CUDA;
+    return cudaStreamSynchronize(stream) == cudaSuccess ? MDAS_OK : MDAS_ERR_CUDA;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mdas_status_string(int s) {
+    switch (s) {
+        case MDAS_OK: return "ok";
+        case MDAS_ERR_INVALID: return "invalid argument or configuration";
+        case MDAS_ERR_CUDA: return "CUDA error";
+        case MDAS_ERR_CAPACITY: return "sample or leaf capacity exceeded";
+        case MDAS_ERR_TIMEOUT: return "device-side wait timed out";
+        case MDAS_ERR_ALLOC: return "allocation failed";
+        case MDAS_ERR_STATE: return "call out of order";
+    }
+    return "unknown status";
+}
+
+int mdas_create_ex(mdas_grid** out, int dim, int maxSamples, int candidatesNum, int bitsPerDim, int extraImgBits,
+                   float alpha, float scaleX, float scaleY, const char* logPath, int arith, void* stream) {
+    if (!out) return MDAS_ERR_INVALID;
+    *out = nullptr;
+    if (dim < 3 || dim > 6 || maxSamples < 1 || maxSamples >= (1 << 30) || candidatesNum < 1 || bitsPerDim < 0 ||
+        extraImgBits < 0 || bitsPerDim * dim + 2 * extraImgBits > 28 || !(scaleX > 0.0f) || !(scaleY > 0.0f) ||
+        !isfinite(alpha) || !isfinite(scaleX) || !isfinite(scaleY) ||
+        (arith != MDAS_ARITH_REFERENCE && arith != MDAS_ARITH_IEEE))
+        return MDAS_ERR_INVALID;
+    mdas_grid* g = new (std::nothrow) mdas_grid();
+    if (!g) return MDAS_ERR_ALLOC;
+    g->arith = arith;
+    g->stream = (cudaStream_t)stream;
+    if (cudaGetDevice(&g->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&g->numSMs, cudaDevAttrMultiProcessorCount, g->device) != cudaSuccess) {
+        delete g;
+        return MDAS_ERR_CUDA;
+    }
+    for (int k = 0; k < 4; ++k)
+        g->occ[k] = arith == MDAS_ARITH_IEEE ? mdas_ieee::max_blocks_per_sm(dim, k) : mdas_fast::max_blocks_per_sm(dim, k);
+
+    MdasDeviceGrid& d = g->dg;
+    d.D = dim;
+    d.maxSamples = maxSamples;
+    d.maxNodes = 2 * maxSamples - 1;  // kdgrid.cu:627-629
+    d.candidatesNum = candidatesNum;
+    d.maxNodeSize = 4;                // kdgrid.cu:611
+    d.bitsPerDim = bitsPerDim;
+    d.extraImgBits = extraImgBits;
+    d.alpha = alpha;
+    d.scaleX = scaleX;
+    d.scaleY = scaleY;
+    d.maxTiles = (d.maxNodes + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
+    const size_t capSamples = ((size_t)maxSamples + 127) / 128 * 128;  // roundUp(maxSamples, 128), kdgrid.cu:625-626
+    bool ok = cudaMalloc(&d.coords, sizeof(float) * capSamples * dim) == cudaSuccess &&
+              cudaMalloc(&d.values, sizeof(float) * 3 * capSamples) == cudaSuccess &&
+              cudaMalloc(&d.nodes, sizeof(int4) * (size_t)d.maxNodes) == cudaSuccess &&
+              cudaMalloc(&d.boxes, sizeof(float) * 2 * dim * (size_t)d.maxNodes) == cudaSuccess &&
+              cudaMalloc(&d.errors, sizeof(float) * (size_t)d.maxNodes) == cudaSuccess &&
+              cudaMalloc(&d.seeds, sizeof(unsigned) * (size_t)d.maxNodes) == cudaSuccess &&
+              cudaMalloc(&d.counts, sizeof(MdasCounts)) == cudaSuccess &&
+              cudaMalloc(&d.ctl, sizeof(MdasCtl)) == cudaSuccess &&
+              cudaMalloc(&d.tiles, sizeof(unsigned long long) * (size_t)d.maxTiles) == cudaSuccess &&
+              cudaMallocHost(&g->hcounts, sizeof(MdasCounts)) == cudaSuccess;
+    if (ok) {
+        ok = cudaMemset(d.counts, 0, sizeof(MdasCounts)) == cudaSuccess &&
+             cudaMemset(d.ctl, 0, sizeof(MdasCtl)) == cudaSuccess &&
+             cudaMemset(d.tiles, 0, sizeof(unsigned long long) * (size_t)d.maxTiles) == cudaSuccess &&
+             cudaDeviceSynchronize() == cudaSuccess;
+    }
+    if (!ok) {
+        cudaGetLastError();
+        free_grid(g);
+        return MDAS_ERR_ALLOC;
+    }
+    memset(g->hcounts, 0, sizeof(MdasCounts));
+    if (logPath && logPath[0]) {
+        g->log = new (std::nothrow) std::ofstream(logPath, std::ios::app);
+        if (!g->log || !g->log->good()) {
+            free_grid(g);
+            return MDAS_ERR_INVALID;
+        }
+        g->timing = true;
+    }
+    *out = g;
+    return MDAS_OK;
+}
+
+int mdas_create(mdas_grid** out, int dim, int maxSamples, int candidatesNum, int bitsPerDim, int extraImgBits,
+                float alpha, float scaleX, float scaleY, const char* logPath) {
+    return mdas_create_ex(out, dim, maxSamples, candidatesNum, bitsPerDim, extraImgBits, alpha, scaleX, scaleY,
+                          logPath, MDAS_ARITH_REFERENCE, nullptr);
+}
+
+int mdas_destroy(mdas_grid* g) {
+    if (!g) return MDAS_ERR_INVALID;
+    cudaStreamSynchronize(g->stream);
+    free_grid(g);
+    return MDAS_OK;
+}
+
+int mdas_set_stream(mdas_grid* g, void* stream) {
+    if (!g) return MDAS_ERR_INVALID;
+    g->stream = (cudaStream_t)stream;
+    return MDAS_OK;
+}
+
+int mdas_initial_sampling(mdas_grid* g) {
+    if (!g) return MDAS_ERR_INVALID;
+    const MdasDeviceGrid& d = g->dg;
+    const int64_t L = ((int64_t)1 << (d.bitsPerDim * d.D)) << (2 * d.extraImgBits);  // kdgrid.cu:641
+    const int64_t N = 4 * L;                                                        // kdgrid.cu:642
+    if (N > d.maxSamples) return MDAS_ERR_CAPACITY;
+    int rc = timed(g, 0, [&]() {
+        // the reference zeroes the seed buffer here (kdgrid.cu:637); the kernels write every
+        // leaf slot's seed when the slot is created instead, so no memset is needed
+        cudaError_t e = launch_initial(g, (int)L);
+        if (e != cudaSuccess) return e;
+        k_set_counts<<<1, 1, 0, g->stream>>>(d.counts, (int)N, (int)L);
+        return cudaGetLastError();
+    });
+    g->launches += 2;
+    if (rc) return rc;
+    g->N = (int)N;
+    g->L = (int)L;
+    g->newN = 0;
+    g->newL = 0;
+    g->initialized = true;
+    if (g->log) {
+        const double t = last_stage_ms(g, 0);
+        *g->log << "INITIAL SAMPLES\n" << g->N << std::endl;
+        *g->log << "INITIAL SAMPLING TIME\n" << t << std::endl;
+    }
+    return MDAS_OK;
+}
+
+int mdas_compute_errors(mdas_grid* g) {
+    if (!g) return MDAS_ERR_INVALID;
+    if (!g->initialized) return MDAS_ERR_STATE;
+    const int grid = grid_for(g, MDAS_K_ERRORS, g->L);
+    int rc = timed(g, 1, [&]() { return launch_errors(g, grid); });
+    g->launches += 1;
+    if (rc) return rc;
+    if (g->log) *g->log << "COMPUTE ERRORS TIME\n" << last_stage_ms(g, 1) << std::endl;
+    return MDAS_OK;
+}
+
+int mdas_adaptive_sampling(mdas_grid* g) {
+    if (!g) return MDAS_ERR_INVALID;
+    if (!g->initialized) return MDAS_ERR_STATE;
+    // a pass adds at most one sample and one leaf per leaf
+    if ((int64_t)g->N + g->L > g->dg.maxSamples || 2 * (int64_t)g->L > g->dg.maxNodes) return MDAS_ERR_CAPACITY;
+    const int grid = grid_for(g, MDAS_K_ADAPTIVE, g->L);
+    int rc = timed(g, 2, [&]() { return launch_adaptive(g, grid); });
+    g->launches += 1;
+    if (rc) return rc;
+    rc = read_counts(g);
+    if (g->log) {
+        const double t = last_stage_ms(g, 2);
+        *g->log << "SAMPLES\n" << g->newN << std::endl;
+        *g->log << "ADAPTIVE SAMPLING TIME\n" << t << std::endl;
+    }
+    return rc;
+}
+
+int mdas_sampling_pass(mdas_grid* g) {
+    int rc = mdas_compute_errors(g);
+    if (rc) return rc;
+    return mdas_adaptive_sampling(g);
+}
+
+int mdas_integrate(mdas_grid* g, float* pixels, int width, int height) {
+    if (!g || !pixels || width <= 0 || height <= 0) return MDAS_ERR_INVALID;
+    if (!g->initialized) return MDAS_ERR_STATE;
+    const int grid = grid_for(g, MDAS_K_INTEGRATE, g->L);
+    int rc = timed(g, 3, [&]() { return launch_integrate(g, grid, pixels, width, height); });
+    g->launches += 1;
+    if (rc) return rc;
+    if (g->log) {
+        const double t = last_stage_ms(g, 3);
+        *g->log << "TOTAL SAMPLES\n" << g->N << std::endl;
+        *g->log << "INTEGRATE TIME\n" << t << std::endl;
+    }
+    return MDAS_OK;
+}
+
+int mdas_convert_to_bytes(mdas_grid* g, const float* pixels, unsigned char* bytes, int width, int height) {
+    if (!g || !pixels || !bytes || width <= 0 || height <= 0) return MDAS_ERR_INVALID;
+    const cudaError_t e = g->arith == MDAS_ARITH_IEEE
+                              ? mdas_ieee::convert_to_bytes(pixels, bytes, width * height, g->stream)
+                              : mdas_fast::convert_to_bytes(pixels, bytes, width * height, g->stream);
+    g->launches += 1;
+    return status_of(e);
+}
+
+int mdas_sampling_density_device(mdas_grid* g, float* pixels, int width, int height) {
+    if (!g || !pixels || width <= 0 || height <= 0) return MDAS_ERR_INVALID;
+    if (!g->initialized) return MDAS_ERR_STATE;
+    const cudaError_t e = g->arith == MDAS_ARITH_IEEE
+                              ? mdas_ieee::sampling_density(g->dg, pixels, width, height, g->stream)
+                              : mdas_fast::sampling_density(g->dg, pixels, width, height, g->stream);
+    g->launches += 2;
+    return status_of(e);
+}
+
+int mdas_sampling_density(mdas_grid* g, float* hostPixels, int width, int height) {
+    if (!g || !hostPixels || width <= 0 || height <= 0) return MDAS_ERR_INVALID;
+    const size_t bytes = sizeof(float) * 4 * (size_t)width * height;
+    int rc = ensure_scratch(g, bytes);
+    if (rc) return rc;
+    rc = mdas_sampling_density_device(g, g->scratch, width, height);
+    if (rc) return rc;
+    cudaError_t e = cudaMemcpyAsync(hostPixels, g->scratch, bytes, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    return status_of(e);
+}
+
+float* mdas_sample_coordinates(mdas_grid* g) { return g ? g->dg.coords : nullptr; }
+float* mdas_sample_values(mdas_grid* g) { return g ? g->dg.values : nullptr; }
+
+int mdas_get_counts(mdas_grid* g, int* numberOfSamples, int* newSamples, int* numberOfNodes, int* newNodes) {
+    if (!g) return MDAS_ERR_INVALID;
+    if (numberOfSamples) *numberOfSamples = g->N;
+    if (newSamples) *newSamples = g->newN;
+    if (numberOfNodes) *numberOfNodes = g->L;
+    if (newNodes) *newNodes = g->newL;
+    return MDAS_OK;
+}
+
+int mdas_get_info(mdas_grid* g, int* dim, int* maxSamples, int* candidatesNum, int* maxNodeSize, float* scaleX,
+                  float* scaleY, int* arith) {
+    if (!g) return MDAS_ERR_INVALID;
+    if (dim) *dim = g->dg.D;
+    if (maxSamples) *maxSamples = g->dg.maxSamples;
+    if (candidatesNum) *candidatesNum = g->dg.candidatesNum;
+    if (maxNodeSize) *maxNodeSize = g->dg.maxNodeSize;
+    if (scaleX) *scaleX = g->dg.scaleX;
+    if (scaleY) *scaleY = g->dg.scaleY;
+    if (arith) *arith = g->arith;
+    return MDAS_OK;
+}
+
+int mdas_get_gerror(mdas_grid* g, float* gError) {
+    if (!g || !gError) return MDAS_ERR_INVALID;
+    cudaError_t e = cudaMemcpyAsync(g->hcounts, g->dg.counts, sizeof(MdasCounts), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    unsigned bits = g->hcounts->gerr;
+    memcpy(gError, &bits, 4);
+    return MDAS_OK;
+}
+
+int mdas_dump_state(mdas_grid* g, float* coords, float* values, int* nodes, float* boxes, float* errors,
+                    uint32_t* seeds) {
+    if (!g) return MDAS_ERR_INVALID;
+    const MdasDeviceGrid& d = g->dg;
+    cudaError_t e = cudaSuccess;
+    const size_t N = (size_t)g->N, L = (size_t)g->L;
+    auto cp = [&](void* dst, const void* src, size_t bytes) {
+        if (dst && bytes && e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, g->stream);
+    };
+    cp(coords, d.coords, sizeof(float) * N * d.D);
+    cp(values, d.values, sizeof(float) * 3 * N);
+    cp(nodes, d.nodes, sizeof(int4) * L);
+    cp(boxes, d.boxes, sizeof(float) * 2 * d.D * L);
+    cp(errors, d.errors, sizeof(float) * L);
+    cp(seeds, d.seeds, sizeof(unsigned) * L);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    return status_of(e);
+}
+
+int mdas_load_state(mdas_grid* g, int numberOfSamples, int numberOfNodes, const float* coords, const float* values,
+                    const int* nodes, const float* boxes, const float* errors, const uint32_t* seeds) {
+    if (!g || numberOfSamples < 0 || numberOfNodes < 0 || numberOfSamples > g->dg.maxSamples ||
+        numberOfNodes > g->dg.maxNodes || !coords || !values || !nodes || !boxes || !errors || !seeds)
+        return MDAS_ERR_INVALID;
+    const MdasDeviceGrid& d = g->dg;
+    const size_t N = (size_t)numberOfSamples, L = (size_t)numberOfNodes;
+    cudaError_t e = cudaSuccess;
+    auto cp = [&](void* dst, const void* src, size_t bytes) {
+        if (bytes && e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, g->stream);
+    };
+    cp(d.coords, coords, sizeof(float) * N * d.D);
+    cp(d.values, values, sizeof(float) * 3 * N);
+    cp(d.nodes, nodes, sizeof(int4) * L);
+    cp(d.boxes, boxes, sizeof(float) * 2 * d.D * L);
+    cp(d.errors, errors, sizeof(float) * L);
+    cp(d.seeds, seeds, sizeof(unsigned) * L);
+    if (e == cudaSuccess && (size_t)d.maxNodes > L)
+        e = cudaMemsetAsync(d.seeds + L, 0, sizeof(unsigned) * ((size_t)d.maxNodes - L), g->stream);
+    if (e == cudaSuccess) {
+        k_set_counts<<<1, 1, 0, g->stream>>>(d.counts, (int)N, (int)L);
+        g->launches += 1;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);  // host buffers may go away after return
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    g->N = (int)N;
+    g->L = (int)L;
+    g->newN = 0;
+    g->newL = 0;
+    g->initialized = true;
+    return MDAS_OK;
+}
+
+int mdas_validate(mdas_grid* g, int* valid) {
+    if (!g || !valid) return MDAS_ERR_INVALID;
+    const int D = g->dg.D;
+    const size_t N = (size_t)g->N, L = (size_t)g->L;
+    std::vector<float> coords(N * D), boxes(L * 2 * D);
+    std::vector<int> nodes(L * 4);
+    int rc = mdas_dump_state(g, coords.data(), nullptr, nodes.data(), boxes.data(), nullptr, nullptr);
+    if (rc) return rc;
+    bool ok = true;
+    std::vector<int> hist(N, 0);
+    float totalVolume = 0.0f;
+    size_t total = 0;
+    for (size_t k = 0; k < L; ++k) {
+        const float* box = boxes.data() + k * 2 * D;
+        float vol = 1.0f;
+        for (int i = 0; i < D; ++i) vol *= box[D + i] - box[i];
+        totalVolume += vol;
+        for (int i = 0; i < 4; ++i) {
+            const int s = nodes[k * 4 + i];
+            if (s < 0) continue;
+            if ((size_t)s >= N) {
+                ok = false;
+                continue;
+            }
+            for (int j = 0; j < D; ++j) {
+                const float c = coords[(size_t)s * D + j];
+                if (c < box[j] || c > box[D + j]) ok = false;
+            }
+            hist[s]++;
+            total++;
+        }
+    }
+    const float rootVolume = g->dg.scaleX * g->dg.scaleY;
+    if (fabsf(totalVolume - rootVolume) > 1.0e-2f * rootVolume) ok = false;
+    if (total != N) ok = false;
+    for (size_t i = 0; i < N; ++i)
+        if (hist[i] != 1) ok = false;
+    *valid = ok ? 1 : 0;
+    return MDAS_OK;
+}
+
+int mdas_set_timing(mdas_grid* g, int on) {
+    if (!g) return MDAS_ERR_INVALID;
+    g->timing = on != 0 || g->log != nullptr;
+    return MDAS_OK;
+}
+
+int mdas_get_stage_times(mdas_grid* g, double* ms5, int reset) {
+    if (!g || !ms5) return MDAS_ERR_INVALID;
+    flush_timing(g);
+    for (int i = 0; i < 5; ++i) ms5[i] = g->stageMs[i];
+    if (reset)
+        for (double& x : g->stageMs) x = 0.0;
+    return MDAS_OK;
+}
+
+int mdas_get_pass_stats(mdas_grid* g, int* recomputed, int* selected, int* splits, int64_t* gathered) {
+    if (!g) return MDAS_ERR_INVALID;
+    if (recomputed) *recomputed = g->hcounts->recomputed;
+    if (selected) *selected = g->hcounts->selected;
+    if (splits) *splits = g->hcounts->newL;
+    if (gathered) *gathered = (int64_t)g->hcounts->gathered;
+    return MDAS_OK;
+}
+
+int mdas_get_launch_count(mdas_grid* g, uint64_t* launches) {
+    if (!g || !launches) return MDAS_ERR_INVALID;
+    *launches = g->launches;
+    return MDAS_OK;
+}
+
+// ---- scenes and the integrand ------------------------------------------------------
+
+int mdas_scene_create(mdas_scene** out, int kind, uint64_t seed, int count, float scaleX, float scaleY, int width,
+                      int height) {
+    if (!out) return MDAS_ERR_INVALID;
+    *out = nullptr;
+    mdas_scene* s = new (std::nothrow) mdas_scene();
+    if (!s) return MDAS_ERR_ALLOC;
+    int rc = mdas_generate_scene(kind, seed, count, scaleX, scaleY, width, height, &s->desc, &s->prims);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *out = s;  // the device copy is made on first use, so scenes can be generated without a GPU
+    return MDAS_OK;
+}
+
+int mdas_scene_destroy(mdas_scene* s) {
+    if (!s) return MDAS_ERR_INVALID;
+    if (s->d_prims) cudaFree(s->d_prims);
+    delete s;
+    return MDAS_OK;
+}
+
+int mdas_scene_desc_size(void) { return (int)sizeof(MdasScene); }
+
+int mdas_scene_export(mdas_scene* s, void* desc, int descBytes, float* prims, int maxPrims, int* dim, int* count) {
+    if (!s) return MDAS_ERR_INVALID;
+    if (desc) {
+        if (descBytes < (int)sizeof(MdasScene)) return MDAS_ERR_INVALID;
+        memcpy(desc, &s->desc, sizeof(MdasScene));
+    }
+    if (prims) {
+        if (maxPrims < s->desc.count) return MDAS_ERR_INVALID;
+        memcpy(prims, s->prims.data(), sizeof(float) * s->prims.size());
+    }
+    if (dim) *dim = s->desc.dim;
+    if (count) *count = s->desc.count;
+    return MDAS_OK;
+}
+
+int mdas_evaluate(mdas_grid* g, mdas_scene* s, int offset, int count) {
+    if (!g || !s || s->desc.dim > g->dg.D) return MDAS_ERR_INVALID;
+    if (!g->initialized) return MDAS_ERR_STATE;
+    if (count >= 0 && (offset < 0 || (int64_t)offset + count > g->dg.maxSamples)) return MDAS_ERR_INVALID;
+    const int grid = count >= 0 ? grid_for(g, MDAS_K_INIT, count) : g->numSMs * 8;
+    if (count == 0) return MDAS_OK;
+    int rc = scene_upload(s, g->stream);
+    if (rc) return rc;
+    rc = timed(g, 4, [&]() {
+        return mdas_launch_evaluate(s->desc, s->d_prims, g->dg.coords, g->dg.values, g->dg.D,
+                                    count < 0 ? g->dg.counts : nullptr, offset, count, grid, g->stream);
+    });
+    g->launches += 1;
+    return rc;
+}
+
+int mdas_scene_evaluate(mdas_scene* s, const float* coords, float* values, int dim, int offset, int count,
+                        void* stream) {
+    if (!s || !coords || !values || dim < s->desc.dim || dim > 6 || offset < 0 || count < 0)
+        return MDAS_ERR_INVALID;
+    if (count == 0) return MDAS_OK;
+    int rc = scene_upload(s, (cudaStream_t)stream);
+    if (rc) return rc;
+    int nsm = 1, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t want = ((int64_t)count + 255) / 256;
+    const int grid = (int)(want < (int64_t)nsm * 8 ? want : (int64_t)nsm * 8);
+    return status_of(mdas_launch_evaluate(s->desc, s->d_prims, coords, values, dim, nullptr, offset, count, grid,
+                                          (cudaStream_t)stream));
+}
+
+int mdas_render(mdas_grid* g, mdas_scene* s, int budget, float* pixels, int width, int height,
+                mdas_render_stats* stats) {
+    if (!g || !s || !pixels) return MDAS_ERR_INVALID;
+    int rc = mdas_initial_sampling(g);
+    if (rc) return rc;
+    rc = mdas_evaluate(g, s, 0, g->N);
+    if (rc) return rc;
+    int passes = 0;
+    while (g->N < budget) {
+        if ((int64_t)g->N + g->L > g->dg.maxSamples || 2 * (int64_t)g->L > g->dg.maxNodes) break;
+        rc = mdas_sampling_pass(g);
+        if (rc) return rc;
+        rc = mdas_evaluate(g, s, g->N - g->newN, g->newN);
+        if (rc) return rc;
+        passes++;
+    }
+    rc = mdas_integrate(g, pixels, width, height);
+    if (rc) return rc;
+    if (stats) {
+        stats->numberOfSamples = g->N;
+        stats->numberOfNodes = g->L;
+        stats->passes = passes;
+        stats->reserved = 0;
+        mdas_get_stage_times(g, stats->stageMs, 0);
+    }
+    return MDAS_OK;
+}
+
+int mdas_render_host(mdas_grid* g, mdas_scene* s, const float* hostPrims, int budget, float* hostPixels, int width,
+                     int height, mdas_render_stats* stats) {
+    if (!g || !s || !hostPixels || width <= 0 || height <= 0) return MDAS_ERR_INVALID;
+    const size_t bytes = sizeof(float) * 4 * (size_t)width * height;
+    int rc = ensure_scratch(g, bytes);
+    if (rc) return rc;
+    rc = scene_upload(s, g->stream);
+    if (rc) return rc;
+    if (hostPrims && s->desc.count > 0) {
+        const cudaError_t e = cudaMemcpyAsync(s->d_prims, hostPrims, sizeof(float) * MDAS_PRIM_STRIDE * s->desc.count,
+                                              cudaMemcpyHostToDevice, g->stream);
+        if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    }
+    rc = mdas_render(g, s, budget, g->scratch, width, height, stats);
+    if (rc) return rc;
+    cudaError_t e = cudaMemcpyAsync(hostPixels, g->scratch, bytes, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    return status_of(e);
+}
+
+}  // extern "C"

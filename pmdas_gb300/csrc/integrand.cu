@@ -1,0 +1,179 @@
+// integrand.cu — the analytic integrand kernel and the seeded scene generators.
+//
+// Stands in for the reference's OptiX launch over the sample buffer
+// (launchSubframe, SDK/optixMotionBlur/optixMotionBlur.cpp:420-470): evaluates
+// samples [offset, offset + count) of a grid's coordinate buffer into its value
+// buffer.  Compiled with strict IEEE flags so the CPU oracle, which shares
+// integrand.h, gets identical values.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <math.h>
+#include <vector>
+#include "integrand.h"
+#include "grid_types.h"
+#include "scene.h"
+
+namespace {
+
+template <int D>
+__global__ void __launch_bounds__(256) k_evaluate(MdasScene sc, const float* __restrict__ prims,
+                                                   const float* __restrict__ coords, float* __restrict__ values,
+                                                   const MdasCounts* __restrict__ counts, int offset, int count) {
+    extern __shared__ float s_prims[];
+    const int nfl = sc.count * MDAS_PRIM_STRIDE;
+    for (int k = threadIdx.x; k < nfl; k += blockDim.x) s_prims[k] = prims[k];
+    __syncthreads();
+    if (counts) {  // the samples the last adaptive pass added
+        offset = counts->N - counts->newN;
+        count = counts->newN;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const size_t s = (size_t)offset + i;
+        float c[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) c[d] = coords[s * D + d];
+        float out[3];
+        mdas_shade(&sc, s_prims, c, out);
+        values[3 * s + 0] = out[0];
+        values[3 * s + 1] = out[1];
+        values[3 * s + 2] = out[2];
+    }
+}
+
+// splitmix64 (Steele, Lea & Flood, "Fast splittable pseudorandom number
+// generators", OOPSLA 2014): the documented stream every scene is drawn from.
+struct SplitMix64 {
+    uint64_t s;
+    uint64_t next() {
+        uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    // 24 random bits -> [0, 1)
+    float uniform() { return (float)(next() >> 40) * (1.0f / 16777216.0f); }
+    float range(float a, float b) { return a + (b - a) * uniform(); }
+};
+
+}  // namespace
+
+cudaError_t mdas_launch_evaluate(const MdasScene& sc, const float* d_prims, const float* coords, float* values,
+                                 int dim, const MdasCounts* counts, int offset, int count, int grid, cudaStream_t s) {
+    const size_t smem = sizeof(float) * MDAS_PRIM_STRIDE * (size_t)sc.count;
+    if (grid <= 0) grid = 1;
+    if (dim < sc.dim) return cudaErrorInvalidValue;
+    switch (dim) {
+        case 3: k_evaluate<3><<<grid, 256, smem, s>>>(sc, d_prims, coords, values, counts, offset, count); break;
+        case 4: k_evaluate<4><<<grid, 256, smem, s>>>(sc, d_prims, coords, values, counts, offset, count); break;
+        case 5: k_evaluate<5><<<grid, 256, smem, s>>>(sc, d_prims, coords, values, counts, offset, count); break;
+        case 6: k_evaluate<6><<<grid, 256, smem, s>>>(sc, d_prims, coords, values, counts, offset, count); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// Scene generators.  Draw order is part of the format: the same seed gives the
+// same primitives on every machine (host code is built with -ffp-contract=off).
+int mdas_generate_scene(int kind, uint64_t seed, int count, float scaleX, float scaleY, int width, int height,
+                        MdasScene* sc, std::vector<float>* prims) {
+    if (count < 0 || count > MDAS_MAX_PRIMS || width <= 0 || height <= 0) return MDAS_ERR_INVALID;
+    *sc = MdasScene();
+    sc->kind = kind;
+    sc->count = count;
+    sc->scaleX = scaleX;
+    sc->scaleY = scaleY;
+    sc->background = 0.1f;
+    // fovy = 45 degrees: tan(pi/8) = sqrt(2) - 1 exactly in real arithmetic
+    const float tanHalf = (float)(sqrt(2.0) - 1.0);
+    sc->filmHalfH = tanHalf;
+    sc->filmHalfW = tanHalf * ((float)width / (float)height);
+    sc->focalDistance = 4.0f;
+    sc->lensRadius = 0.1f;
+    prims->assign((size_t)count * MDAS_PRIM_STRIDE, 0.0f);
+    SplitMix64 rng{seed};
+    float* p = prims->data();
+    switch (kind) {
+        case MDAS_SCENE_DISCS_MB: {
+            sc->dim = 3;
+            for (int k = 0; k < count; ++k) {
+                float* q = p + MDAS_PRIM_STRIDE * k;
+                q[0] = rng.uniform();             // center x in [0,1)
+                q[1] = rng.uniform();             // center y
+                q[3] = rng.range(0.02f, 0.08f);   // radius
+                q[8] = rng.uniform();             // R
+                q[9] = rng.uniform();             // G
+                q[10] = rng.uniform();            // B
+                q[4] = rng.range(-0.1f, 0.1f);    // velocity x per unit shutter time
+                q[5] = rng.range(-0.1f, 0.1f);    // velocity y
+                q[7] = q[3] * q[3];
+            }
+            break;
+        }
+        case MDAS_SCENE_DISCS_DOF:
+        case MDAS_SCENE_DISCS_MBDOF: {
+            sc->dim = kind == MDAS_SCENE_DISCS_DOF ? 4 : 5;
+            for (int k = 0; k < count; ++k) {
+                float* q = p + MDAS_PRIM_STRIDE * k;
+                q[2] = rng.range(1.0f, 10.0f);    // depth
+                q[3] = rng.range(0.05f, 0.3f);    // radius (world units)
+                q[8] = rng.uniform();
+                q[9] = rng.uniform();
+                q[10] = rng.uniform();
+                // center uniform over the view frustum's cross-section at that depth
+                q[0] = (2.0f * rng.uniform() - 1.0f) * (q[2] * sc->filmHalfW);
+                q[1] = (2.0f * rng.uniform() - 1.0f) * (q[2] * sc->filmHalfH);
+                q[6] = q[2] / sc->focalDistance;
+                q[7] = q[3] * q[3];
+            }
+            if (kind == MDAS_SCENE_DISCS_MBDOF) {
+                for (int k = 0; k < count; ++k) {
+                    float* q = p + MDAS_PRIM_STRIDE * k;
+                    q[4] = rng.range(-0.1f, 0.1f);
+                    q[5] = rng.range(-0.1f, 0.1f);
+                }
+            }
+            break;
+        }
+        case MDAS_SCENE_DIRECT_LIGHT: {
+            sc->dim = 4;
+            sc->background = 0.0f;
+            for (int k = 0; k < count; ++k) {
+                float* q = p + MDAS_PRIM_STRIDE * k;
+                q[3] = rng.range(0.3f, 1.0f);
+                q[0] = rng.range(-2.0f, 2.0f);
+                q[1] = rng.range(-2.0f, 2.0f);
+                q[2] = rng.range(0.5f, 2.0f);
+                q[6] = 1.0f / q[3];
+                q[7] = q[3] * q[3];
+            }
+            // pinhole at (0,-6,3) looking at the origin, up = +z
+            const double eye[3] = {0.0, -6.0, 3.0};
+            const double wl = sqrt(eye[0] * eye[0] + eye[1] * eye[1] + eye[2] * eye[2]);
+            const double w[3] = {-eye[0] / wl, -eye[1] / wl, -eye[2] / wl};
+            // u = w x up, normalised
+            double u[3] = {w[1] * 1.0 - w[2] * 0.0, w[2] * 0.0 - w[0] * 1.0, w[0] * 0.0 - w[1] * 0.0};
+            const double ul = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+            for (double& x : u) x /= ul;
+            // v = u x w
+            const double v[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
+            const double th = sqrt(2.0) - 1.0;
+            const double aspect = (double)width / (double)height;
+            for (int i = 0; i < 3; ++i) {
+                sc->eye[i] = (float)eye[i];
+                sc->W[i] = (float)w[i];
+                sc->U[i] = (float)(u[i] * th * aspect);
+                sc->V[i] = (float)(v[i] * th);
+            }
+            sc->lightCorner[0] = -0.5f;
+            sc->lightCorner[1] = -0.5f;
+            sc->lightCorner[2] = 4.0f;
+            sc->lightSize = 1.0f;
+            sc->emission = 10.0f;
+            sc->albedo = 0.7f;
+            break;
+        }
+        default:
+            return MDAS_ERR_INVALID;
+    }
+    return MDAS_OK;
+}

@@ -1,0 +1,25 @@
+// scene.h — host-side scene object and the integrand launcher (internal).
+#pragma once
+
+#include <stdint.h>
+#include <vector>
+#include <cuda_runtime.h>
+#include "integrand.h"
+#include "grid_types.h"
+
+#define MDAS_MAX_PRIMS 1024  // 48 KB of shared memory in the integrand kernel
+
+// Evaluates samples [offset, offset+count) of an AoS coordinate buffer with `dim`
+// floats per sample (dim >= the scene's own dimension; extra coordinates are
+// ignored).  With `counts`, the range is the last adaptive pass's new samples.
+cudaError_t mdas_launch_evaluate(const MdasScene& sc, const float* d_prims, const float* coords, float* values,
+                                 int dim, const MdasCounts* counts, int offset, int count, int grid, cudaStream_t s);
+
+int mdas_generate_scene(int kind, uint64_t seed, int count, float scaleX, float scaleY, int width, int height,
+                        MdasScene* sc, std::vector<float>* prims);
+
+struct mdas_scene {
+    MdasScene desc;
+    std::vector<float> prims;  // host copy
+    float* d_prims = nullptr;  // device copy
+};

@@ -1,0 +1,291 @@
+"""Python mirror of the reference's sampler class ``mdas::KDGrid<Point>``
+(SDK/lib/mdas/kdgrid.h:10-107) over the C ABI of libpmdas_gb300.
+
+Method names, argument meaning and call order follow the reference:
+``InitialSampling()``, ``SamplingPass()`` (= ``ComputeErrors()`` +
+``AdaptiveSampling()``), ``Integrate(pixels, w, h)``, ``ConvertToBytes(...)``,
+``SamplingDensity(...)``, ``Validate()`` and the ``Get*`` getters.  Device
+buffers are exchanged as torch CUDA tensors (torch is only the allocator and
+stream plumbing here; all work runs in the library's own kernels).
+
+Differences from the reference, all on error paths: failures raise
+:class:`MdasError` instead of printing and continuing, and a pass that would
+write past the buffers raises MDAS_ERR_CAPACITY instead of overrunning them.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as N
+
+
+class _DeviceArray:
+    """Minimal __cuda_array_interface__ view of a library-owned device buffer."""
+
+    def __init__(self, ptr: int, shape, typestr: str = "<f4"):
+        self.__cuda_array_interface__ = {"data": (int(ptr), False), "shape": tuple(shape), "typestr": typestr,
+                                         "version": 3, "strides": None}
+
+
+def _ptr(t) -> int:
+    if t is None:
+        return 0
+    if hasattr(t, "data_ptr"):
+        return t.data_ptr()
+    if isinstance(t, np.ndarray):
+        return t.ctypes.data
+    return int(t)
+
+
+class KDGrid:
+    """``mdas::KDGrid<PointN<dim>>`` with ``dim`` in 3..6."""
+
+    def __init__(self, dim: int, maxSamples: int, candidatesNum: int, bitsPerDim: int, extraImgBits: int,
+                 alpha: float, scaleX: float, scaleY: float, log: str | None = None,
+                 arith: int = N.ARITH_REFERENCE, stream: int | None = None):
+        lib = N.load()
+        h = C.c_void_p()
+        N.check(lib.mdas_create_ex(C.byref(h), dim, maxSamples, candidatesNum, bitsPerDim, extraImgBits,
+                                   float(alpha), float(scaleX), float(scaleY),
+                                   log.encode() if log else None, arith, stream or 0), "mdas_create")
+        self._lib = lib
+        self._h = h
+        self.dim = dim
+
+    # ---- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mdas_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream: int | None):
+        N.check(self._lib.mdas_set_stream(self._h, stream or 0), "mdas_set_stream")
+
+    # ---- the reference's methods
+    def InitialSampling(self):
+        N.check(self._lib.mdas_initial_sampling(self._h), "InitialSampling")
+
+    def ComputeErrors(self):
+        N.check(self._lib.mdas_compute_errors(self._h), "ComputeErrors")
+
+    def AdaptiveSampling(self):
+        N.check(self._lib.mdas_adaptive_sampling(self._h), "AdaptiveSampling")
+
+    def SamplingPass(self):
+        N.check(self._lib.mdas_sampling_pass(self._h), "SamplingPass")
+
+    def Integrate(self, pixels, width: int, height: int):
+        """``pixels``: CUDA float32 tensor with width*height*4 elements (float4 per pixel)."""
+        N.check(self._lib.mdas_integrate(self._h, _ptr(pixels), width, height), "Integrate")
+
+    def ConvertToBytes(self, pixels, pixelsBytes, width: int, height: int):
+        N.check(self._lib.mdas_convert_to_bytes(self._h, _ptr(pixels), _ptr(pixelsBytes), width, height),
+                "ConvertToBytes")
+
+    def SamplingDensity(self, pixels: np.ndarray, width: int, height: int):
+        """``pixels``: HOST float32 array with width*height*4 elements, as in the reference."""
+        assert pixels.dtype == np.float32 and pixels.flags.c_contiguous and pixels.size >= width * height * 4
+        N.check(self._lib.mdas_sampling_density(self._h, _ptr(pixels), width, height), "SamplingDensity")
+
+    def Validate(self) -> bool:
+        v = C.c_int()
+        N.check(self._lib.mdas_validate(self._h, C.byref(v)), "Validate")
+        return bool(v.value)
+
+    # ---- getters (kdgrid.h:65-77)
+    def _counts(self):
+        a, b, c, d = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        N.check(self._lib.mdas_get_counts(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)), "counts")
+        return a.value, b.value, c.value, d.value
+
+    def _info(self):
+        d, m, c, n, a = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        sx, sy = C.c_float(), C.c_float()
+        N.check(self._lib.mdas_get_info(self._h, C.byref(d), C.byref(m), C.byref(c), C.byref(n), C.byref(sx),
+                                        C.byref(sy), C.byref(a)), "info")
+        return dict(dim=d.value, maxSamples=m.value, candidatesNum=c.value, maxNodeSize=n.value, scaleX=sx.value,
+                    scaleY=sy.value, arith=a.value)
+
+    def GetNumberOfSamples(self) -> int:
+        return self._counts()[0]
+
+    def GetNewSamples(self) -> int:
+        return self._counts()[1]
+
+    def GetNumberOfNodes(self) -> int:
+        return self._counts()[2]
+
+    def GetNewNodes(self) -> int:
+        return self._counts()[3]
+
+    def GetMaxSamples(self) -> int:
+        return self._info()["maxSamples"]
+
+    def GetCandidatesNum(self) -> int:
+        return self._info()["candidatesNum"]
+
+    def GetMaxNodeSize(self) -> int:
+        return self._info()["maxNodeSize"]
+
+    def GetScaleX(self) -> float:
+        return self._info()["scaleX"]
+
+    def GetScaleY(self) -> float:
+        return self._info()["scaleY"]
+
+    def GetGError(self) -> float:
+        f = C.c_float()
+        N.check(self._lib.mdas_get_gerror(self._h, C.byref(f)), "g_error")
+        return f.value
+
+    def GetSampleCoordinatesPtr(self) -> int:
+        return self._lib.mdas_sample_coordinates(self._h)
+
+    def GetSampleValuesPtr(self) -> int:
+        return self._lib.mdas_sample_values(self._h)
+
+    def GetSampleCoordinates(self, count: int | None = None):
+        """Device view (torch CUDA tensor [count, dim]) of the coordinate buffer."""
+        import torch
+        n = self.GetNumberOfSamples() if count is None else count
+        return torch.as_tensor(_DeviceArray(self.GetSampleCoordinatesPtr(), (n, self.dim)), device="cuda")
+
+    def GetSampleValues(self, count: int | None = None):
+        """Device view (torch CUDA tensor [count, 3]) of the value buffer (float3)."""
+        import torch
+        n = self.GetNumberOfSamples() if count is None else count
+        return torch.as_tensor(_DeviceArray(self.GetSampleValuesPtr(), (n, 3)), device="cuda")
+
+    # ---- state (checkpoint / parity)
+    def dump_state(self) -> dict:
+        n, _, l, _ = self._counts()
+        st = dict(N=n, L=l,
+                  coords=np.empty((n, self.dim), np.float32), values=np.empty((n, 3), np.float32),
+                  nodes=np.empty((l, 4), np.int32), boxes=np.empty((l, 2 * self.dim), np.float32),
+                  errors=np.empty(l, np.float32), seeds=np.empty(l, np.uint32))
+        N.check(self._lib.mdas_dump_state(self._h, _ptr(st["coords"]), _ptr(st["values"]), _ptr(st["nodes"]),
+                                          _ptr(st["boxes"]), _ptr(st["errors"]), _ptr(st["seeds"])), "dump_state")
+        return st
+
+    def load_state(self, st: dict):
+        arrs = {}
+        for k, dt in (("coords", np.float32), ("values", np.float32), ("nodes", np.int32), ("boxes", np.float32),
+                      ("errors", np.float32), ("seeds", np.uint32)):
+            arrs[k] = np.ascontiguousarray(st[k], dtype=dt)
+        N.check(self._lib.mdas_load_state(self._h, int(st["N"]), int(st["L"]), _ptr(arrs["coords"]),
+                                          _ptr(arrs["values"]), _ptr(arrs["nodes"]), _ptr(arrs["boxes"]),
+                                          _ptr(arrs["errors"]), _ptr(arrs["seeds"])), "load_state")
+
+    # ---- timing / accounting
+    def set_timing(self, on: bool = True):
+        N.check(self._lib.mdas_set_timing(self._h, 1 if on else 0), "set_timing")
+
+    def stage_times(self, reset: bool = False) -> list:
+        a = (C.c_double * 5)()
+        N.check(self._lib.mdas_get_stage_times(self._h, a, 1 if reset else 0), "stage_times")
+        return list(a)
+
+    def pass_stats(self) -> dict:
+        """Tallies of the last pass: recomputed errors, accepted leaves, splits, gathered samples."""
+        r, s, p, g = C.c_int(), C.c_int(), C.c_int(), C.c_int64()
+        N.check(self._lib.mdas_get_pass_stats(self._h, C.byref(r), C.byref(s), C.byref(p), C.byref(g)), "stats")
+        return dict(recomputed=r.value, selected=s.value, splits=p.value, gathered=g.value)
+
+    def launch_count(self) -> int:
+        v = C.c_uint64()
+        N.check(self._lib.mdas_get_launch_count(self._h, C.byref(v)), "launch_count")
+        return v.value
+
+
+@dataclass
+class SceneDesc:
+    kind: int
+    dim: int
+    count: int
+    desc_bytes: bytes
+    prims: np.ndarray
+
+
+class Scene:
+    """A seeded analytic integrand (stands in for the OptiX ray generation programs)."""
+
+    def __init__(self, kind: int, seed: int, count: int, scaleX: float, scaleY: float, width: int, height: int):
+        lib = N.load()
+        h = C.c_void_p()
+        N.check(lib.mdas_scene_create(C.byref(h), kind, seed, count, float(scaleX), float(scaleY), width, height),
+                "mdas_scene_create")
+        self._lib = lib
+        self._h = h
+        self.kind = kind
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mdas_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def export(self) -> SceneDesc:
+        size = self._lib.mdas_scene_desc_size()
+        desc = C.create_string_buffer(size)
+        dim, count = C.c_int(), C.c_int()
+        N.check(self._lib.mdas_scene_export(self._h, None, 0, None, 0, C.byref(dim), C.byref(count)), "export")
+        prims = np.zeros((max(count.value, 1), N.PRIM_STRIDE), np.float32)
+        N.check(self._lib.mdas_scene_export(self._h, desc, size, prims.ctypes.data, count.value, C.byref(dim),
+                                            C.byref(count)), "export")
+        return SceneDesc(self.kind, dim.value, count.value, desc.raw, prims[:count.value].copy())
+
+    def evaluate_buffers(self, coords_ptr: int, values_ptr: int, dim: int, offset: int, count: int,
+                         stream: int | None = None):
+        """Evaluate samples [offset, offset+count) of any device coordinate buffer into a value buffer."""
+        N.check(self._lib.mdas_scene_evaluate(self._h, coords_ptr, values_ptr, dim, offset, count, stream or 0),
+                "mdas_scene_evaluate")
+
+    def evaluate(self, grid: KDGrid, offset: int, count: int):
+        """launchSubframe: evaluate samples [offset, offset+count) of `grid` in place."""
+        N.check(self._lib.mdas_evaluate(grid.handle, self._h, offset, count), "mdas_evaluate")
+
+
+def render(grid: KDGrid, scene: Scene, budget: int, pixels, width: int, height: int) -> N.RenderStats:
+    """The headless budget loop of the sample apps (optixMotionBlur.cpp:768-793)."""
+    st = N.RenderStats()
+    N.check(grid._lib.mdas_render(grid.handle, scene.handle, int(budget), _ptr(pixels), width, height,
+                                  C.byref(st)), "mdas_render")
+    return st
+
+
+def render_host(grid: KDGrid, scene: Scene, budget: int, host_pixels: np.ndarray, width: int, height: int,
+                host_prims: np.ndarray | None = None) -> N.RenderStats:
+    """The budget loop with host input (scene primitives) and host output (float4 image)."""
+    assert host_pixels.dtype == np.float32 and host_pixels.size >= width * height * 4
+    st = N.RenderStats()
+    N.check(grid._lib.mdas_render_host(grid.handle, scene.handle, _ptr(host_prims), int(budget), _ptr(host_pixels),
+                                       width, height, C.byref(st)), "mdas_render_host")
+    return st

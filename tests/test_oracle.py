@@ -1,0 +1,335 @@
+"""CPU checks of the oracle itself (no GPU).
+
+The C++ oracle (oracle/mdas_oracle.cpp) is compared bit for bit with a
+second, independent restatement written here in plain Python over numpy
+float32 scalars (IEEE binary32, one rounding per operation), on tiny grids of
+every dimension the reference instantiates (SDK/lib/mdas/kdgrid.cu:25-104).
+The reproducible pow/sin/cos used by both are checked against float64 libm.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+
+f32 = np.float32
+M32 = 0xFFFFFFFF
+
+
+# ---- SDK/cuda/random.h:31-67, restated -----------------------------------------
+def tea4(v0, v1):
+    s0 = 0
+    for _ in range(4):
+        s0 = (s0 + 0x9E3779B9) & M32
+        v0 = (v0 + ((((v1 << 4) & M32) + 0xA341316C) ^ ((v1 + s0) & M32) ^ ((v1 >> 5) + 0xC8013EA4))) & M32
+        v1 = (v1 + ((((v0 << 4) & M32) + 0xAD90777D) ^ ((v0 + s0) & M32) ^ ((v0 >> 5) + 0x7E95761E))) & M32
+    return v0
+
+
+class Rng:
+    def __init__(self, seed):
+        self.s = seed
+
+    def rnd(self):
+        self.s = (1664525 * self.s + 1013904223) & M32
+        return f32(self.s & 0xFFFFFF) / f32(16777216.0)
+
+
+def py_initial(D, bpd, eib, sx, sy):
+    L = (1 << (bpd * D)) << (2 * eib)
+    coords = np.zeros((4 * L, D), np.float32)
+    nodes = np.zeros((L, 4), np.int32)
+    boxes = np.zeros((L, 2 * D), np.float32)
+    seeds = np.zeros(L, np.uint32)
+    for n in range(L):
+        off = [f32(0)] * D
+        ext = [f32(0)] * D
+        for j in range(D):
+            xq = 0
+            inv = 1 << bpd
+            for k in range(bpd):
+                xq |= ((n >> (D * k + (D - j - 1))) & 1) << k
+            if j < 2:
+                for k in range(bpd, bpd + eib):
+                    xq |= ((n >> (D * bpd + 2 * (k - bpd) + 1 - j)) & 1) << k
+                inv <<= eib
+            ext[j] = f32(1.0) / f32(inv)
+            off[j] = f32(xq) * ext[j]
+        off[0] *= f32(sx)
+        off[1] *= f32(sy)
+        ext[0] *= f32(sx)
+        ext[1] *= f32(sy)
+        r = Rng(tea4(n, 0))
+        for s in range(4):
+            rs = [r.rnd() for _ in range(D)]
+            coords[4 * n + s] = [off[i] + rs[i] * ext[i] for i in range(D)]
+            nodes[n, s] = 4 * n + s
+        seeds[n] = r.s
+        boxes[n, :D] = off
+        boxes[n, D:] = [off[i] + ext[i] for i in range(D)]
+    return dict(N=4 * L, L=L, coords=coords, nodes=nodes, boxes=boxes, errors=np.full(L, -1, np.float32),
+                seeds=seeds)
+
+
+def py_errors(st, D):
+    L = st["L"]
+    gmax = f32(0)
+    for i in range(L):
+        e = st["errors"][i]
+        if e < 0:
+            idx = [x for x in st["nodes"][i] if x >= 0]
+            vals = [st["values"][x] for x in idx]
+            vol = f32(1)
+            for d in range(D):
+                vol = vol * (st["boxes"][i, D + d] - st["boxes"][i, d])
+            avg = [f32(0)] * 3
+            for v in vals:
+                avg = [avg[c] + v[c] for c in range(3)]
+            inv = f32(1) / f32(len(vals))
+            avg = [a * inv for a in avg]
+            diff = [f32(0)] * 3
+            for v in vals:
+                diff = [diff[c] + abs(v[c] - avg[c]) for c in range(3)]
+            e = f32(0)
+            for c in range(3):
+                if avg[c] != 0:
+                    e = e + diff[c] / avg[c]
+            e = e / f32(len(vals))
+            e = e + f32(1e-5)
+            e = e * vol
+            st["errors"][i] = e
+        gmax = max(gmax, e)
+    return gmax
+
+
+def py_adaptive(st, D, cand, alpha, gerr):
+    N, L = st["N"], st["L"]
+    flags, cands = [], []
+    for i in range(L):
+        seed = int(st["seeds"][i]) or tea4(i, 0)
+        r = Rng(seed)
+        p = O.powf(st["errors"][i] / gerr, alpha)
+        sel = p >= r.rnd()
+        best, split = None, False
+        if sel:
+            box = st["boxes"][i]
+            idx = [x for x in st["nodes"][i] if x >= 0]
+            maxd = f32(-1)
+            best = [f32(0)] * D
+            diag = [box[D + d] - box[d] for d in range(D)]
+            for _ in range(cand):
+                rs = [r.rnd() for _ in range(D)]
+                c = [box[d] + rs[d] * diag[d] for d in range(D)]
+                mind = f32(3.4028234663852886e38)
+                for x in idx:
+                    acc = f32(0)
+                    for d in range(D):
+                        t = c[d] - st["coords"][x, d]
+                        acc = acc + t * t
+                    dist = np.sqrt(acc)
+                    if mind > dist:
+                        mind = dist
+                if maxd < mind:
+                    maxd = mind
+                    best = c
+            split = len(idx) >= 4
+        st["seeds"][i] = r.s
+        flags.append((sel, split))
+        cands.append(best)
+    ns = nn = 0
+    newc = np.zeros((L, D), np.float32)
+    for i in range(L):
+        sel, split = flags[i]
+        if not sel:
+            continue
+        si = N + ns
+        ns += 1
+        st["coords"] = _grow(st["coords"], si + 1)
+        st["coords"][si] = cands[i]
+        idx = [x for x in st["nodes"][i] if x >= 0]
+        if not split:
+            st["nodes"][i, len(idx)] = si
+            continue
+        box = st["boxes"][i].copy()
+        loc = idx + [si]
+        diag = [box[D + d] - box[d] for d in range(D)]
+        axis, mx = -1, f32(-3.4028234663852886e38)
+        for d in range(D - 1, -1, -1):
+            if mx < diag[d]:
+                mx, axis = diag[d], d
+        for a in range(len(loc) - 1):
+            for b in range(len(loc) - a - 1):
+                if st["coords"][loc[b], axis] > st["coords"][loc[b + 1], axis]:
+                    loc[b], loc[b + 1] = loc[b + 1], loc[b]
+        md = len(loc) >> 1
+        pos = f32(0.5) * (st["coords"][loc[md - 1], axis] + st["coords"][loc[md], axis])
+        ro = L + nn
+        nn += 1
+        for k in ("nodes", "boxes", "errors", "seeds"):
+            st[k] = _grow(st[k], ro + 1)
+        st["nodes"][ro] = [loc[md + k] if k < len(loc) - md else ~D for k in range(4)]
+        st["nodes"][i] = [loc[k] if k < md else ~D for k in range(4)]
+        st["boxes"][ro] = box
+        st["boxes"][i, D + axis] = pos
+        st["boxes"][ro, axis] = pos
+        st["errors"][i] = -1
+        st["errors"][ro] = -1
+        st["seeds"][ro] = 0
+    st["N"] += ns
+    st["L"] += nn
+    del newc
+    return ns, nn
+
+
+def _grow(a, n):
+    if len(a) >= n:
+        return a
+    b = np.zeros((max(n, 2 * len(a)),) + a.shape[1:], a.dtype)
+    b[:len(a)] = a
+    return b
+
+
+@pytest.mark.parametrize("D,bpd,eib,sx,sy", [(3, 1, 2, 16.0, 16.0), (4, 1, 1, 8.0, 4.0), (5, 1, 0, 1.0, 1.0),
+                                             (6, 1, 0, 3.0, 2.0), (4, 0, 2, 7.5, 3.75)])
+def test_oracle_matches_python_restatement(D, bpd, eib, sx, sy):
+    cand, alpha = 4, 0.25
+    ref = py_initial(D, bpd, eib, sx, sy)
+    g = O.OracleGrid(D, 8192, cand, bpd, eib, alpha, sx, sy)
+    g.initial_sampling()
+    st = g.dump_state()
+    for k in ("coords", "nodes", "boxes", "errors", "seeds"):
+        np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
+    rng = np.random.default_rng(D)
+    for _ in range(4):
+        vals = rng.random((g.N, 3), dtype=np.float32)
+        vals[rng.random(g.N) < 0.1, 1] = 0.0  # zero channels exercise the avg != 0 guard
+        g.values[:g.N] = vals
+        ref["values"] = vals.copy()
+        ge = g.compute_errors()
+        gp = py_errors(ref, D)
+        assert ge == gp
+        g.adaptive_sampling()
+        py_adaptive(ref, D, cand, alpha, gp)
+        st = g.dump_state()
+        assert (st["N"], st["L"]) == (ref["N"], ref["L"])
+        n, l = st["N"], st["L"]
+        np.testing.assert_array_equal(st["coords"], ref["coords"][:n])
+        np.testing.assert_array_equal(st["nodes"], ref["nodes"][:l])
+        np.testing.assert_array_equal(st["boxes"], ref["boxes"][:l])
+        np.testing.assert_array_equal(st["errors"], ref["errors"][:l])
+        np.testing.assert_array_equal(st["seeds"], ref["seeds"][:l])
+        assert g.validate() == 0
+
+
+def py_integrate(st, D, W, H, sx, sy):
+    px = np.zeros((H, W, 4), np.float32)
+    sx, sy = f32(sx), f32(sy)
+    step = (sx / f32(W), sy / f32(H))
+    pix_area = (sx * sy) / f32(W * H)
+    inv_area = f32(1) / pix_area
+    for i in range(st["L"]):
+        idx = [x for x in st["nodes"][i] if x >= 0]
+        v = [f32(0)] * 3
+        for x in idx:
+            v = [v[c] + st["values"][x, c] for c in range(3)]
+        inv = f32(1) / f32(len(idx))
+        v = [a * inv for a in v]
+        b = st["boxes"][i]
+        vol = f32(1)
+        for d in range(D):
+            vol = vol * (b[D + d] - b[d])
+        x0 = int(b[0] * f32(W) / sx)
+        x1 = min(int(b[D] * f32(W) / sx) + 1, W)
+        y0 = int(b[1] * f32(H) / sy)
+        y1 = min(int(b[D + 1] * f32(H) / sy) + 1, H)
+        pminy = f32(y0) * sy / f32(H)
+        pmaxy = pminy + step[1]
+        for y in range(y0, y1):
+            pminx = f32(x0) * sx / f32(W)
+            pmaxx = pminx + step[0]
+            for x in range(x0, x1):
+                clox, chix = max(pminx, b[0]), min(pmaxx, b[D])
+                cloy, chiy = max(pminy, b[1]), min(pmaxy, b[D + 1])
+                if clox < chix and cloy < chiy:
+                    w = (chix - clox) * (chiy - cloy) * vol / ((b[D] - b[0]) * (b[D + 1] - b[1]))
+                    for c in range(3):
+                        px[y, x, c] += (v[c] * w) * inv_area
+                pminx = pmaxx
+                pmaxx = pmaxx + step[0]
+            pminy = pmaxy
+            pmaxy = pmaxy + step[1]
+    return px
+
+
+@pytest.mark.parametrize("D,W,H,sx,sy", [(3, 12, 10, 12.0, 10.0), (4, 16, 8, 4.0, 2.0)])
+def test_oracle_integrate_matches_python(D, W, H, sx, sy):
+    g = O.OracleGrid(D, 8192, 4, 1, 1, 0.25, sx, sy)
+    g.initial_sampling()
+    rng = np.random.default_rng(7)
+    for _ in range(3):
+        g.values[:g.N] = rng.random((g.N, 3), dtype=np.float32)
+        g.sampling_pass()
+    g.values[:g.N] = rng.random((g.N, 3), dtype=np.float32)
+    st = g.dump_state()
+    px = g.integrate(W, H, threads=1)
+    np.testing.assert_array_equal(px, py_integrate(st, D, W, H, sx, sy))
+    # partition of unity: a constant value integrates to that constant everywhere
+    g.values[:g.N] = 0.5
+    px = g.integrate(W, H, threads=1)
+    np.testing.assert_allclose(px[..., :3], 0.5, rtol=1e-5)
+    assert np.all(px[..., 3] == 0)
+
+
+def test_oracle_density_and_bytes():
+    g = O.OracleGrid(3, 8192, 4, 1, 2, 0.25, 32.0, 32.0)
+    g.initial_sampling()
+    d = g.sampling_density(32, 32)
+    assert np.all(d[..., 3] == 1.0)
+    # every sample lands in one pixel; equal addends -> exact multiples
+    cnt = np.round(d[..., 0] / np.float32(0.05)).astype(int)
+    assert cnt.sum() == g.N
+    px = np.array([[[0.0, 0.002, 0.5, 7.0], [1.0, 2.0, -1.0, 0.0]]], np.float32)
+    b = O.convert_to_bytes(px)
+    assert b[0, 0, 3] == 255 and b[0, 1, 3] == 255
+    assert b[0, 0, 0] == 0 and b[0, 1, 0] == 255 and b[0, 1, 1] == 255 and b[0, 1, 2] == 0
+    assert b[0, 0, 1] == int(min(np.float32(12.92) * np.float32(0.002) * 256, 255))
+    s = 1.055 * 0.5 ** (1 / 2.4) - 0.055
+    assert abs(int(b[0, 0, 2]) - int(s * 256)) <= 1
+
+
+def test_pow_log_exp_accuracy():
+    lib = O.load()
+    xs = np.concatenate([np.geomspace(1e-38, 1.0, 4000), np.geomspace(1.0, 1e30, 200),
+                         np.array([1e-45, 3e-42, 0.5, 0.25, 1.0])]).astype(np.float32)
+    for y in (0.25, 1.0 / 2.4, 0.015625, 0.5, 1.0, 2.0, 0.0625):
+        for x in xs:
+            got = O.powf(x, y)
+            want = float(x) ** float(np.float32(y))
+            if want < 1e-37 or want > 3.0e38:
+                continue
+            assert abs(got - want) <= 3e-6 * want, (x, y, got, want)
+    assert O.powf(0.0, 0.25) == 0.0 and O.powf(1.0, 0.3) == 1.0 and O.powf(0.7, 0.0) == 1.0
+    for x in np.geomspace(1e-30, 1e30, 500).astype(np.float32):
+        assert abs(lib.orc_log2f(x) - math.log2(float(x))) <= 2e-6 * max(1.0, abs(math.log2(float(x))))
+    for t in np.linspace(-120, 120, 1001).astype(np.float32):
+        assert abs(lib.orc_exp2f(t) - 2.0 ** float(t)) <= 2e-6 * 2.0 ** float(t)
+
+
+def test_sincos_accuracy():
+    import ctypes as C
+    lib = O.load()
+    s, c = C.c_float(), C.c_float()
+    for phi in np.linspace(-math.pi / 4, math.pi / 4, 2001).astype(np.float32):
+        lib.orc_sincos(phi, C.byref(s), C.byref(c))
+        assert abs(s.value - math.sin(float(phi))) < 2e-7
+        assert abs(c.value - math.cos(float(phi))) < 2e-7
+
+
+def test_oracle_render_invariants():
+    import pmdas_gb300 as P
+    W = H = 32
+    sc = P.Scene(P.SCENE_DISCS_MB, 3, 16, W, H, W, H).export()
+    px, n, l, passes, t, _ = O.render(3, 1, 3, 4, 0.25, W, H, 8 * W * H, 60000, sc, W, H, threads=2)
+    assert n >= 8 * W * H and passes > 0
+    assert np.all(np.isfinite(px)) and px[..., :3].min() >= 0.0 and px[..., :3].max() <= 1.0 + 1e-5
