@@ -183,8 +183,8 @@ def test_reference_build_matches_reference_kernels(cuda, refgrid_cls, case):
 
 # ---- edge cases ------------------------------------------------------------------
 def test_capacity_is_an_error_not_an_overrun(cuda):
-    # initial grid alone does not fit
-    g = P.KDGrid(3, 1000, 4, 1, 2, 0.25, 16, 16)
+    # initial grid alone (128 leaves, 512 samples) does not fit
+    g = P.KDGrid(3, 500, 4, 1, 2, 0.25, 16, 16)
     with pytest.raises(N.MdasError) as e:
         g.InitialSampling()
     assert e.value.status == N.MDAS_ERR_CAPACITY
