@@ -107,12 +107,16 @@ def stage_bytes(D: int, W: int, H: int, L0: int, passes: list, N_final: int, L_f
     """Algorithmic (compulsory) DRAM bytes of each stage over one render.
 
     init     : per initial leaf 4 samples * D floats + node 16 + box 8D + error 4 + seed 4 = 24D + 24
-    errors   : error read 4 per leaf; per recomputed leaf error write 4 + node 16 + box 8D
-               + its sample values (12 B each; 4 per leaf on the first pass, 5 per split pair after)
-    adaptive : error + seed read and seed write, 12 per leaf; per accepted leaf node 16 + box 8D +
-               new coordinate 4D + node write 16 (append) + 4D per gathered sample coordinate;
-               per split: left + right node 32 + left box coordinate 4 + right box 8D +
-               two errors 8 + right seed 4, minus the append's node write
+    errors   : first pass (every leaf): error read 4 per leaf; later passes visit only the split
+               children: dirty-list entry 4 per split + error read 4 per child; per recomputed
+               leaf error write 4 + node 16 + box 8D + its sample values (12 B each; 4 per leaf
+               on the first pass, 5 per split pair after)
+    adaptive : error + seed read and seed write, 12 per leaf; per accepted leaf: its node 16
+               (decide), its entry in the accepted list written and read 16, node + box
+               16 + 8D, new coordinate 4D, 4D per sample coordinate it holds (its private
+               copy); per append: node 16 + the new coordinate in the private copy 4D;
+               per split: left node 16 + left mx 4 + left copy 8D + right node + box
+               16 + 8D + right copy 12D + two errors 8 + right seed 4 + dirty entry 4
     integrate: per leaf node 16 + box 8D, 12 per sample value, pixels cleared and written 32 per pixel
     """
     init = L0 * (24 * D + 24)
@@ -120,11 +124,31 @@ def stage_bytes(D: int, W: int, H: int, L0: int, passes: list, N_final: int, L_f
     for k, p in enumerate(passes):
         L, R = p["L"], p["recomputed"]
         V = 4 * R if k == 0 else (5 * R) // 2
-        err += 4 * L + R * (4 + 16 + 8 * D) + 12 * V
+        scan = 4 * L if k == 0 else 4 * R + 2 * R
+        err += scan + R * (4 + 16 + 8 * D) + 12 * V
         S, P, G = p["selected"], p["splits"], p["gathered"]
-        adap += 12 * L + S * (16 + 8 * D + 4 * D + 16) + 4 * D * G + P * (48 + 8 * D - 16)
+        adap += 12 * L + S * (48 + 12 * D) + 4 * D * G + (S - P) * (16 + 4 * D) + P * (52 + 28 * D)
     integ = L_final * (16 + 8 * D) + 12 * N_final + 32 * W * H
     return {"init": init, "errors": err, "adaptive": adap, "integrate": integ}
+
+
+# ---- replicas ------------------------------------------------------------------------
+def replica_seed(base_seed: int, rank: int) -> int:
+    """Scene seed of a rank: each replica renders its own image (no data exchange)."""
+    return base_seed + rank
+
+
+def reduce_across_ranks(mdas_ms: float, wall_ms: float, samples: int, world: int, device: str):
+    """Job time = max over ranks (each rank's own device time), work = sum over ranks."""
+    if world <= 1:
+        return mdas_ms, wall_ms, samples
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([mdas_ms, wall_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    s = torch.tensor([float(samples)], dtype=torch.float64, device=device)
+    dist.all_reduce(s)
+    return float(t[0].item()), float(t[1].item()), int(s.item())
 
 
 # ---- the GB300 arm ------------------------------------------------------------------
@@ -141,7 +165,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     grid = P.KDGrid(D, wl.maxSamples, wl.candidatesNum, wl.bitsPerDim, wl.extraImgBits, wl.alpha, wl.scaleX,
                     wl.scaleY, arith=P.ARITH_REFERENCE)
     # replicas: each rank renders its own scene (independent images, no exchange)
-    scene = P.Scene(wl.scene_kind, wl.scene_seed + rank, wl.scene_count, wl.scaleX, wl.scaleY, W, H)
+    scene = P.Scene(wl.scene_kind, replica_seed(wl.scene_seed, rank), wl.scene_count, wl.scaleX, wl.scaleY, W, H)
     pixels = torch.zeros(H, W, 4, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
     grid.set_timing(True)
@@ -197,21 +221,14 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     mdas_ms = sum(stage_ms[:4])
     n_final, l_final, L0, passes = results[0]
     total_samples = sum(r[0] for r in results)
-    # max over ranks of the time, sum of the work
-    if world > 1:
-        t = torch.tensor([mdas_ms, wall_ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        mdas_ms, wall_ms = t.tolist()
-        s = torch.tensor([total_samples], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(s)
-        total_samples = int(s.item())
+    mdas_ms, wall_ms, total_samples = reduce_across_ranks(mdas_ms, wall_ms, total_samples, world, "cuda")
     value = total_samples / (mdas_ms / 1e3) / 1e6
 
     # roofline of the dominant kernel
     by = stage_bytes(D, W, H, L0, passes, n_final, l_final)
     names = ["init", "errors", "adaptive", "integrate"]
     dom = max(range(4), key=lambda i: stage_ms[i])
-    launches_of = {0: 1, 1: len(passes), 2: len(passes), 3: 1}[dom]
+    launches_of = {0: 1, 1: len(passes), 2: len(passes), 3: 1}[dom]  # adaptive: decide + scan + place per pass
     per_launch_bytes = by[names[dom]] / max(launches_of, 1)
     per_launch_ms = stage_ms[dom] / args.steps / max(launches_of, 1)
     peaks = {}

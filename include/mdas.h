@@ -34,7 +34,7 @@ typedef struct mdas_scene mdas_scene;
 #define MDAS_OK 0
 #define MDAS_ERR_INVALID 1   /* bad argument or configuration */
 #define MDAS_ERR_CUDA 2      /* a CUDA call failed */
-#define MDAS_ERR_CAPACITY 3  /* a pass could write past maxSamples / 2*maxSamples-1 leaves */
+#define MDAS_ERR_CAPACITY 3  /* a pass could write past maxSamples samples */
 #define MDAS_ERR_TIMEOUT 4   /* a bounded device-side wait gave up */
 #define MDAS_ERR_ALLOC 5     /* device or host allocation failed */
 #define MDAS_ERR_STATE 6     /* call out of order (e.g. a pass before InitialSampling) */
@@ -73,7 +73,7 @@ int mdas_compute_errors(mdas_grid* g);
 
 /* Replaces KDGrid::AdaptiveSampling (kdgrid.cu:718-773).  Returns
  * MDAS_ERR_CAPACITY instead of writing out of bounds when N + L > maxSamples
- * or 2L > 2*maxSamples-1. */
+ * (the pass could add one sample per leaf). */
 int mdas_adaptive_sampling(mdas_grid* g);
 
 /* Replaces KDGrid::SamplingPass (kdgrid.cu:775-779). */

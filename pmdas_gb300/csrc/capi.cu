@@ -31,6 +31,7 @@ __global__ void k_set_counts(MdasCounts* c, int N, int L) {
     c->selected = 0;
     c->passes = 0;
     c->gathered = 0u;
+    c->gerrNext = 0u;
 }
 
 struct PendingTiming {
@@ -46,9 +47,14 @@ struct mdas_grid {
     cudaStream_t stream = nullptr;
     int device = 0;
     int numSMs = 1;
-    int occ[4] = {1, 1, 1, 1};
+    int occ[5] = {1, 1, 1, 1, 1};
     int N = 0, L = 0, newN = 0, newL = 0;
     bool initialized = false;
+    // errorsClean: every leaf error is >= 0 (an errors pass ran since the last change).
+    // dirtyValid: the last adaptive pass ran on a clean state, so the leaves needing an
+    // error are exactly its split children and the next errors pass can visit only those.
+    bool errorsClean = false;
+    bool dirtyValid = false;
     MdasCounts* hcounts = nullptr;  // pinned mirror of the device counters
     std::ofstream* log = nullptr;
     bool timing = false;
@@ -121,13 +127,13 @@ cudaError_t launch_initial(mdas_grid* g, int L) {
     return g->arith == MDAS_ARITH_IEEE ? mdas_ieee::initial_sampling(g->dg, L, g->stream)
                                        : mdas_fast::initial_sampling(g->dg, L, g->stream);
 }
-cudaError_t launch_errors(mdas_grid* g, int grid) {
-    return g->arith == MDAS_ARITH_IEEE ? mdas_ieee::compute_errors(g->dg, grid, g->stream)
-                                       : mdas_fast::compute_errors(g->dg, grid, g->stream);
+cudaError_t launch_errors(mdas_grid* g, int grid, bool dirty) {
+    return g->arith == MDAS_ARITH_IEEE ? mdas_ieee::compute_errors(g->dg, grid, dirty, g->stream)
+                                       : mdas_fast::compute_errors(g->dg, grid, dirty, g->stream);
 }
-cudaError_t launch_adaptive(mdas_grid* g, int grid) {
-    return g->arith == MDAS_ARITH_IEEE ? mdas_ieee::adaptive_sampling(g->dg, grid, g->stream)
-                                       : mdas_fast::adaptive_sampling(g->dg, grid, g->stream);
+cudaError_t launch_adaptive(mdas_grid* g, int gridDecide, int gridPlace) {
+    return g->arith == MDAS_ARITH_IEEE ? mdas_ieee::adaptive_sampling(g->dg, gridDecide, gridPlace, g->stream)
+                                       : mdas_fast::adaptive_sampling(g->dg, gridDecide, gridPlace, g->stream);
 }
 cudaError_t launch_integrate(mdas_grid* g, int grid, float* pixels, int W, int H) {
     return g->arith == MDAS_ARITH_IEEE ? mdas_ieee::integrate(g->dg, grid, pixels, W, H, g->stream)
@@ -161,13 +167,16 @@ void free_grid(mdas_grid* g) {
     for (cudaEvent_t e : g->eventPool) cudaEventDestroy(e);
     cudaFree(g->dg.coords);
     cudaFree(g->dg.values);
-    cudaFree(g->dg.nodes);
-    cudaFree(g->dg.boxes);
+    cudaFree(g->dg.nb);
+    cudaFree(g->dg.lsc);
     cudaFree(g->dg.errors);
     cudaFree(g->dg.seeds);
     cudaFree(g->dg.counts);
     cudaFree(g->dg.ctl);
-    cudaFree(g->dg.tiles);
+    cudaFree(g->dg.tileCounts);
+    cudaFree(g->dg.tilePrefix);
+    cudaFree(g->dg.accepted);
+    cudaFree(g->dg.dirty);
     if (g->scratch) cudaFree(g->scratch);
     if (g->hcounts) cudaFreeHost(g->hcounts);
     delete g->log;
@@ -222,13 +231,17 @@ int mdas_create_ex(mdas_grid** out, int dim, int maxSamples, int candidatesNum, 
         delete g;
         return MDAS_ERR_CUDA;
     }
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < 5; ++k)
         g->occ[k] = arith == MDAS_ARITH_IEEE ? mdas_ieee::max_blocks_per_sm(dim, k) : mdas_fast::max_blocks_per_sm(dim, k);
 
     MdasDeviceGrid& d = g->dg;
     d.D = dim;
     d.maxSamples = maxSamples;
-    d.maxNodes = 2 * maxSamples - 1;  // kdgrid.cu:627-629
+    // every leaf holds at least 2 samples (initial leaves 4, split children 2 and 3),
+    // so L <= N/2 and maxSamples/2 + 1 leaf slots always suffice (the reference
+    // allocates 2 * maxSamples - 1, kdgrid.cu:627-629)
+    d.maxNodes = maxSamples / 2 + 1;
+    d.nbFloats = mdas_fast::record_floats(dim);
     d.candidatesNum = candidatesNum;
     d.maxNodeSize = 4;                // kdgrid.cu:611
     d.bitsPerDim = bitsPerDim;
@@ -240,18 +253,20 @@ int mdas_create_ex(mdas_grid** out, int dim, int maxSamples, int candidatesNum, 
     const size_t capSamples = ((size_t)maxSamples + 127) / 128 * 128;  // roundUp(maxSamples, 128), kdgrid.cu:625-626
     bool ok = cudaMalloc(&d.coords, sizeof(float) * capSamples * dim) == cudaSuccess &&
               cudaMalloc(&d.values, sizeof(float) * 3 * capSamples) == cudaSuccess &&
-              cudaMalloc(&d.nodes, sizeof(int4) * (size_t)d.maxNodes) == cudaSuccess &&
-              cudaMalloc(&d.boxes, sizeof(float) * 2 * dim * (size_t)d.maxNodes) == cudaSuccess &&
+              cudaMalloc(&d.nb, sizeof(float) * (size_t)d.nbFloats * (size_t)d.maxNodes) == cudaSuccess &&
+              cudaMalloc(&d.lsc, sizeof(float) * 4 * dim * (size_t)d.maxNodes) == cudaSuccess &&
               cudaMalloc(&d.errors, sizeof(float) * (size_t)d.maxNodes) == cudaSuccess &&
               cudaMalloc(&d.seeds, sizeof(unsigned) * (size_t)d.maxNodes) == cudaSuccess &&
               cudaMalloc(&d.counts, sizeof(MdasCounts)) == cudaSuccess &&
               cudaMalloc(&d.ctl, sizeof(MdasCtl)) == cudaSuccess &&
-              cudaMalloc(&d.tiles, sizeof(unsigned long long) * (size_t)d.maxTiles) == cudaSuccess &&
+              cudaMalloc(&d.tileCounts, sizeof(uint2) * (size_t)d.maxTiles) == cudaSuccess &&
+              cudaMalloc(&d.tilePrefix, sizeof(uint2) * (size_t)d.maxTiles) == cudaSuccess &&
+              cudaMalloc(&d.accepted, sizeof(uint2) * (size_t)d.maxTiles * MDAS_TILE_LEAVES) == cudaSuccess &&
+              cudaMalloc(&d.dirty, sizeof(int) * ((size_t)d.maxNodes / 2 + 1)) == cudaSuccess &&
               cudaMallocHost(&g->hcounts, sizeof(MdasCounts)) == cudaSuccess;
     if (ok) {
         ok = cudaMemset(d.counts, 0, sizeof(MdasCounts)) == cudaSuccess &&
              cudaMemset(d.ctl, 0, sizeof(MdasCtl)) == cudaSuccess &&
-             cudaMemset(d.tiles, 0, sizeof(unsigned long long) * (size_t)d.maxTiles) == cudaSuccess &&
              cudaDeviceSynchronize() == cudaSuccess;
     }
     if (!ok) {
@@ -312,6 +327,8 @@ int mdas_initial_sampling(mdas_grid* g) {
     g->newN = 0;
     g->newL = 0;
     g->initialized = true;
+    g->errorsClean = false;
+    g->dirtyValid = false;
     if (g->log) {
         const double t = last_stage_ms(g, 0);
         *g->log << "INITIAL SAMPLES\n" << g->N << std::endl;
@@ -323,10 +340,12 @@ int mdas_initial_sampling(mdas_grid* g) {
 int mdas_compute_errors(mdas_grid* g) {
     if (!g) return MDAS_ERR_INVALID;
     if (!g->initialized) return MDAS_ERR_STATE;
-    const int grid = grid_for(g, MDAS_K_ERRORS, g->L);
-    int rc = timed(g, 1, [&]() { return launch_errors(g, grid); });
+    const bool dirty = g->dirtyValid;
+    const int grid = grid_for(g, MDAS_K_ERRORS, dirty ? 2 * (int64_t)g->newL : (int64_t)g->L);
+    int rc = timed(g, 1, [&]() { return launch_errors(g, grid, dirty); });
     g->launches += 1;
     if (rc) return rc;
+    g->errorsClean = true;
     if (g->log) *g->log << "COMPUTE ERRORS TIME\n" << last_stage_ms(g, 1) << std::endl;
     return MDAS_OK;
 }
@@ -334,11 +353,17 @@ int mdas_compute_errors(mdas_grid* g) {
 int mdas_adaptive_sampling(mdas_grid* g) {
     if (!g) return MDAS_ERR_INVALID;
     if (!g->initialized) return MDAS_ERR_STATE;
-    // a pass adds at most one sample and one leaf per leaf
-    if ((int64_t)g->N + g->L > g->dg.maxSamples || 2 * (int64_t)g->L > g->dg.maxNodes) return MDAS_ERR_CAPACITY;
-    const int grid = grid_for(g, MDAS_K_ADAPTIVE, g->L);
-    int rc = timed(g, 2, [&]() { return launch_adaptive(g, grid); });
-    g->launches += 1;
+    // A pass adds at most one sample per leaf.  Leaves then still hold >= 2 samples
+    // each, so the leaf count stays <= (N + L) / 2 <= maxSamples / 2 < maxNodes.
+    if ((int64_t)g->N + g->L > g->dg.maxSamples) return MDAS_ERR_CAPACITY;
+    // one CTA iteration per tile of MDAS_TILE_LEAVES leaves
+    const int64_t tiles = ((int64_t)g->L + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
+    const int gridDecide = grid_for(g, MDAS_K_DECIDE, tiles * 256);
+    const int gridPlace = grid_for(g, MDAS_K_ADAPTIVE, tiles * 256);
+    int rc = timed(g, 2, [&]() { return launch_adaptive(g, gridDecide, gridPlace); });
+    g->dirtyValid = g->errorsClean;
+    g->errorsClean = false;
+    g->launches += 3;
     if (rc) return rc;
     rc = read_counts(g);
     if (g->log) {
@@ -447,11 +472,25 @@ int mdas_dump_state(mdas_grid* g, float* coords, float* values, int* nodes, floa
     };
     cp(coords, d.coords, sizeof(float) * N * d.D);
     cp(values, d.values, sizeof(float) * 3 * N);
-    cp(nodes, d.nodes, sizeof(int4) * L);
-    cp(boxes, d.boxes, sizeof(float) * 2 * d.D * L);
     cp(errors, d.errors, sizeof(float) * L);
     cp(seeds, d.seeds, sizeof(unsigned) * L);
+    // nodes and boxes live inside the leaf records: unpack into a staging buffer
+    void* stage = nullptr;
+    if ((nodes || boxes) && L && e == cudaSuccess) {
+        const size_t nb = sizeof(int4) * L, bb = sizeof(float) * 2 * d.D * L;
+        e = cudaMalloc(&stage, nb + bb);
+        if (e == cudaSuccess) {
+            int* dn = reinterpret_cast<int*>(stage);
+            float* db = reinterpret_cast<float*>(reinterpret_cast<char*>(stage) + nb);
+            e = g->arith == MDAS_ARITH_IEEE ? mdas_ieee::unpack_records(d, (int)L, dn, db, g->stream)
+                                            : mdas_fast::unpack_records(d, (int)L, dn, db, g->stream);
+            g->launches += 1;
+            cp(nodes, dn, nb);
+            cp(boxes, db, bb);
+        }
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (stage) cudaFree(stage);
     return status_of(e);
 }
 
@@ -468,10 +507,26 @@ int mdas_load_state(mdas_grid* g, int numberOfSamples, int numberOfNodes, const 
     };
     cp(d.coords, coords, sizeof(float) * N * d.D);
     cp(d.values, values, sizeof(float) * 3 * N);
-    cp(d.nodes, nodes, sizeof(int4) * L);
-    cp(d.boxes, boxes, sizeof(float) * 2 * d.D * L);
     cp(d.errors, errors, sizeof(float) * L);
     cp(d.seeds, seeds, sizeof(unsigned) * L);
+    // build the leaf records from the nodes, boxes and (already loaded) coordinates
+    void* stage = nullptr;
+    if (L && e == cudaSuccess) {
+        for (size_t k = 0; k < 4 * L; ++k)
+            if (nodes[k] >= (int)N) return MDAS_ERR_INVALID;  // a node names a sample that does not exist
+        const size_t nb = sizeof(int4) * L, bb = sizeof(float) * 2 * d.D * L;
+        e = cudaMalloc(&stage, nb + bb);
+        if (e == cudaSuccess) {
+            int* dn = reinterpret_cast<int*>(stage);
+            float* db = reinterpret_cast<float*>(reinterpret_cast<char*>(stage) + nb);
+            cp(dn, nodes, nb);
+            cp(db, boxes, bb);
+            if (e == cudaSuccess)
+                e = g->arith == MDAS_ARITH_IEEE ? mdas_ieee::pack_records(d, (int)L, dn, db, g->stream)
+                                                : mdas_fast::pack_records(d, (int)L, dn, db, g->stream);
+            g->launches += 1;
+        }
+    }
     if (e == cudaSuccess && (size_t)d.maxNodes > L)
         e = cudaMemsetAsync(d.seeds + L, 0, sizeof(unsigned) * ((size_t)d.maxNodes - L), g->stream);
     if (e == cudaSuccess) {
@@ -480,12 +535,15 @@ int mdas_load_state(mdas_grid* g, int numberOfSamples, int numberOfNodes, const 
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);  // host buffers may go away after return
+    if (stage) cudaFree(stage);
     if (e != cudaSuccess) return MDAS_ERR_CUDA;
     g->N = (int)N;
     g->L = (int)L;
     g->newN = 0;
     g->newL = 0;
     g->initialized = true;
+    g->errorsClean = false;
+    g->dirtyValid = false;
     return MDAS_OK;
 }
 
@@ -642,7 +700,7 @@ int mdas_render(mdas_grid* g, mdas_scene* s, int budget, float* pixels, int widt
     if (rc) return rc;
     int passes = 0;
     while (g->N < budget) {
-        if ((int64_t)g->N + g->L > g->dg.maxSamples || 2 * (int64_t)g->L > g->dg.maxNodes) break;
+        if ((int64_t)g->N + g->L > g->dg.maxSamples) break;
         rc = mdas_sampling_pass(g);
         if (rc) return rc;
         rc = mdas_evaluate(g, s, g->N - g->newN, g->newN);

@@ -18,14 +18,15 @@ struct MdasCounts {
     int selected;    // leaves selected by the last adaptive pass (== newN)
     int passes;      // adaptive passes since the initial sampling
     unsigned gathered;  // sample coordinates read by the last adaptive pass
-    int pad[2];
+    unsigned gerrNext;  // max error of the leaves the last adaptive pass did not split (reset with gathered)
+    int pad;
 };
 
-// Per-launch scratch of the persistent kernels: tile tickets and exit counter.
+// Scratch of one adaptive pass: the counts before it, for the place kernel.
 struct MdasCtl {
-    unsigned ticket;
-    unsigned done;
-    unsigned pad[2];
+    int N0;
+    int L0;
+    int pad[2];
 };
 
 struct MdasDeviceGrid {
@@ -41,22 +42,23 @@ struct MdasDeviceGrid {
     float scaleY;
     float* coords;        // [capSamples * D], AoS like the reference's Point buffer
     float* values;        // [capSamples * 3], float3
-    int4* nodes;          // [maxNodes], 4 sample indices, ~D = empty
-    float* boxes;         // [maxNodes * 2D], mn[D] then mx[D]
+    float* nb;            // [maxNodes * nbFloats], per leaf: node (4 sample indices) + box
+    int nbFloats;         // floats per node + box record
+    float* lsc;           // [maxNodes * 4D], per leaf: coordinates of its samples in node-slot order
     float* errors;        // [maxNodes], < 0 = needs recomputation
     unsigned* seeds;      // [maxNodes], 0 = not drawn yet
     MdasCounts* counts;   // device counters
-    MdasCtl* ctl;         // persistent-kernel scratch
-    unsigned long long* tiles;  // decoupled look-back tile states, one per 256 leaves
+    MdasCtl* ctl;         // per-pass scratch
+    uint2* tileCounts;    // [maxTiles] (accepted, split) per tile of MDAS_TILE_LEAVES leaves
+    uint2* tilePrefix;    // [maxTiles] exclusive prefix of tileCounts
+    uint2* accepted;      // [maxTiles * MDAS_TILE_LEAVES] accepted leaves, compacted per tile
     int maxTiles;
+    int* dirty;           // [maxNodes/2 + 1], slots of the left children of the last pass's splits
 };
 
-// Decoupled look-back tile state: [63:62] status, [61:31] split count, [30:0] selected count.
-#define MDAS_TILE_AGG 1ull
-#define MDAS_TILE_INC 2ull
-#define MDAS_TILE_LEAVES 256
-// Spin limit of the look-back wait; on expiry the kernel records MDAS_ERR_TIMEOUT and moves on.
-#define MDAS_SPIN_LIMIT (1u << 22)
+// Leaves per thread and per tile of the adaptive pass.
+#define MDAS_LEAVES_PER_THREAD 4
+#define MDAS_TILE_LEAVES (256 * MDAS_LEAVES_PER_THREAD)
 
 #define MDAS_OK 0
 #define MDAS_ERR_INVALID 1
@@ -70,15 +72,19 @@ struct MdasDeviceGrid {
 #define MDAS_DECLARE_LAUNCHERS(NS)                                                                          \
     namespace NS {                                                                                          \
     cudaError_t initial_sampling(const MdasDeviceGrid& g, int L, cudaStream_t s);                           \
-    cudaError_t compute_errors(const MdasDeviceGrid& g, int grid, cudaStream_t s);                          \
-    cudaError_t adaptive_sampling(const MdasDeviceGrid& g, int grid, cudaStream_t s);                       \
+    cudaError_t compute_errors(const MdasDeviceGrid& g, int grid, bool dirty, cudaStream_t s);              \
+    cudaError_t adaptive_sampling(const MdasDeviceGrid& g, int gridDecide, int gridPlace, cudaStream_t s);  \
     cudaError_t integrate(const MdasDeviceGrid& g, int grid, float* pixels, int W, int H, cudaStream_t s);  \
     cudaError_t convert_to_bytes(const float* pixels, unsigned char* bytes, int P, cudaStream_t s);         \
     cudaError_t sampling_density(const MdasDeviceGrid& g, float* pixels, int W, int H, cudaStream_t s);     \
+    cudaError_t unpack_records(const MdasDeviceGrid& g, int L, int* nodes, float* boxes, cudaStream_t s);   \
+    cudaError_t pack_records(const MdasDeviceGrid& g, int L, const int* nodes, const float* boxes,          \
+                             cudaStream_t s);                                                               \
+    int record_floats(int D);                                                                               \
     int max_blocks_per_sm(int D, int which);                                                                \
     }
 
 MDAS_DECLARE_LAUNCHERS(mdas_fast)
 MDAS_DECLARE_LAUNCHERS(mdas_ieee)
 
-enum { MDAS_K_INIT = 0, MDAS_K_ERRORS = 1, MDAS_K_ADAPTIVE = 2, MDAS_K_INTEGRATE = 3 };
+enum { MDAS_K_INIT = 0, MDAS_K_ERRORS = 1, MDAS_K_ADAPTIVE = 2, MDAS_K_INTEGRATE = 3, MDAS_K_DECIDE = 4 };

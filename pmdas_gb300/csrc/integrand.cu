@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <math.h>
+#include <algorithm>
 #include <vector>
 #include "integrand.h"
 #include "grid_types.h"
@@ -125,6 +126,18 @@ int mdas_generate_scene(int kind, uint64_t seed, int count, float scaleX, float 
                 q[6] = q[2] / sc->focalDistance;
                 q[7] = q[3] * q[3];
             }
+            // list by increasing depth (stable), so that shading can stop at the first cover
+            std::vector<float> sorted(prims->size());
+            std::vector<int> order(count);
+            for (int k = 0; k < count; ++k) order[k] = k;
+            std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+                return p[MDAS_PRIM_STRIDE * a + 2] < p[MDAS_PRIM_STRIDE * b + 2];
+            });
+            for (int k = 0; k < count; ++k)
+                for (int f = 0; f < MDAS_PRIM_STRIDE; ++f)
+                    sorted[MDAS_PRIM_STRIDE * k + f] = p[MDAS_PRIM_STRIDE * order[k] + f];
+            *prims = sorted;
+            p = prims->data();
             if (kind == MDAS_SCENE_DISCS_MBDOF) {
                 for (int k = 0; k < count; ++k) {
                     float* q = p + MDAS_PRIM_STRIDE * k;

@@ -26,7 +26,8 @@ extern "C" {
 #define MDAS_SCENE_DIRECT_LIGHT 3  // (x, y, u, v): ground + spheres lit by a rectangular light
 #endif
 
-// Floats per primitive.  Discs: [cx, cy, z, r, vx, vy, z/focal, r*r, R, G, B, 0].
+// Floats per primitive.  Discs: [cx, cy, z, r, vx, vy, z/focal, r*r, R, G, B, 0];
+// depth-of-field scenes list their discs by increasing depth (stable order).
 // Spheres: [cx, cy, cz, r, 0, 0, 1/r, r*r, 0, 0, 0, 0].
 #define MDAS_PRIM_STRIDE 12
 
@@ -87,14 +88,16 @@ MDAS_HD void mdas_shade_discs_mb(const MdasScene* sc, const float* prims, const 
     const float py = c[1] / sc->scaleY;
     const float t = c[2];
     float R = sc->background, G = sc->background, B = sc->background;
-    for (int k = 0; k < sc->count; ++k) {
+    // the last listed covering disc wins: scan from the back, stop at the first cover
+    for (int k = sc->count - 1; k >= 0; --k) {
         const float* p = prims + MDAS_PRIM_STRIDE * k;
         const float dx = px - mdas_fma(p[4], t, p[0]);
         const float dy = py - mdas_fma(p[5], t, p[1]);
-        if (mdas_fma(dx, dx, dy * dy) <= p[7]) {  // the last listed covering disc wins
+        if (mdas_fma(dx, dx, dy * dy) <= p[7]) {
             R = p[8];
             G = p[9];
             B = p[10];
+            break;
         }
     }
     out[0] = R;
@@ -106,7 +109,9 @@ MDAS_HD void mdas_shade_discs_mb(const MdasScene* sc, const float* prims, const 
 // the pinhole ray through the film point meets the focal plane at
 // focal * (nx * filmHalfW, ny * filmHalfH, 1); the lens ray starts at the lens
 // sample and passes through that point.  All discs are fronto-parallel, so the
-// nearest hit is the covering disc with the smallest depth.
+// nearest hit is the covering disc with the smallest depth (the first listed
+// among equal depths).  Scenes keep their discs sorted by depth (stable), so
+// the first covering disc in list order is that hit.
 MDAS_HD void mdas_shade_discs_dof(const MdasScene* sc, const float* prims, const float* c, int moving,
                                   float* out) {
     const float px = c[0] / sc->scaleX;
@@ -120,7 +125,6 @@ MDAS_HD void mdas_shade_discs_dof(const MdasScene* sc, const float* prims, const
     mdas_concentric(u, v, sc->lensRadius, &lx, &ly);
     const float wx = sc->focalDistance * (nx * sc->filmHalfW) - lx;
     const float wy = sc->focalDistance * (ny * sc->filmHalfH) - ly;
-    float bestZ = 3.0e38f;
     float R = sc->background, G = sc->background, B = sc->background;
     for (int k = 0; k < sc->count; ++k) {
         const float* p = prims + MDAS_PRIM_STRIDE * k;
@@ -130,11 +134,11 @@ MDAS_HD void mdas_shade_discs_dof(const MdasScene* sc, const float* prims, const
         const float cy = moving ? mdas_fma(p[5], t, p[1]) : p[1];
         const float dx = hx - cx;
         const float dy = hy - cy;
-        if (mdas_fma(dx, dx, dy * dy) <= p[7] && p[2] < bestZ) {
-            bestZ = p[2];
+        if (mdas_fma(dx, dx, dy * dy) <= p[7]) {
             R = p[8];
             G = p[9];
             B = p[10];
+            break;
         }
     }
     out[0] = R;

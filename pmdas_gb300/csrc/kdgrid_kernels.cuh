@@ -14,14 +14,19 @@
 // computes in the respective arithmetic.
 //
 // What differs from the reference is the execution design, not the results:
-//   * one pass over the leaves per stage with persistent CTAs that read the
-//     leaf and sample counts from device memory (no host round trip needed);
-//   * new sample and leaf slots come from a single-pass decoupled look-back scan
-//     over the selection/split flags in leaf order (deterministic), not from
-//     warp-aggregated atomics (kdgrid.cu:366-378, 428-440);
-//   * stores of the initial samples are staged in shared memory and written
-//     out as contiguous 16-byte vectors; the split writes only the one
-//     coordinate of the left box that changes;
+//   * each leaf keeps a private copy of its sample coordinates (`lsc`, 4 x D
+//     floats, contiguous) beside its node + box record (`nb`), so that an
+//     accepted leaf costs two DRAM bursts instead of one random gather per
+//     sample; the sample buffers the integrand reads and writes keep the
+//     reference's AoS layout;
+//   * kernels read the leaf and sample counts from device memory (no host round
+//     trip is needed inside a pass);
+//   * new sample and leaf slots come from a scan over the acceptance/split flags
+//     in leaf order (deterministic): decide (per-tile counts + a compacted list
+//     of accepted leaves), scan (one CTA over the tile counts), place (one
+//     thread per accepted leaf) — instead of warp-aggregated atomics
+//     (kdgrid.cu:366-378, 428-440);
+//   * the errors pass after an adaptive pass visits only the split children;
 //   * pixel accumulation uses one 16-byte vector atomic per pixel instead of
 //     three scalar ones.
 #pragma once
@@ -64,67 +69,91 @@ __device__ __forceinline__ unsigned lcg(unsigned& prev) {
 
 __device__ __forceinline__ float rnd(unsigned& prev) { return (float)lcg(prev) / (float)0x01000000; }
 
-// ---- small vector helpers -----------------------------------------------------
-template <int D>
-__device__ __forceinline__ void load_point(const float* __restrict__ p, float (&out)[D]) {
-    if constexpr (D == 4) {
-        const float4 v = *reinterpret_cast<const float4*>(p);
-        out[0] = v.x; out[1] = v.y; out[2] = v.z; out[3] = v.w;
-    } else if constexpr (D == 6) {
-        const float2 a = *reinterpret_cast<const float2*>(p);
-        const float2 b = *reinterpret_cast<const float2*>(p + 2);
-        const float2 c = *reinterpret_cast<const float2*>(p + 4);
-        out[0] = a.x; out[1] = a.y; out[2] = b.x; out[3] = b.y; out[4] = c.x; out[5] = c.y;
-    } else {
+// ---- vector loads and stores of NF floats from a 16-byte aligned address ---------
+template <int NF>
+__device__ __forceinline__ void ld_floats(const float* __restrict__ p, float (&out)[NF]) {
 #pragma unroll
-        for (int i = 0; i < D; ++i) out[i] = p[i];
+    for (int k = 0; k + 4 <= NF; k += 4) {
+        const float4 v = *reinterpret_cast<const float4*>(p + k);
+        out[k] = v.x; out[k + 1] = v.y; out[k + 2] = v.z; out[k + 3] = v.w;
     }
+    constexpr int base = NF - NF % 4;
+    if constexpr (NF % 4 >= 2) {
+        const float2 v = *reinterpret_cast<const float2*>(p + base);
+        out[base] = v.x; out[base + 1] = v.y;
+    }
+    if constexpr (NF % 2) out[NF - 1] = p[NF - 1];
 }
 
+template <int NF>
+__device__ __forceinline__ void st_floats(float* __restrict__ p, const float (&v)[NF]) {
+#pragma unroll
+    for (int k = 0; k + 4 <= NF; k += 4)
+        *reinterpret_cast<float4*>(p + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+    constexpr int base = NF - NF % 4;
+    if constexpr (NF % 4 >= 2) *reinterpret_cast<float2*>(p + base) = make_float2(v[base], v[base + 1]);
+    if constexpr (NF % 2) p[NF - 1] = v[NF - 1];
+}
+
+// One point of D floats at an address aligned to its natural vector (16 B for D=4,
+// 8 B for even D, 4 B otherwise).
 template <int D>
 __device__ __forceinline__ void store_point(float* __restrict__ p, const float (&v)[D]) {
     if constexpr (D == 4) {
         *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
-    } else if constexpr (D == 6) {
-        *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
-        *reinterpret_cast<float2*>(p + 2) = make_float2(v[2], v[3]);
-        *reinterpret_cast<float2*>(p + 4) = make_float2(v[4], v[5]);
+    } else if constexpr (D % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < D; i += 2) *reinterpret_cast<float2*>(p + i) = make_float2(v[i], v[i + 1]);
     } else {
 #pragma unroll
         for (int i = 0; i < D; ++i) p[i] = v[i];
     }
 }
 
-// Box = mn[D] then mx[D]; 8D bytes per leaf, 8-byte aligned for every D.
+// ---- leaf storage ------------------------------------------------------------------
+// nb:  NbLayout<D>::FLOATS floats per leaf, 16-byte aligned:
+//        [0, 4)        node: the 4 sample indices (int bits), ~D marks an empty slot
+//                      (the Node union of kdgrid.h:15-40)
+//        [4, 4+D)      box mn       [4+D, 4+2D)  box mx          (AABB, aabb.h:10-17)
+//        padding to a multiple of 4 floats
+// lsc: 4 x D floats per leaf: coordinates of the leaf's samples in node-slot order
 template <int D>
-__device__ __forceinline__ void load_box(const float* __restrict__ b, float (&mn)[D], float (&mx)[D]) {
-    if constexpr (D == 4) {
-        const float4 a = *reinterpret_cast<const float4*>(b);
-        const float4 c = *reinterpret_cast<const float4*>(b + 4);
-        mn[0] = a.x; mn[1] = a.y; mn[2] = a.z; mn[3] = a.w;
-        mx[0] = c.x; mx[1] = c.y; mx[2] = c.z; mx[3] = c.w;
-    } else {
+struct NbLayout {
+    static constexpr int BOX = 4;
+    static constexpr int FLOATS = (4 + 2 * D + 3) / 4 * 4;
+};
+
+// node and box of a leaf
+template <int D>
+__device__ __forceinline__ int4 nb_load(const float* __restrict__ nb, float (&mn)[D], float (&mx)[D]) {
+    float v[4 + 2 * D];
+    ld_floats<4 + 2 * D>(nb, v);
 #pragma unroll
-        for (int i = 0; i < D; i += 1) {
-            mn[i] = b[i];
-            mx[i] = b[D + i];
-        }
+    for (int i = 0; i < D; ++i) {
+        mn[i] = v[4 + i];
+        mx[i] = v[4 + D + i];
     }
+    return make_int4(__float_as_int(v[0]), __float_as_int(v[1]), __float_as_int(v[2]), __float_as_int(v[3]));
 }
 
 template <int D>
-__device__ __forceinline__ void store_box(float* __restrict__ b, const float (&mn)[D], const float (&mx)[D]) {
-    if constexpr (D == 4) {
-        *reinterpret_cast<float4*>(b) = make_float4(mn[0], mn[1], mn[2], mn[3]);
-        *reinterpret_cast<float4*>(b + 4) = make_float4(mx[0], mx[1], mx[2], mx[3]);
-    } else {
+__device__ __forceinline__ void nb_store(float* __restrict__ nb, int4 n, const float (&mn)[D], const float (&mx)[D]) {
+    float v[4 + 2 * D];
+    v[0] = __int_as_float(n.x);
+    v[1] = __int_as_float(n.y);
+    v[2] = __int_as_float(n.z);
+    v[3] = __int_as_float(n.w);
 #pragma unroll
-        for (int i = 0; i < D; ++i) {
-            b[i] = mn[i];
-            b[D + i] = mx[i];
-        }
+    for (int i = 0; i < D; ++i) {
+        v[4 + i] = mn[i];
+        v[4 + D + i] = mx[i];
     }
+    st_floats<4 + 2 * D>(nb, v);
 }
+
+__device__ __forceinline__ int4 nb_node(const float* __restrict__ nb) { return *reinterpret_cast<const int4*>(nb); }
+
+__device__ __forceinline__ void nb_set_node(float* __restrict__ nb, int4 n) { *reinterpret_cast<int4*>(nb) = n; }
 
 // AABB::Volume (aabb.h:20-25)
 template <int D>
@@ -159,12 +188,14 @@ __device__ __forceinline__ int node_get(const int4 n, int i) {
 // Initial stratified sampling — uniformSamplingKernel, kdgrid.cu:121-202.
 // One thread per initial cell: Morton-decode the cell index into an n-D cell
 // (bitsPerDim bits per dimension, extraImgBits more for x and y), draw 4
-// samples with the cell's tea<4>/LCG stream, write leaf, box, error -1, seed.
+// samples with the cell's tea<4>/LCG stream, write record, error -1, seed.
+// The AoS sample coordinates are staged in shared memory and written out as
+// contiguous 16-byte vectors.
 // =====================================================================================
 template <int D>
 __global__ void __launch_bounds__(256) k_initial_sampling(MdasDeviceGrid g, int L) {
+    constexpr int NB = NbLayout<D>::FLOATS;
     __shared__ __align__(16) float s_coords[256 * 4 * D];
-    __shared__ __align__(16) float s_boxes[256 * 2 * D];
     const int bpd = g.bitsPerDim, eib = g.extraImgBits;
     for (int base = blockIdx.x * 256; base < L; base += gridDim.x * 256) {
         const int nodeIndex = base + threadIdx.x;
@@ -206,32 +237,22 @@ __global__ void __launch_bounds__(256) k_initial_sampling(MdasDeviceGrid g, int 
             g.seeds[nodeIndex] = seed;
             g.errors[nodeIndex] = -1.0f;
             const int s0 = 4 * nodeIndex;
-            g.nodes[nodeIndex] = make_int4(s0, s0 + 1, s0 + 2, s0 + 3);
+            float mx[D];
 #pragma unroll
-            for (int i = 0; i < D; ++i) {
-                s_boxes[threadIdx.x * 2 * D + i] = offset[i];
-                s_boxes[threadIdx.x * 2 * D + D + i] = offset[i] + extent[i];
-            }
+            for (int i = 0; i < D; ++i) mx[i] = offset[i] + extent[i];
+            nb_store<D>(g.nb + (size_t)nodeIndex * NB, make_int4(s0, s0 + 1, s0 + 2, s0 + 3), offset, mx);
         }
         __syncthreads();
         {
-            // 4*D floats per leaf, leaf `base` starts at a 16*D-byte boundary
+            // 4*D floats per leaf, leaf `base` starts at a 16*D-byte boundary; an initial
+            // leaf's private sample copy has the same layout as its 4 AoS samples
             float4* dst = reinterpret_cast<float4*>(g.coords + (size_t)base * 4 * D);
+            float4* dsl = reinterpret_cast<float4*>(g.lsc + (size_t)base * 4 * D);
             const float4* src = reinterpret_cast<const float4*>(s_coords);
-            for (int k = threadIdx.x; k < n * D; k += 256) dst[k] = src[k];
-        }
-        {
-            // 2*D floats per leaf, leaf `base` (a multiple of 256) starts 16-byte aligned
-            const int total = n * 2 * D;
-            float* dstf = g.boxes + (size_t)base * 2 * D;
-            if ((total & 3) == 0) {
-                float4* dst = reinterpret_cast<float4*>(dstf);
-                const float4* src = reinterpret_cast<const float4*>(s_boxes);
-                for (int k = threadIdx.x; k < total / 4; k += 256) dst[k] = src[k];
-            } else {
-                float2* dst = reinterpret_cast<float2*>(dstf);
-                const float2* src = reinterpret_cast<const float2*>(s_boxes);
-                for (int k = threadIdx.x; k < total / 2; k += 256) dst[k] = src[k];
+            for (int k = threadIdx.x; k < n * D; k += 256) {
+                const float4 v = src[k];
+                dst[k] = v;
+                dsl[k] = v;
             }
         }
         __syncthreads();
@@ -243,60 +264,80 @@ __global__ void __launch_bounds__(256) k_initial_sampling(MdasDeviceGrid g, int 
 // Only leaves with error < 0 (new or just split) are recomputed; stale errors
 // of leaves that only gained a sample are kept, as in the reference.  The max
 // over all leaves goes to counts->gerr (float bits; all errors are >= 0).
+//
+// Two launch shapes with the same result:
+//   full  — every leaf (after InitialSampling or a loaded state);
+//   dirty — only the children of the last pass's splits (the left child keeps
+//           the parent's slot, listed in g.dirty; the right children are the
+//           slot range [L - newL, L)); the max over all other leaves was taken
+//           by the adaptive pass that left them unchanged (counts->gerrNext).
 // =====================================================================================
 template <int D>
+__device__ __forceinline__ float leaf_error(const MdasDeviceGrid& g, int nodeIndex) {
+    float mn[D], mx[D];
+    const int4 node = nb_load<D>(g.nb + (size_t)nodeIndex * NbLayout<D>::FLOATS, mn, mx);
+    const float volume = box_volume<D>(mn, mx);
+    float3 avg = make_float3(0.0f, 0.0f, 0.0f);
+    float3 loc[4];
+    int sampleCount = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int idx = node_get(node, i);
+        if (idx >= 0) {
+            const float* v = g.values + 3 * (size_t)idx;
+            loc[i] = make_float3(__ldg(v), __ldg(v + 1), __ldg(v + 2));
+            avg.x += loc[i].x;
+            avg.y += loc[i].y;
+            avg.z += loc[i].z;
+            sampleCount++;
+        }
+    }
+    {
+        // float3 /= float multiplies by the reciprocal (sutil/vec_math.h:492-496)
+        const float inv = 1.0f / float(sampleCount);
+        avg.x *= inv;
+        avg.y *= inv;
+        avg.z *= inv;
+    }
+    float3 diffSum = make_float3(0.0f, 0.0f, 0.0f);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (i < sampleCount) {
+            diffSum.x += fabsf(loc[i].x - avg.x);
+            diffSum.y += fabsf(loc[i].y - avg.y);
+            diffSum.z += fabsf(loc[i].z - avg.z);
+        }
+    }
+    float error = 0.0f;
+    if (avg.x != 0.0f) error += diffSum.x / avg.x;
+    if (avg.y != 0.0f) error += diffSum.y / avg.y;
+    if (avg.z != 0.0f) error += diffSum.z / avg.z;
+    error /= float(sampleCount);
+    error += 1.0e-5f;
+    error *= volume;
+    return error;
+}
+
+template <int D, bool DIRTY>
 __global__ void __launch_bounds__(256) k_compute_errors(MdasDeviceGrid g) {
     __shared__ unsigned s_max[8];
     __shared__ unsigned s_cnt[8];
-    const int L = g.counts->L;
+    int items, newL = 0, firstRight = 0;
     float maxError = 0.0f;
+    if (DIRTY) {
+        newL = g.counts->newL;
+        firstRight = g.counts->L - newL;
+        items = 2 * newL;
+        maxError = __uint_as_float(g.counts->gerrNext);
+    } else {
+        items = g.counts->L;
+    }
     unsigned recomputed = 0;
-    for (int nodeIndex = blockIdx.x * blockDim.x + threadIdx.x; nodeIndex < L;
-         nodeIndex += gridDim.x * blockDim.x) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < items; k += gridDim.x * blockDim.x) {
+        const int nodeIndex = DIRTY ? (k < newL ? g.dirty[k] : firstRight + (k - newL)) : k;
         float error = g.errors[nodeIndex];
         if (error < 0.0f) {
-            const int4 node = __ldg(g.nodes + nodeIndex);
-            float mn[D], mx[D];
-            load_box<D>(g.boxes + (size_t)nodeIndex * 2 * D, mn, mx);
-            const float volume = box_volume<D>(mn, mx);
-            float3 avg = make_float3(0.0f, 0.0f, 0.0f);
-            float3 loc[4];
-            int sampleCount = 0;
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const int idx = node_get(node, i);
-                if (idx >= 0) {
-                    const float* v = g.values + 3 * (size_t)idx;
-                    loc[i] = make_float3(__ldg(v), __ldg(v + 1), __ldg(v + 2));
-                    avg.x += loc[i].x;
-                    avg.y += loc[i].y;
-                    avg.z += loc[i].z;
-                    sampleCount++;
-                }
-            }
-            {
-                // float3 /= float multiplies by the reciprocal (sutil/vec_math.h:492-496)
-                const float inv = 1.0f / float(sampleCount);
-                avg.x *= inv;
-                avg.y *= inv;
-                avg.z *= inv;
-            }
-            float3 diffSum = make_float3(0.0f, 0.0f, 0.0f);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                if (i < sampleCount) {
-                    diffSum.x += fabsf(loc[i].x - avg.x);
-                    diffSum.y += fabsf(loc[i].y - avg.y);
-                    diffSum.z += fabsf(loc[i].z - avg.z);
-                }
-            }
-            error = 0.0f;
-            if (avg.x != 0.0f) error += diffSum.x / avg.x;
-            if (avg.y != 0.0f) error += diffSum.y / avg.y;
-            if (avg.z != 0.0f) error += diffSum.z / avg.z;
-            error /= float(sampleCount);
-            error += 1.0e-5f;
-            error *= volume;
+            error = leaf_error<D>(g, nodeIndex);
             g.errors[nodeIndex] = error;
             recomputed++;
         }
@@ -332,62 +373,102 @@ __global__ void __launch_bounds__(256) k_compute_errors(MdasDeviceGrid g) {
 //
 // Slots: sample slot = N + (#accepted leaves before this one),
 //        leaf slot   = L + (#split leaves before this one),
-// from a decoupled look-back scan over tiles of 256 leaves taken in ticket
-// order, so a tile only ever waits on tiles that running CTAs already hold.
+// i.e. the reference's outcome when warps retire in leaf order.  Three kernels,
+// no waiting between CTAs:
+//   decide — tiles of MDAS_TILE_LEAVES leaves; every thread streams
+//            MDAS_LEAVES_PER_THREAD consecutive leaves (16-byte loads of errors
+//            and seeds), decides acceptance, reads the node of each accepted
+//            leaf, writes every final seed (the candidate draws are a fixed
+//            number of LCG steps, applied by jump-ahead), and writes the tile's
+//            (accepted, split) counts and its accepted leaves, compacted in leaf
+//            order, to scratch;
+//   scan   — one CTA: exclusive prefix of the tile counts, and the new counts;
+//   place  — one thread per accepted leaf: best candidate from the leaf's box
+//            and private sample copy, append or split, writes.
+// decide also takes the max error of the leaves the pass does not split (their
+// error is final for the next errors pass); place lists the split leaves.
 // =====================================================================================
-__device__ __forceinline__ unsigned long long tile_pack(unsigned long long status, unsigned sel, unsigned split) {
-    return (status << 62) | ((unsigned long long)split << 31) | (unsigned long long)sel;
-}
 
-__device__ __forceinline__ unsigned long long tile_load(const unsigned long long* p) {
-    return *reinterpret_cast<const volatile unsigned long long*>(p);
-}
-
-__device__ __forceinline__ void tile_store(unsigned long long* p, unsigned long long v) {
-    *reinterpret_cast<volatile unsigned long long*>(p) = v;
+// Accepted-leaf entry: x = local leaf index in the tile (bits 0-10) | split rank
+// in the tile (bits 11-21) | split flag (bit 22) | sample count (bits 23-25);
+// y = the leaf's seed after the acceptance draw.
+__device__ __forceinline__ unsigned acc_pack(unsigned local, unsigned splitRank, unsigned split, unsigned cnt) {
+    return local | (splitRank << 11) | (split << 22) | (cnt << 23);
 }
 
 template <int D>
-__global__ void __launch_bounds__(256) k_adaptive_sampling(MdasDeviceGrid g) {
+__global__ void __launch_bounds__(256) k_adaptive_decide(MdasDeviceGrid g, unsigned jumpA, unsigned jumpC) {
     constexpr int kMaxNodeSize = 4;  // KDGrid ctor: maxNodeSize(4), kdgrid.cu:611
-    __shared__ int s_tile;
+    constexpr int K = MDAS_LEAVES_PER_THREAD;
+    constexpr int TILE = MDAS_TILE_LEAVES;
+    constexpr int NB = NbLayout<D>::FLOATS;
+    static_assert(TILE == 256 * K && TILE <= 2048, "tile = 256 threads x K leaves, local index in 11 bits");
     __shared__ unsigned s_warp[8];
-    __shared__ unsigned long long s_prefix;
 
-    const int N = g.counts->N;
     const int L = g.counts->L;
     const float gError = __uint_as_float(g.counts->gerr);
-    const int ntiles = (L + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
+    const int ntiles = (L + TILE - 1) / TILE;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
+    float keptMax = 0.0f;   // max error of the leaves this CTA does not split
+    unsigned gathered = 0;  // sample coordinates read
 
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = (int)atomicAdd(&g.ctl->ticket, 1u);
-        __syncthreads();
-        const int tile = s_tile;
-        if (tile >= ntiles) break;
-        const int nodeIndex = tile * MDAS_TILE_LEAVES + threadIdx.x;
-        const bool valid = nodeIndex < L;
-
-        // ---- phase 1: acceptance test and split flag
-        unsigned seed = 0;
-        bool sel = false;
-        int4 node = make_int4(0, 0, 0, 0);
-        int sampleCount = 0;
-        if (valid) {
-            const float error = g.errors[nodeIndex];
-            seed = g.seeds[nodeIndex];
-            if (seed == 0) seed = tea4((unsigned)nodeIndex, 0);
-            sel = mdas_pow(error / gError, g.alpha) >= rnd(seed);
-            if (sel) {
-                node = g.nodes[nodeIndex];
-                sampleCount = node_count(node);
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int i0 = tile * TILE + threadIdx.x * K;
+        const bool full = i0 + K <= L;
+        float err[K];
+        unsigned sd[K];
+        if (full) {
+#pragma unroll
+            for (int q = 0; q < K; q += 4) {
+                const float4 e4 = *reinterpret_cast<const float4*>(g.errors + i0 + q);
+                const uint4 s4 = *reinterpret_cast<const uint4*>(g.seeds + i0 + q);
+                err[q] = e4.x; err[q + 1] = e4.y; err[q + 2] = e4.z; err[q + 3] = e4.w;
+                sd[q] = s4.x; sd[q + 1] = s4.y; sd[q + 2] = s4.z; sd[q + 3] = s4.w;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                const bool v = i0 + j < L;
+                err[j] = v ? g.errors[i0 + j] : 0.0f;
+                sd[j] = v ? g.seeds[i0 + j] : 0u;
             }
         }
-        const bool split = sel && sampleCount >= kMaxNodeSize;
+        unsigned accMask = 0;
+        unsigned seedAcc[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            const int leaf = i0 + j;
+            unsigned seed = sd[j];
+            if (seed == 0) seed = tea4((unsigned)leaf, 0);
+            bool a = false;
+            if (leaf < L) a = mdas_pow(err[j] / gError, g.alpha) >= rnd(seed);
+            seedAcc[j] = seed;
+            sd[j] = a ? jumpA * seed + jumpC : seed;  // the seed after the candidate draws
+            if (a) accMask |= 1u << j;
+        }
+        int cnt[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j) cnt[j] = ((accMask >> j) & 1u) ? node_count(nb_node(g.nb + (size_t)(i0 + j) * NB)) : 0;
+        unsigned splitMask = 0;
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            gathered += (unsigned)cnt[j];
+            if (cnt[j] >= kMaxNodeSize) splitMask |= 1u << j;
+            if (i0 + j < L && !((splitMask >> j) & 1u)) keptMax = fmaxf(keptMax, err[j]);
+        }
+        if (full) {
+#pragma unroll
+            for (int q = 0; q < K; q += 4)
+                *reinterpret_cast<uint4*>(g.seeds + i0 + q) = make_uint4(sd[q], sd[q + 1], sd[q + 2], sd[q + 3]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < K; ++j)
+                if (i0 + j < L) g.seeds[i0 + j] = sd[j];
+        }
 
-        // ---- block scan of (accepted, split) packed as lo16 | hi16
-        const unsigned flag = (sel ? 1u : 0u) | (split ? 0x10000u : 0u);
+        // block scan of (accepted, split) counts, packed lo16 | hi16
+        const unsigned flag = (unsigned)__popc(accMask) | ((unsigned)__popc(splitMask) << 16);
         unsigned incl = flag;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -406,42 +487,150 @@ __global__ void __launch_bounds__(256) k_adaptive_sampling(MdasDeviceGrid g) {
             if (lane < 8) s_warp[lane] = w;
         }
         __syncthreads();
-        const unsigned exclInTile = (warp ? s_warp[warp - 1] : 0u) + incl - flag;
+        const unsigned excl = (warp ? s_warp[warp - 1] : 0u) + incl - flag;
         const unsigned tileTotal = s_warp[7];
-        if (threadIdx.x == 0) {
-            // publish early so that successors can look back while this tile works
-            tile_store(g.tiles + tile, tile == 0 ? tile_pack(MDAS_TILE_INC, tileTotal & 0xffffu, tileTotal >> 16)
-                                                 : tile_pack(MDAS_TILE_AGG, tileTotal & 0xffffu, tileTotal >> 16));
-        }
-
-        // ---- phase 2: best candidate (kdgrid.cu:332-361)
-        float samples[4][D];
-        float mn[D], mx[D];
-        float best[D];
+        {
+            unsigned r = excl & 0xffffu, rp = excl >> 16;
+            uint2* acc = g.accepted + (size_t)tile * TILE;
 #pragma unroll
-        for (int i = 0; i < D; ++i) best[i] = 0.0f;
-        if (sel) {
-            load_box<D>(g.boxes + (size_t)nodeIndex * 2 * D, mn, mx);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int idx = node_get(node, k);
-                if (idx >= 0) load_point<D>(g.coords + (size_t)idx * D, samples[k]);
+            for (int j = 0; j < K; ++j) {
+                if ((accMask >> j) & 1u) {
+                    const unsigned sp = (splitMask >> j) & 1u;
+                    acc[r] = make_uint2(acc_pack((unsigned)(threadIdx.x * K + j), rp, sp, (unsigned)cnt[j]), seedAcc[j]);
+                    r++;
+                    rp += sp;
+                }
             }
+        }
+        if (threadIdx.x == 0) g.tileCounts[tile] = make_uint2(tileTotal & 0xffffu, tileTotal >> 16);
+        __syncthreads();  // s_warp is reused by the next tile
+    }
+    unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(keptMax));
+    unsigned c = __reduce_add_sync(0xffffffffu, gathered);
+    if (lane == 0) {
+        if (m) atomicMax(&g.counts->gerrNext, m);
+        if (c) atomicAdd(&g.counts->gathered, c);
+    }
+}
+
+// One CTA of 1024 threads: exclusive prefix over the tile counts, then the
+// counters (N, L as the place kernel must see them go to ctl).
+__global__ void __launch_bounds__(1024) k_adaptive_scan(MdasDeviceGrid g) {
+    __shared__ unsigned s_sel[32], s_split[32];
+    const int N = g.counts->N;
+    const int L = g.counts->L;
+    const int ntiles = (L + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
+    const int per = (ntiles + 1023) / 1024;
+    const int t0 = threadIdx.x * per;
+    const int t1 = min(t0 + per, ntiles);
+    unsigned sel = 0, spl = 0;
+    for (int t = t0; t < t1; ++t) {
+        const uint2 c = g.tileCounts[t];
+        sel += c.x;
+        spl += c.y;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned is = sel, ip = spl;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned a = __shfl_up_sync(0xffffffffu, is, o);
+        const unsigned b = __shfl_up_sync(0xffffffffu, ip, o);
+        if (lane >= o) {
+            is += a;
+            ip += b;
+        }
+    }
+    if (lane == 31) {
+        s_sel[warp] = is;
+        s_split[warp] = ip;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        unsigned a = s_sel[lane], b = s_split[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned x = __shfl_up_sync(0xffffffffu, a, o);
+            const unsigned y = __shfl_up_sync(0xffffffffu, b, o);
+            if (lane >= o) {
+                a += x;
+                b += y;
+            }
+        }
+        s_sel[lane] = a;
+        s_split[lane] = b;
+    }
+    __syncthreads();
+    unsigned ps = (warp ? s_sel[warp - 1] : 0u) + is - sel;
+    unsigned pp = (warp ? s_split[warp - 1] : 0u) + ip - spl;
+    for (int t = t0; t < t1; ++t) {
+        const uint2 c = g.tileCounts[t];
+        g.tilePrefix[t] = make_uint2(ps, pp);
+        ps += c.x;
+        pp += c.y;
+    }
+    if (threadIdx.x == 1023) {
+        const unsigned newN = ps, newL = pp;  // the last thread ends at the totals
+        g.ctl->N0 = N;
+        g.ctl->L0 = L;
+        g.counts->newN = (int)newN;
+        g.counts->newL = (int)newL;
+        g.counts->selected = (int)newN;
+        g.counts->N = N + (int)newN;
+        g.counts->L = L + (int)newL;
+        g.counts->passes += 1;
+    }
+}
+
+template <int D>
+__global__ void __launch_bounds__(256, 3) k_adaptive_place(MdasDeviceGrid g) {
+    constexpr int kMaxNodeSize = 4;
+    constexpr int TILE = MDAS_TILE_LEAVES;
+    constexpr int NB = NbLayout<D>::FLOATS;
+    const int N = g.ctl->N0;
+    const int L = g.ctl->L0;
+    const int ntiles = (L + TILE - 1) / TILE;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int tileSel = (int)g.tileCounts[tile].x;
+        if ((int)threadIdx.x >= tileSel) continue;
+        const uint2 pre = g.tilePrefix[tile];
+        for (int r = threadIdx.x; r < tileSel; r += 256) {
+            const uint2 e = g.accepted[(size_t)tile * TILE + r];
+            const int nodeIndex = tile * TILE + (int)(e.x & 0x7ffu);
+            const int splitRankInTile = (int)((e.x >> 11) & 0x7ffu);
+            const bool split = (e.x >> 22) & 1u;
+            const int sampleCount = (int)((e.x >> 23) & 7u);
+            unsigned seed = e.y;
+            float* nb = g.nb + (size_t)nodeIndex * NB;
+            float* sc = g.lsc + (size_t)nodeIndex * 4 * D;
+            float mn[D], mx[D];
+            int4 node = nb_load<D>(nb, mn, mx);
+            float scv[4 * D];
+            ld_floats<4 * D>(sc, scv);
+            float samples[4][D];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+#pragma unroll
+                for (int i = 0; i < D; ++i) samples[k][i] = scv[k * D + i];
+
+            // best candidate (kdgrid.cu:332-361)
+            float best[D];
+#pragma unroll
+            for (int i = 0; i < D; ++i) best[i] = 0.0f;
             float maxDistance = -1.0f;
             float diag[D];
 #pragma unroll
             for (int i = 0; i < D; ++i) diag[i] = mx[i] - mn[i];
             for (int j = 0; j < g.candidatesNum; ++j) {
-                float r[D];
+                float rr[D];
 #pragma unroll
-                for (int i = 0; i < D; ++i) r[i] = rnd(seed);
+                for (int i = 0; i < D; ++i) rr[i] = rnd(seed);
                 float candidate[D];
 #pragma unroll
-                for (int i = 0; i < D; ++i) candidate[i] = mn[i] + r[i] * diag[i];
+                for (int i = 0; i < D; ++i) candidate[i] = mn[i] + rr[i] * diag[i];
                 float minDistance = FLT_MAX;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    if (node_get(node, k) >= 0) {
+                    if (k < sampleCount) {
                         const float distance_k = distance<D>(candidate, samples[k]);
                         if (minDistance > distance_k) minDistance = distance_k;
                     }
@@ -452,75 +641,34 @@ __global__ void __launch_bounds__(256) k_adaptive_sampling(MdasDeviceGrid g) {
                     for (int i = 0; i < D; ++i) best[i] = candidate[i];
                 }
             }
-        }
 
-        // ---- phase 3: look-back for the tile's exclusive prefix (warp 0)
-        if (warp == 0) {
-            unsigned preSel = 0, preSplit = 0;
-            if (tile > 0) {
-                int window = tile - 1;  // lane l inspects tile window - l
-                for (;;) {
-                    const int pred = window - lane;
-                    unsigned long long st = tile_pack(MDAS_TILE_INC, 0, 0);
-                    if (pred >= 0) {
-                        unsigned spins = 0;
-                        st = tile_load(g.tiles + pred);
-                        while ((st >> 62) == 0ull) {
-                            if (++spins > MDAS_SPIN_LIMIT) {
-                                atomicCAS(&g.counts->status, 0, MDAS_ERR_TIMEOUT);
-                                st = tile_pack(MDAS_TILE_INC, 0, 0);
-                                break;
-                            }
-                            __nanosleep(64);
-                            st = tile_load(g.tiles + pred);
-                        }
-                    }
-                    const bool isInc = (st >> 62) == MDAS_TILE_INC;
-                    const unsigned incMask = __ballot_sync(0xffffffffu, isInc);
-                    const int firstInc = incMask ? __ffs(incMask) - 1 : 32;
-                    const bool take = lane <= firstInc;
-                    const unsigned s = take ? (unsigned)(st & 0x7fffffffull) : 0u;
-                    const unsigned p = take ? (unsigned)((st >> 31) & 0x7fffffffull) : 0u;
-                    preSel += __reduce_add_sync(0xffffffffu, s);
-                    preSplit += __reduce_add_sync(0xffffffffu, p);
-                    if (incMask) break;
-                    window -= 32;
-                }
-                if (lane == 0)
-                    tile_store(g.tiles + tile, tile_pack(MDAS_TILE_INC, preSel + (tileTotal & 0xffffu),
-                                                         preSplit + (tileTotal >> 16)));
-            }
-            if (lane == 0) s_prefix = ((unsigned long long)preSplit << 32) | preSel;
-        }
-        __syncthreads();
-
-        // ---- phase 4: writes (kdgrid.cu:380-477)
-        if (sel) {
-            const unsigned long long pre = s_prefix;
-            const int sampleIndex = N + (int)(unsigned)pre + (int)(exclInTile & 0xffffu);
+            const int sampleIndex = N + (int)pre.x + r;
             store_point<D>(g.coords + (size_t)sampleIndex * D, best);
             if (!split) {
-                // room left: append the index, the error stays as it was
+                // room left: append the index (and its coordinates), the error stays as it was
                 if (sampleCount == 0) node.x = sampleIndex;
                 else if (sampleCount == 1) node.y = sampleIndex;
                 else if (sampleCount == 2) node.z = sampleIndex;
                 else node.w = sampleIndex;
-                g.nodes[nodeIndex] = node;
+                nb_set_node(nb, node);
+                store_point<D>(sc + sampleCount * D, best);
             } else {
                 // split dimension: AABB::LargestAxis, ties to the highest index (aabb.h:34-45)
                 int axis = -1;
                 float maxExtent = -FLT_MAX;
 #pragma unroll
                 for (int i = D - 1; i >= 0; --i) {
-                    const float e = mx[i] - mn[i];
-                    if (maxExtent < e) {
-                        maxExtent = e;
+                    const float ext = mx[i] - mn[i];
+                    if (maxExtent < ext) {
+                        maxExtent = ext;
                         axis = i;
                     }
                 }
-                int loc[5];
+                // The reference bubble-sorts the 5 samples (4 old in slot order, then the
+                // new one) by the split coordinate (kdgrid.cu:408-417); the sort is stable,
+                // so sample k lands at rank[k] = #{m : key[m] < key[k], or key[m] == key[k]
+                // and m < k}.  Each sample is written straight to its ranked slot.
                 float key[5];
-                loc[0] = node.x; loc[1] = node.y; loc[2] = node.z; loc[3] = node.w; loc[4] = sampleIndex;
 #pragma unroll
                 for (int k = 0; k < 5; ++k) {
                     float v = 0.0f;
@@ -531,65 +679,56 @@ __global__ void __launch_bounds__(256) k_adaptive_sampling(MdasDeviceGrid g) {
                     }
                     key[k] = v;
                 }
-                // stable bubble sort of the 5 samples by the split coordinate (kdgrid.cu:408-417)
+                int rank[5];
 #pragma unroll
-                for (int i = 0; i < 4; i++) {
+                for (int k = 0; k < 5; ++k) {
+                    int rk = 0;
 #pragma unroll
-                    for (int j = 0; j < 4 - i; j++) {
-                        if (key[j] > key[j + 1]) {
-                            const float tk = key[j]; key[j] = key[j + 1]; key[j + 1] = tk;
-                            const int tl = loc[j]; loc[j] = loc[j + 1]; loc[j + 1] = tl;
-                        }
-                    }
+                    for (int m = 0; m < 5; ++m)
+                        if (m != k) rk += (key[m] < key[k] || (key[m] == key[k] && m < k)) ? 1 : 0;
+                    rank[k] = rk;
                 }
-                const float splitPosition = 0.5f * (key[1] + key[2]);  // md = 5 >> 1 = 2
-                const int nodeOffset = L + (int)(unsigned)(pre >> 32) + (int)(exclInTile >> 16);
-                g.nodes[nodeIndex] = make_int4(loc[0], loc[1], ~D, ~D);
-                g.nodes[nodeOffset] = make_int4(loc[2], loc[3], loc[4], ~D);
-                // left child: only mx[axis] changes
-                g.boxes[(size_t)nodeIndex * 2 * D + D + axis] = splitPosition;
+                const int idx5[5] = {node.x, node.y, node.z, node.w, sampleIndex};
+                float k1 = 0.0f, k2 = 0.0f;
+                int l0 = 0, l1 = 0, r0 = 0, r1 = 0, r2 = 0;
+#pragma unroll
+                for (int k = 0; k < 5; ++k) {
+                    const int rk = rank[k];
+                    if (rk == 1) k1 = key[k];
+                    if (rk == 2) k2 = key[k];
+                    if (rk == 0) l0 = idx5[k];
+                    if (rk == 1) l1 = idx5[k];
+                    if (rk == 2) r0 = idx5[k];
+                    if (rk == 3) r1 = idx5[k];
+                    if (rk == 4) r2 = idx5[k];
+                }
+                const float splitPosition = 0.5f * (k1 + k2);  // md = 5 >> 1 = 2
+                const int rank_ = (int)pre.y + splitRankInTile;
+                const int nodeOffset = L + rank_;
+                float* rnb = g.nb + (size_t)nodeOffset * NB;
+                float* rsc = g.lsc + (size_t)nodeOffset * 4 * D;
+                // left child keeps the slot: node, mx[axis], its 2 sample coordinates;
+                // right child: node, box, its 3 sample coordinates
+                nb_set_node(nb, make_int4(l0, l1, ~D, ~D));
+                nb[NbLayout<D>::BOX + D + axis] = splitPosition;
                 float rmn[D];
 #pragma unroll
                 for (int i = 0; i < D; ++i) rmn[i] = (i == axis) ? splitPosition : mn[i];
-                store_box<D>(g.boxes + (size_t)nodeOffset * 2 * D, rmn, mx);
+                nb_store<D>(rnb, make_int4(r0, r1, r2, ~D), rmn, mx);
+#pragma unroll
+                for (int k = 0; k < 5; ++k) {
+                    float* dst = rank[k] < 2 ? sc + rank[k] * D : rsc + (rank[k] - 2) * D;
+                    if (k < 4) store_point<D>(dst, samples[k < 4 ? k : 0]);
+                    else store_point<D>(dst, best);
+                }
                 g.errors[nodeIndex] = -1.0f;
                 g.errors[nodeOffset] = -1.0f;
                 // a new slot starts without a seed: the reference's seed buffer is zeroed
                 // once at InitialSampling (kdgrid.cu:637) and right-child slots are never
                 // written before; writing the 0 here makes that memset unnecessary
                 g.seeds[nodeOffset] = 0u;
+                g.dirty[rank_] = nodeIndex;  // for the next errors pass
             }
-        }
-        if (valid) g.seeds[nodeIndex] = seed;
-        // samples gathered by this tile (for the traffic accounting)
-        {
-            const unsigned gathered = __reduce_add_sync(0xffffffffu, sel ? (unsigned)sampleCount : 0u);
-            if (lane == 0 && gathered) atomicAdd(&g.counts->gathered, gathered);
-        }
-        __syncthreads();
-    }
-
-    // ---- the last CTA out commits the counters and resets the tickets
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const unsigned prev = atomicAdd(&g.ctl->done, 1u);
-        if (prev == gridDim.x - 1) {
-            __threadfence();
-            unsigned newN = 0, newL = 0;
-            if (ntiles > 0) {
-                const unsigned long long st = tile_load(g.tiles + ntiles - 1);
-                newN = (unsigned)(st & 0x7fffffffull);
-                newL = (unsigned)((st >> 31) & 0x7fffffffull);
-            }
-            g.counts->newN = (int)newN;
-            g.counts->newL = (int)newL;
-            g.counts->selected = (int)newN;
-            g.counts->N = N + (int)newN;
-            g.counts->L = L + (int)newL;
-            g.counts->passes += 1;
-            g.ctl->ticket = 0;
-            g.ctl->done = 0;
-            __threadfence();
         }
     }
 }
@@ -603,6 +742,7 @@ __global__ void __launch_bounds__(256) k_adaptive_sampling(MdasDeviceGrid g) {
 template <int D>
 __global__ void __launch_bounds__(256) k_integrate(MdasDeviceGrid g, float4* __restrict__ pixels, int width,
                                                     int height) {
+    constexpr int NB = NbLayout<D>::FLOATS;
     const int L = g.counts->L;
     const float scaleX = g.scaleX, scaleY = g.scaleY;
     for (int nodeIndex = blockIdx.x * blockDim.x + threadIdx.x; nodeIndex < L;
@@ -610,7 +750,8 @@ __global__ void __launch_bounds__(256) k_integrate(MdasDeviceGrid g, float4* __r
         float2 pixelStep;
         pixelStep.x = scaleX / width;
         pixelStep.y = scaleY / height;
-        const int4 node = __ldg(g.nodes + nodeIndex);
+        float mn[D], mx[D];
+        const int4 node = nb_load<D>(g.nb + (size_t)nodeIndex * NB, mn, mx);
         float3 sampleValue = make_float3(0.0f, 0.0f, 0.0f);
         int sampleCount = 0;
 #pragma unroll
@@ -630,8 +771,6 @@ __global__ void __launch_bounds__(256) k_integrate(MdasDeviceGrid g, float4* __r
             sampleValue.y *= inv;
             sampleValue.z *= inv;
         }
-        float mn[D], mx[D];
-        load_box<D>(g.boxes + (size_t)nodeIndex * 2 * D, mn, mx);
         const float boxVolume = box_volume<D>(mn, mx);
 
         const int x0 = mn[0] * width / scaleX;
@@ -720,6 +859,48 @@ __global__ void k_density_alpha(float4* __restrict__ pixels, int P) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) pixels[i].w = 1.0f;
 }
 
+// =====================================================================================
+// Leaf records <-> the reference's node / box arrays (state dump and load).
+// =====================================================================================
+template <int D>
+__global__ void k_unpack_records(const float* __restrict__ nb, int L, int4* __restrict__ nodes,
+                                 float* __restrict__ boxes) {
+    constexpr int NB = NbLayout<D>::FLOATS;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
+        float mn[D], mx[D];
+        nodes[i] = nb_load<D>(nb + (size_t)i * NB, mn, mx);
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            boxes[(size_t)i * 2 * D + k] = mn[k];
+            boxes[(size_t)i * 2 * D + D + k] = mx[k];
+        }
+    }
+}
+
+template <int D>
+__global__ void k_pack_records(float* __restrict__ nb, float* __restrict__ lsc, int L, const int4* __restrict__ nodes,
+                               const float* __restrict__ boxes, const float* __restrict__ coords) {
+    constexpr int NB = NbLayout<D>::FLOATS;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
+        const int4 n = nodes[i];
+        float mn[D], mx[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            mn[k] = boxes[(size_t)i * 2 * D + k];
+            mx[k] = boxes[(size_t)i * 2 * D + D + k];
+        }
+        nb_store<D>(nb + (size_t)i * NB, n, mn, mx);
+        float sc[4 * D];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int idx = node_get(n, k);
+#pragma unroll
+            for (int d = 0; d < D; ++d) sc[k * D + d] = idx >= 0 ? coords[(size_t)idx * D + d] : 0.0f;
+        }
+        st_floats<4 * D>(lsc + (size_t)i * 4 * D, sc);
+    }
+}
+
 // ---- host launchers -------------------------------------------------------------
 #define MDAS_SWITCH_D(D, EXPR)                 \
     switch (D) {                               \
@@ -737,19 +918,37 @@ cudaError_t initial_sampling(const MdasDeviceGrid& g, int L, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t compute_errors(const MdasDeviceGrid& g, int grid, cudaStream_t s) {
+cudaError_t compute_errors(const MdasDeviceGrid& g, int grid, bool dirty, cudaStream_t s) {
     // g_error = 0 (kdgrid.cu:684-685) and the recomputed-leaf counter next to it
     cudaError_t e = cudaMemsetAsync(&g.counts->gerr, 0, 2 * sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
-    MDAS_SWITCH_D(g.D, (k_compute_errors<DD><<<grid, 256, 0, s>>>(g)));
+    if (dirty) {
+        MDAS_SWITCH_D(g.D, (k_compute_errors<DD, true><<<grid, 256, 0, s>>>(g)));
+    } else {
+        MDAS_SWITCH_D(g.D, (k_compute_errors<DD, false><<<grid, 256, 0, s>>>(g)));
+    }
     return cudaGetLastError();
 }
 
-cudaError_t adaptive_sampling(const MdasDeviceGrid& g, int grid, cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(g.tiles, 0, sizeof(unsigned long long) * (size_t)g.maxTiles, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(&g.counts->gathered, 0, sizeof(unsigned), s);
+// LCG jump-ahead: n draws take a seed s to A_n * s + C_n (mod 2^32).
+static void lcg_jump(unsigned n, unsigned* A, unsigned* C) {
+    unsigned a = 1u, c = 0u;
+    for (unsigned k = 0; k < n; ++k) {
+        a = 1664525u * a;
+        c = 1664525u * c + 1013904223u;
+    }
+    *A = a;
+    *C = c;
+}
+
+cudaError_t adaptive_sampling(const MdasDeviceGrid& g, int gridDecide, int gridPlace, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(&g.counts->gathered, 0, 2 * sizeof(unsigned), s);  // + gerrNext
     if (e != cudaSuccess) return e;
-    MDAS_SWITCH_D(g.D, (k_adaptive_sampling<DD><<<grid, 256, 0, s>>>(g)));
+    unsigned A, C;
+    lcg_jump((unsigned)(g.candidatesNum * g.D), &A, &C);
+    MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD><<<gridDecide, 256, 0, s>>>(g, A, C)));
+    k_adaptive_scan<<<1, 1024, 0, s>>>(g);
+    MDAS_SWITCH_D(g.D, (k_adaptive_place<DD><<<gridPlace, 256, 0, s>>>(g)));
     return cudaGetLastError();
 }
 
@@ -777,18 +976,47 @@ cudaError_t sampling_density(const MdasDeviceGrid& g, float* pixels, int W, int 
     return cudaGetLastError();
 }
 
+cudaError_t unpack_records(const MdasDeviceGrid& g, int L, int* nodes, float* boxes, cudaStream_t s) {
+    if (L == 0) return cudaSuccess;
+    const int grid = (L + 255) / 256 < 4096 ? (L + 255) / 256 : 4096;
+    MDAS_SWITCH_D(g.D, (k_unpack_records<DD><<<grid, 256, 0, s>>>(g.nb, L, reinterpret_cast<int4*>(nodes), boxes)));
+    return cudaGetLastError();
+}
+
+cudaError_t pack_records(const MdasDeviceGrid& g, int L, const int* nodes, const float* boxes, cudaStream_t s) {
+    if (L == 0) return cudaSuccess;
+    const int grid = (L + 255) / 256 < 4096 ? (L + 255) / 256 : 4096;
+    MDAS_SWITCH_D(g.D, (k_pack_records<DD><<<grid, 256, 0, s>>>(g.nb, g.lsc, L, reinterpret_cast<const int4*>(nodes),
+                                                               boxes, g.coords)));
+    return cudaGetLastError();
+}
+
+int record_floats(int D) {
+    switch (D) {
+        case 3: return NbLayout<3>::FLOATS;
+        case 4: return NbLayout<4>::FLOATS;
+        case 5: return NbLayout<5>::FLOATS;
+        case 6: return NbLayout<6>::FLOATS;
+    }
+    return 0;
+}
+
 int max_blocks_per_sm(int D, int which) {
     int n = 0;
     cudaError_t e = cudaSuccess;
     switch (which) {
         case MDAS_K_ERRORS:
-            MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_compute_errors<DD>, 256, 0)));
+            MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_compute_errors<DD, false>, 256,
+                                                                                 0)));
             break;
         case MDAS_K_ADAPTIVE:
-            MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adaptive_sampling<DD>, 256, 0)));
+            MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adaptive_place<DD>, 256, 0)));
             break;
         case MDAS_K_INTEGRATE:
             MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_integrate<DD>, 256, 0)));
+            break;
+        case MDAS_K_DECIDE:
+            MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adaptive_decide<DD>, 256, 0)));
             break;
         default:
             MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_initial_sampling<DD>, 256, 0)));
