@@ -126,6 +126,39 @@ int mdas_dump_state(mdas_grid* g, float* coords, float* values, int* nodes, floa
 int mdas_load_state(mdas_grid* g, int numberOfSamples, int numberOfNodes, const float* coords, const float* values,
                     const int* nodes, const float* boxes, const float* errors, const uint32_t* seeds);
 
+/* One adaptive sampling pass that allocates no memory (no counterpart in the
+ * reference; it exists for callers of this library that cannot allocate).
+ *
+ * mdas_create allocates the sampler's state with cudaMalloc.  Some callers
+ * cannot allocate when they sample: a renderer that records its frame into a
+ * CUDA graph by stream capture (allocating during capture is an error), a
+ * plugin host that hands out all device memory up front, or a process whose
+ * device memory belongs to another framework's allocator.  This call runs one
+ * pass of KDGrid::AdaptiveSampling on buffers the caller owns, laid out like
+ * the reference's sampler: coords (dim floats per sample, room for maxSamples
+ * samples), nodes (4 ints per leaf, ~dim = empty), boxes (mn[dim] then
+ * mx[dim] per leaf), errors and seeds (one per leaf; nodes, boxes, errors and
+ * seeds with room for nodeCapacity leaves).  gError is the max leaf error of
+ * the caller's errors pass.  The results equal mdas_adaptive_sampling's in
+ * the reference arithmetic; the new counts are returned in *newSamples and
+ * *newNodes (the call synchronises `stream`, like mdas_adaptive_sampling).
+ *
+ * Its only scratch (per-tile counts of 1024 leaves) lives in a fixed array of
+ * device memory inside this library, so a pass takes at most
+ * MDAS_STATIC_MAX_LEAVES leaves; larger passes return MDAS_ERR_INVALID, and
+ * passes that could write past maxSamples samples or nodeCapacity leaves
+ * return MDAS_ERR_CAPACITY.  Nothing in the array needs clearing between
+ * calls: every call overwrites the entries it reads.  All calls share that
+ * one array, so calls that overlap on the GPU (two streams, two threads)
+ * race and must be serialised by the caller.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); make that first
+ * call before any stream capture that should contain later calls. */
+#define MDAS_STATIC_MAX_LEAVES (1 << 22)
+int mdas_adaptive_sampling_static(int dim, int numberOfSamples, int numberOfNodes, int candidatesNum, float alpha,
+                                  float gError, int maxSamples, int nodeCapacity, float* coords, int* nodes,
+                                  float* boxes, float* errors, uint32_t* seeds, int* newSamples, int* newNodes,
+                                  void* stream);
+
 /* Per-stage CUDA-event times accumulated since the last reset, in ms:
  * [0] initial sampling, [1] compute errors, [2] adaptive sampling,
  * [3] integrate, [4] integrand.  Timing is off until mdas_set_timing(g, 1). */

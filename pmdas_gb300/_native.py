@@ -77,6 +77,8 @@ SIGNATURES = {
     "mdas_get_gerror": (_I, [_P, _FP]),
     "mdas_dump_state": (_I, [_P, _P, _P, _P, _P, _P, _P]),
     "mdas_load_state": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P]),
+    "mdas_adaptive_sampling_static": (_I, [_I, _I, _I, _I, _F, _F, _I, _I, _P, _P, _P, _P, _P, C.POINTER(_I),
+                                           C.POINTER(_I), _P]),
     "mdas_set_timing": (_I, [_P, _I]),
     "mdas_get_stage_times": (_I, [_P, C.POINTER(C.c_double), _I]),
     "mdas_get_launch_count": (_I, [_P, C.POINTER(C.c_uint64)]),

@@ -38,6 +38,7 @@ UNITS = [
     ("kdgrid_ieee.cu", IEEE),
     ("integrand.cu", IEEE),
     ("capi.cu", []),
+    ("noalloc.cu", FAST),
 ]
 CXX_UNITS = ["env.cpp"]
 HEADERS = ["grid_types.h", "ieee_math.h", "integrand.h", "kdgrid_kernels.cuh", "scene.h"]
