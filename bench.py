@@ -49,6 +49,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-cuda", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-quality", action="store_true")
     return ap.parse_args()
 
 
@@ -242,6 +243,39 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     all_bytes = sum(by.values())
     overall_gbs = all_bytes * args.steps / (mdas_ms / 1e3) / 1e9
 
+    # the same render as one CUDA graph (device-side loop): device time per render,
+    # integrand included
+    graph_ms = None
+    if args.e2e_steps > 0:
+        P.render_graph(grid, scene, wl.budget, pixels, W, H)  # build + warm
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record()
+        for _ in range(args.e2e_steps):
+            P.render_graph(grid, scene, wl.budget, pixels, W, H)
+        a1.record()
+        torch.cuda.synchronize()
+        graph_ms = a0.elapsed_time(a1) / args.e2e_steps
+
+    # quality: rel-MSE (parse_logs.py:48-50) of the last render against a 4096-spp
+    # reference image of the same integrand accumulated in FP64
+    quality = None
+    if not args.no_quality:
+        img = pixels[..., :3].double()
+        t0 = time.perf_counter()
+        ref = scene.reference_image(W, H, spp=4096)
+        torch.cuda.synchronize()
+        ref_ms = (time.perf_counter() - t0) * 1e3
+        def rel_mse(a):
+            v = (ref - a) ** 2 / (ref ** 2 + 1e-2)
+            return float(torch.nan_to_num(v, nan=0.0).mean().item())
+        spp_sq = int(round(wl.spp ** 0.5))
+        quality = {"rel_mse": rel_mse(img),
+                   "reference": "4096 spp per pixel, stratified image plane, FP64 accumulation",
+                   "reference_ms": round(ref_ms, 1)}
+        if spp_sq * spp_sq == wl.spp:  # stratified Monte Carlo at the same spp, for context
+            quality["stratified_mc_rel_mse_same_spp"] = rel_mse(scene.reference_image(W, H, spp=int(wl.spp),
+                                                                                      seed=99))
+
     # e2e through the host-buffer C-ABI call
     e2e = None
     if args.e2e_steps > 0:
@@ -278,6 +312,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         "stage_ms_per_step": {k: round(stage_ms[i] / args.steps, 4)
                               for i, k in enumerate(["init", "errors", "adaptive", "integrate", "integrand"])},
         "wall_ms_per_step": round(wall_ms / args.steps, 3),
+        "graph_render_ms": round(graph_ms, 3) if graph_ms else None,
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
                      "algorithmic_bytes_per_launch": int(per_launch_bytes), "launches_per_step": launches_of,
@@ -285,6 +320,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
                      "all_stages_gbs": round(overall_gbs, 1)},
         "stage_bytes_per_step": by,
         "e2e": e2e,
+        "quality": quality,
         "gpu_launches": int(launches),
         "clocks": clk,
     }

@@ -202,6 +202,14 @@ int mdas_evaluate(mdas_grid* g, mdas_scene* s, int offset, int count);
 int mdas_scene_evaluate(mdas_scene* s, const float* coords, float* values, int dim, int offset, int count,
                         void* stream);
 
+/* Reference image of the scene for quality measurement: `spp` (a square
+ * number) samples per pixel, image plane stratified with jitter, radiance
+ * accumulated in FP64; `out` is a device buffer of width*height*3 doubles.
+ * The rel-MSE of an MDAS image is measured against it, as the reference's
+ * scripts measure against a high-spp render (SDK/data/Scripts/parse_logs.py:48-50). */
+int mdas_scene_reference_image(mdas_scene* s, int width, int height, int spp, uint64_t seed, double* out,
+                               void* stream);
+
 /* ---- the headless budget loop of the sample apps (optixMotionBlur.cpp:768-793) ----
  * initial sampling, integrand, then while N < budget: sampling pass + integrand
  * for the new samples, then integrate into a device float4 image.  Stops early
@@ -218,7 +226,17 @@ typedef struct mdas_render_stats {
 int mdas_render(mdas_grid* g, mdas_scene* s, int budget, float* pixels, int width, int height,
                 mdas_render_stats* stats);
 
-/* mdas_render with HOST input and output: the scene primitives are uploaded
+/* The same budget loop as one CUDA graph: the loop runs on the device (a
+ * conditional while node around errors + adaptive pass + integrand for the new
+ * samples + the loop condition), so a whole render costs one launch and one
+ * synchronisation instead of one per pass.  Results are identical to
+ * mdas_render.  The graph is built on the first call and reused while the
+ * scene, budget and pixel buffer stay the same; stats->stageMs stays zero
+ * (no per-stage events inside the graph). */
+int mdas_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, int width, int height,
+                      mdas_render_stats* stats);
+
+/* mdas_render_graph with HOST input and output: the scene primitives are uploaded
  * from `hostPrims` (12 floats each, may be NULL to keep the scene's) and the
  * float4 image is copied back into `hostPixels`. */
 int mdas_render_host(mdas_grid* g, mdas_scene* s, const float* hostPrims, int budget, float* hostPixels, int width,

@@ -90,8 +90,10 @@ SIGNATURES = {
     "mdas_scene_export": (_I, [_P, _P, _I, _P, _I, C.POINTER(_I), C.POINTER(_I)]),
     "mdas_evaluate": (_I, [_P, _P, _I, _I]),
     "mdas_scene_evaluate": (_I, [_P, _P, _P, _I, _I, _I, _P]),
+    "mdas_scene_reference_image": (_I, [_P, _I, _I, _I, C.c_uint64, _P, _P]),
     "mdas_render": (_I, [_P, _P, _I, _P, _I, _I, C.POINTER(RenderStats)]),
     "mdas_render_host": (_I, [_P, _P, _P, _I, _P, _I, _I, C.POINTER(RenderStats)]),
+    "mdas_render_graph": (_I, [_P, _P, _I, _P, _I, _I, C.POINTER(RenderStats)]),
     "mdas_config_defaults": (_I, [C.POINTER(Config)]),
     "mdas_config_read": (_I, [C.c_char_p, C.POINTER(Config), C.c_char_p, _I]),
 }

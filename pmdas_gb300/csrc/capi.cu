@@ -39,6 +39,16 @@ struct PendingTiming {
     cudaEvent_t a, b;
 };
 
+// An instantiated device-side render (mdas_render_graph) and what it was built for.
+struct RenderGraph {
+    cudaGraphExec_t exec = nullptr;
+    const void* scene = nullptr;
+    int budget = 0;
+    float* pixels = nullptr;
+    int width = 0, height = 0;
+    cudaStream_t stream = nullptr;
+};
+
 }  // namespace
 
 struct mdas_grid {
@@ -64,6 +74,8 @@ struct mdas_grid {
     size_t scratchBytes = 0;
     std::vector<cudaEvent_t> eventPool;
     std::vector<PendingTiming> pending;
+    RenderGraph graph;
+    cudaStream_t captureStream = nullptr, bodyStream = nullptr;
 };
 
 namespace {
@@ -164,6 +176,9 @@ int read_counts(mdas_grid* g) {
 void free_grid(mdas_grid* g) {
     if (!g) return;
     flush_timing(g);
+    if (g->graph.exec) cudaGraphExecDestroy(g->graph.exec);
+    if (g->captureStream) cudaStreamDestroy(g->captureStream);
+    if (g->bodyStream) cudaStreamDestroy(g->bodyStream);
     for (cudaEvent_t e : g->eventPool) cudaEventDestroy(e);
     cudaFree(g->dg.coords);
     cudaFree(g->dg.values);
@@ -691,6 +706,23 @@ int mdas_scene_evaluate(mdas_scene* s, const float* coords, float* values, int d
                                           (cudaStream_t)stream));
 }
 
+int mdas_scene_reference_image(mdas_scene* s, int width, int height, int spp, uint64_t seed, double* out,
+                               void* stream) {
+    if (!s || !out || width <= 0 || height <= 0 || spp < 1) return MDAS_ERR_INVALID;
+    int strata = 1;
+    while ((strata + 1) * (strata + 1) <= spp) ++strata;
+    if (strata * strata != spp) return MDAS_ERR_INVALID;  // a square number of samples per pixel
+    int rc = scene_upload(s, (cudaStream_t)stream);
+    if (rc) return rc;
+    int nsm = 1, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t want = ((int64_t)width * height + 255) / 256;
+    const int grid = (int)(want < (int64_t)nsm * 16 ? want : (int64_t)nsm * 16);
+    return status_of(mdas_launch_reference_image(s->desc, s->d_prims, width, height, strata, seed, out, grid,
+                                                 (cudaStream_t)stream));
+}
+
 int mdas_render(mdas_grid* g, mdas_scene* s, int budget, float* pixels, int width, int height,
                 mdas_render_stats* stats) {
     if (!g || !s || !pixels) return MDAS_ERR_INVALID;
@@ -719,6 +751,148 @@ int mdas_render(mdas_grid* g, mdas_scene* s, int budget, float* pixels, int widt
     return MDAS_OK;
 }
 
+// ---- the device-side budget loop ----------------------------------------------------
+namespace {
+
+constexpr int kMaxGraphPasses = 1 << 20;  // safety stop of the device-side loop
+
+cudaError_t launch_errors_auto(mdas_grid* g, int grid, cudaStream_t s) {
+    return g->arith == MDAS_ARITH_IEEE ? mdas_ieee::compute_errors_auto(g->dg, grid, s)
+                                       : mdas_fast::compute_errors_auto(g->dg, grid, s);
+}
+
+cudaError_t launch_adaptive_on(mdas_grid* g, int gridDecide, int gridPlace, cudaStream_t s) {
+    return g->arith == MDAS_ARITH_IEEE ? mdas_ieee::adaptive_sampling(g->dg, gridDecide, gridPlace, s)
+                                       : mdas_fast::adaptive_sampling(g->dg, gridDecide, gridPlace, s);
+}
+
+// Builds the whole render as one graph: initial sampling, integrand, a
+// conditional while node around {errors, adaptive pass, integrand for the new
+// samples, loop condition}, integrate.  Every kernel has a fixed persistent
+// grid and reads the leaf and sample counts from device memory.
+int build_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, int width, int height) {
+    if (g->graph.exec) {
+        cudaGraphExecDestroy(g->graph.exec);
+        g->graph.exec = nullptr;
+    }
+    if (!g->captureStream && cudaStreamCreateWithFlags(&g->captureStream, cudaStreamNonBlocking) != cudaSuccess)
+        return MDAS_ERR_CUDA;
+    if (!g->bodyStream && cudaStreamCreateWithFlags(&g->bodyStream, cudaStreamNonBlocking) != cudaSuccess)
+        return MDAS_ERR_CUDA;
+    const MdasDeviceGrid& d = g->dg;
+    const int64_t L0 = ((int64_t)1 << (d.bitsPerDim * d.D)) << (2 * d.extraImgBits);
+    const int64_t N0 = 4 * L0;
+    if (N0 > d.maxSamples) return MDAS_ERR_CAPACITY;
+    const unsigned firstPass = (N0 < budget && N0 + L0 <= d.maxSamples) ? 1u : 0u;
+    const int gErr = g->numSMs * (g->occ[MDAS_K_ERRORS] > 0 ? g->occ[MDAS_K_ERRORS] : 1);
+    const int gDecide = g->numSMs * (g->occ[MDAS_K_DECIDE] > 0 ? g->occ[MDAS_K_DECIDE] : 1);
+    const int gPlace = g->numSMs * (g->occ[MDAS_K_ADAPTIVE] > 0 ? g->occ[MDAS_K_ADAPTIVE] : 1);
+    const int gInt = g->numSMs * (g->occ[MDAS_K_INTEGRATE] > 0 ? g->occ[MDAS_K_INTEGRATE] : 1);
+    const int gEval = g->numSMs * 8;
+    cudaStream_t cs = g->captureStream, bs = g->bodyStream;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    auto fail = [&](cudaError_t err) {
+        cudaGraph_t junk = nullptr;
+        cudaStreamEndCapture(cs, &junk);
+        if (junk) cudaGraphDestroy(junk);
+        cudaGetLastError();
+        return err == cudaSuccess ? MDAS_ERR_CUDA : MDAS_ERR_CUDA;
+    };
+    // prologue: initial sampling + integrand for all initial samples
+    e = g->arith == MDAS_ARITH_IEEE ? mdas_ieee::initial_sampling(d, (int)L0, cs)
+                                    : mdas_fast::initial_sampling(d, (int)L0, cs);
+    if (e != cudaSuccess) return fail(e);
+    k_set_counts<<<1, 1, 0, cs>>>(d.counts, (int)N0, (int)L0);
+    e = mdas_launch_evaluate(s->desc, s->d_prims, d.coords, d.values, d.D, nullptr, 0, (int)N0, gEval, cs);
+    if (e != cudaSuccess) return fail(e);
+    // the conditional while node
+    cudaStreamCaptureStatus status;
+    cudaGraph_t capGraph = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    e = cudaStreamGetCaptureInfo(cs, &status, nullptr, &capGraph, &deps, nullptr, &ndeps);
+    if (e != cudaSuccess) return fail(e);
+    cudaGraphConditionalHandle handle;
+    e = cudaGraphConditionalHandleCreate(&handle, capGraph, firstPass, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return fail(e);
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t condNode;
+    e = cudaGraphAddNode(&condNode, capGraph, deps, nullptr, ndeps, &cp);
+    if (e != cudaSuccess) return fail(e);
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    e = cudaStreamUpdateCaptureDependencies(cs, &condNode, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return fail(e);
+    // loop body, captured into the conditional node's child graph
+    e = cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return fail(e);
+    cudaError_t eb = launch_errors_auto(g, gErr, bs);
+    if (eb == cudaSuccess) eb = launch_adaptive_on(g, gDecide, gPlace, bs);
+    if (eb == cudaSuccess)
+        eb = mdas_launch_evaluate(s->desc, s->d_prims, d.coords, d.values, d.D, d.counts, 0, 0, gEval, bs);
+    if (eb == cudaSuccess)
+        eb = g->arith == MDAS_ARITH_IEEE ? mdas_ieee::loop_condition(d, handle, budget, kMaxGraphPasses, bs)
+                                         : mdas_fast::loop_condition(d, handle, budget, kMaxGraphPasses, bs);
+    cudaGraph_t bodyOut = nullptr;
+    e = cudaStreamEndCapture(bs, &bodyOut);
+    if (eb != cudaSuccess || e != cudaSuccess) return fail(eb != cudaSuccess ? eb : e);
+    // epilogue: reconstruction
+    e = g->arith == MDAS_ARITH_IEEE ? mdas_ieee::integrate(d, gInt, pixels, width, height, cs)
+                                    : mdas_fast::integrate(d, gInt, pixels, width, height, cs);
+    if (e != cudaSuccess) return fail(e);
+    e = cudaStreamEndCapture(cs, &graph);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    e = cudaGraphInstantiate(&g->graph.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        g->graph.exec = nullptr;
+        return MDAS_ERR_CUDA;
+    }
+    g->graph.scene = s;
+    g->graph.budget = budget;
+    g->graph.pixels = pixels;
+    g->graph.width = width;
+    g->graph.height = height;
+    return MDAS_OK;
+}
+
+}  // namespace
+
+int mdas_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, int width, int height,
+                      mdas_render_stats* stats) {
+    if (!g || !s || !pixels || width <= 0 || height <= 0 || s->desc.dim > g->dg.D) return MDAS_ERR_INVALID;
+    int rc = scene_upload(s, g->stream);
+    if (rc) return rc;
+    flush_timing(g);
+    const RenderGraph& rg = g->graph;
+    if (!rg.exec || rg.scene != s || rg.budget != budget || rg.pixels != pixels || rg.width != width ||
+        rg.height != height) {
+        rc = build_render_graph(g, s, budget, pixels, width, height);
+        if (rc) return rc;
+    }
+    cudaError_t e = cudaGraphLaunch(g->graph.exec, g->stream);
+    g->launches += 1;
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    rc = read_counts(g);  // synchronises the stream
+    if (rc) return rc;
+    g->initialized = true;
+    g->errorsClean = false;
+    g->dirtyValid = g->hcounts->passes > 0;
+    if (stats) {
+        stats->numberOfSamples = g->N;
+        stats->numberOfNodes = g->L;
+        stats->passes = g->hcounts->passes;
+        stats->reserved = 0;
+        for (double& x : stats->stageMs) x = 0.0;
+    }
+    return MDAS_OK;
+}
+
 int mdas_render_host(mdas_grid* g, mdas_scene* s, const float* hostPrims, int budget, float* hostPixels, int width,
                      int height, mdas_render_stats* stats) {
     if (!g || !s || !hostPixels || width <= 0 || height <= 0) return MDAS_ERR_INVALID;
@@ -732,7 +906,7 @@ int mdas_render_host(mdas_grid* g, mdas_scene* s, const float* hostPrims, int bu
                                               cudaMemcpyHostToDevice, g->stream);
         if (e != cudaSuccess) return MDAS_ERR_CUDA;
     }
-    rc = mdas_render(g, s, budget, g->scratch, width, height, stats);
+    rc = mdas_render_graph(g, s, budget, g->scratch, width, height, stats);
     if (rc) return rc;
     cudaError_t e = cudaMemcpyAsync(hostPixels, g->scratch, bytes, cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);

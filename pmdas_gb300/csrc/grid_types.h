@@ -57,7 +57,7 @@ struct MdasDeviceGrid {
 };
 
 // Leaves per thread and per tile of the adaptive pass.
-#define MDAS_LEAVES_PER_THREAD 4
+#define MDAS_LEAVES_PER_THREAD 8
 #define MDAS_TILE_LEAVES (256 * MDAS_LEAVES_PER_THREAD)
 
 #define MDAS_OK 0
@@ -81,6 +81,9 @@ struct MdasDeviceGrid {
     cudaError_t pack_records(const MdasDeviceGrid& g, int L, const int* nodes, const float* boxes,          \
                              cudaStream_t s);                                                               \
     int record_floats(int D);                                                                               \
+    cudaError_t compute_errors_auto(const MdasDeviceGrid& g, int grid, cudaStream_t s);                     \
+    cudaError_t loop_condition(const MdasDeviceGrid& g, cudaGraphConditionalHandle h, int budget,           \
+                               int maxPasses, cudaStream_t s);                                              \
     int max_blocks_per_sm(int D, int which);                                                                \
     }
 

@@ -41,6 +41,54 @@ __global__ void __launch_bounds__(256) k_evaluate(MdasScene sc, const float* __r
     }
 }
 
+// Reference image of an integrand: `spp` samples per pixel, the image plane
+// stratified on a sqrt(spp) x sqrt(spp) grid with jitter, the other dimensions
+// uniform, radiance accumulated in FP64 (the only FP64 work on the GPU).  One
+// thread per pixel; the sample stream is a per-pixel 64-bit LCG (Knuth's
+// MMIX constants), 24 random bits per float.
+struct Lcg64 {
+    unsigned long long s;
+    __device__ float next() {
+        s = s * 6364136223846793005ull + 1442695040888963407ull;
+        return (float)(unsigned)(s >> 40) * (1.0f / 16777216.0f);
+    }
+};
+
+template <int D>
+__global__ void __launch_bounds__(256) k_reference_image(MdasScene sc, const float* __restrict__ prims, int width,
+                                                          int height, int strata, unsigned long long seed,
+                                                          double* __restrict__ out) {
+    extern __shared__ float s_prims[];
+    const int nfl = sc.count * MDAS_PRIM_STRIDE;
+    for (int k = threadIdx.x; k < nfl; k += blockDim.x) s_prims[k] = prims[k];
+    __syncthreads();
+    const int P = width * height;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+        const int x = p % width, y = p / width;
+        Lcg64 rng{seed ^ (0x9E3779B97F4A7C15ull * (unsigned long long)(p + 1))};
+        double acc[3] = {0.0, 0.0, 0.0};
+        const float px = sc.scaleX / (float)width, py = sc.scaleY / (float)height;
+        for (int i = 0; i < strata; ++i) {
+            for (int j = 0; j < strata; ++j) {
+                float c[D];
+                c[0] = ((float)x + ((float)i + rng.next()) / (float)strata) * px;
+                c[1] = ((float)y + ((float)j + rng.next()) / (float)strata) * py;
+#pragma unroll
+                for (int d = 2; d < D; ++d) c[d] = rng.next();
+                float v[3];
+                mdas_shade(&sc, s_prims, c, v);
+                acc[0] += (double)v[0];
+                acc[1] += (double)v[1];
+                acc[2] += (double)v[2];
+            }
+        }
+        const double inv = 1.0 / ((double)strata * (double)strata);
+        out[3 * (size_t)p + 0] = acc[0] * inv;
+        out[3 * (size_t)p + 1] = acc[1] * inv;
+        out[3 * (size_t)p + 2] = acc[2] * inv;
+    }
+}
+
 // splitmix64 (Steele, Lea & Flood, "Fast splittable pseudorandom number
 // generators", OOPSLA 2014): the documented stream every scene is drawn from.
 struct SplitMix64 {
@@ -68,6 +116,18 @@ cudaError_t mdas_launch_evaluate(const MdasScene& sc, const float* d_prims, cons
         case 4: k_evaluate<4><<<grid, 256, smem, s>>>(sc, d_prims, coords, values, counts, offset, count); break;
         case 5: k_evaluate<5><<<grid, 256, smem, s>>>(sc, d_prims, coords, values, counts, offset, count); break;
         case 6: k_evaluate<6><<<grid, 256, smem, s>>>(sc, d_prims, coords, values, counts, offset, count); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t mdas_launch_reference_image(const MdasScene& sc, const float* d_prims, int width, int height, int strata,
+                                        unsigned long long seed, double* out, int grid, cudaStream_t s) {
+    const size_t smem = sizeof(float) * MDAS_PRIM_STRIDE * (size_t)sc.count;
+    switch (sc.dim) {
+        case 3: k_reference_image<3><<<grid, 256, smem, s>>>(sc, d_prims, width, height, strata, seed, out); break;
+        case 4: k_reference_image<4><<<grid, 256, smem, s>>>(sc, d_prims, width, height, strata, seed, out); break;
+        case 5: k_reference_image<5><<<grid, 256, smem, s>>>(sc, d_prims, width, height, strata, seed, out); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -318,10 +318,13 @@ __device__ __forceinline__ float leaf_error(const MdasDeviceGrid& g, int nodeInd
     return error;
 }
 
-template <int D, bool DIRTY>
+// MODE 0: full, 1: dirty, 2: dirty unless no adaptive pass ran since the
+// initial sampling (the device-side budget loop, where passes alternate).
+template <int D, int MODE>
 __global__ void __launch_bounds__(256) k_compute_errors(MdasDeviceGrid g) {
     __shared__ unsigned s_max[8];
     __shared__ unsigned s_cnt[8];
+    const bool DIRTY = MODE == 1 || (MODE == 2 && g.counts->passes > 0);
     int items, newL = 0, firstRight = 0;
     float maxError = 0.0f;
     if (DIRTY) {
@@ -582,7 +585,7 @@ __global__ void __launch_bounds__(1024) k_adaptive_scan(MdasDeviceGrid g) {
 }
 
 template <int D>
-__global__ void __launch_bounds__(256, 3) k_adaptive_place(MdasDeviceGrid g) {
+__global__ void __launch_bounds__(256, 4) k_adaptive_place(MdasDeviceGrid g) {
     constexpr int kMaxNodeSize = 4;
     constexpr int TILE = MDAS_TILE_LEAVES;
     constexpr int NB = NbLayout<D>::FLOATS;
@@ -923,10 +926,34 @@ cudaError_t compute_errors(const MdasDeviceGrid& g, int grid, bool dirty, cudaSt
     cudaError_t e = cudaMemsetAsync(&g.counts->gerr, 0, 2 * sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
     if (dirty) {
-        MDAS_SWITCH_D(g.D, (k_compute_errors<DD, true><<<grid, 256, 0, s>>>(g)));
+        MDAS_SWITCH_D(g.D, (k_compute_errors<DD, 1><<<grid, 256, 0, s>>>(g)));
     } else {
-        MDAS_SWITCH_D(g.D, (k_compute_errors<DD, false><<<grid, 256, 0, s>>>(g)));
+        MDAS_SWITCH_D(g.D, (k_compute_errors<DD, 0><<<grid, 256, 0, s>>>(g)));
     }
+    return cudaGetLastError();
+}
+
+cudaError_t compute_errors_auto(const MdasDeviceGrid& g, int grid, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(&g.counts->gerr, 0, 2 * sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    MDAS_SWITCH_D(g.D, (k_compute_errors<DD, 2><<<grid, 256, 0, s>>>(g)));
+    return cudaGetLastError();
+}
+
+// Condition of the device-side budget loop (optixMotionBlur.cpp:781 plus the
+// capacity guard of :723-724): another pass while N < budget, the next pass
+// fits, no device error, and fewer than maxPasses passes ran (a safety stop:
+// every pass accepts at least the leaf with the largest error, so N grows).
+__global__ void k_loop_condition(const MdasCounts* __restrict__ c, cudaGraphConditionalHandle h, int budget,
+                                 int maxSamples, int maxPasses) {
+    const long long N = c->N, L = c->L;
+    cudaGraphSetConditional(h, (N < budget && N + L <= maxSamples && c->status == 0 && c->passes < maxPasses) ? 1u
+                                                                                                             : 0u);
+}
+
+cudaError_t loop_condition(const MdasDeviceGrid& g, cudaGraphConditionalHandle h, int budget, int maxPasses,
+                           cudaStream_t s) {
+    k_loop_condition<<<1, 1, 0, s>>>(g.counts, h, budget, g.maxSamples, maxPasses);
     return cudaGetLastError();
 }
 
@@ -1006,7 +1033,7 @@ int max_blocks_per_sm(int D, int which) {
     cudaError_t e = cudaSuccess;
     switch (which) {
         case MDAS_K_ERRORS:
-            MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_compute_errors<DD, false>, 256,
+            MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_compute_errors<DD, 0>, 256,
                                                                                  0)));
             break;
         case MDAS_K_ADAPTIVE:

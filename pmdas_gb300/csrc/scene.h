@@ -15,6 +15,9 @@
 cudaError_t mdas_launch_evaluate(const MdasScene& sc, const float* d_prims, const float* coords, float* values,
                                  int dim, const MdasCounts* counts, int offset, int count, int grid, cudaStream_t s);
 
+cudaError_t mdas_launch_reference_image(const MdasScene& sc, const float* d_prims, int width, int height, int strata,
+                                        unsigned long long seed, double* out, int grid, cudaStream_t s);
+
 int mdas_generate_scene(int kind, uint64_t seed, int count, float scaleX, float scaleY, int width, int height,
                         MdasScene* sc, std::vector<float>* prims);
 

@@ -268,6 +268,14 @@ class Scene:
         N.check(self._lib.mdas_scene_evaluate(self._h, coords_ptr, values_ptr, dim, offset, count, stream or 0),
                 "mdas_scene_evaluate")
 
+    def reference_image(self, width: int, height: int, spp: int = 4096, seed: int = 12345):
+        """FP64-accumulated reference image (torch CUDA float64 tensor [H, W, 3])."""
+        import torch
+        out = torch.empty(height, width, 3, dtype=torch.float64, device="cuda")
+        N.check(self._lib.mdas_scene_reference_image(self._h, width, height, spp, seed, out.data_ptr(), 0),
+                "mdas_scene_reference_image")
+        return out
+
     def evaluate(self, grid: KDGrid, offset: int, count: int):
         """launchSubframe: evaluate samples [offset, offset+count) of `grid` in place."""
         N.check(self._lib.mdas_evaluate(grid.handle, self._h, offset, count), "mdas_evaluate")
@@ -278,6 +286,14 @@ def render(grid: KDGrid, scene: Scene, budget: int, pixels, width: int, height: 
     st = N.RenderStats()
     N.check(grid._lib.mdas_render(grid.handle, scene.handle, int(budget), _ptr(pixels), width, height,
                                   C.byref(st)), "mdas_render")
+    return st
+
+
+def render_graph(grid: KDGrid, scene: Scene, budget: int, pixels, width: int, height: int) -> N.RenderStats:
+    """The budget loop as one CUDA graph with a device-side loop (no host sync per pass)."""
+    st = N.RenderStats()
+    N.check(grid._lib.mdas_render_graph(grid.handle, scene.handle, int(budget), _ptr(pixels), width, height,
+                                        C.byref(st)), "mdas_render_graph")
     return st
 
 

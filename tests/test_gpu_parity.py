@@ -97,6 +97,30 @@ def test_render_loop_matches_oracle(cuda):
     assert ok, worst
 
 
+@pytest.mark.parametrize("arith", [P.ARITH_REFERENCE, P.ARITH_IEEE])
+@pytest.mark.parametrize("case", ["mb3d", "dof4d", "mbdof5d"])
+def test_render_graph_equals_host_loop(cuda, arith, case):
+    """The device-side loop (one CUDA graph) leaves exactly the state of the
+    host-driven loop, and a second launch of the cached graph does too."""
+    import torch
+    g1, sc, _, p = make(case, arith)
+    g2 = P.KDGrid(p["D"], g1.GetMaxSamples(), CASES[case][9], CASES[case][5], CASES[case][6], CASES[case][8],
+                  p["sx"], p["sy"], arith=arith)
+    px1 = torch.zeros(p["H"], p["W"], 4, device="cuda")
+    px2 = torch.zeros(p["H"], p["W"], 4, device="cuda")
+    st1 = P.render(g1, sc, p["budget"], px1, p["W"], p["H"])
+    a = g1.dump_state()
+    for launch in range(2):
+        st2 = P.render_graph(g2, sc, p["budget"], px2, p["W"], p["H"])
+        assert (st2.numberOfSamples, st2.numberOfNodes, st2.passes) == \
+            (st1.numberOfSamples, st1.numberOfNodes, st1.passes), launch
+        assert_states_equal(g2.dump_state(), a, keys=("coords", "values", "nodes", "boxes", "errors", "seeds"),
+                            what=f"graph launch {launch}")
+        ok, worst = rel_close(px2.cpu().numpy(), px1.cpu().numpy())
+        assert ok, worst
+    assert g2.Validate()
+
+
 def test_reference_build_close_to_oracle(cuda):
     """The fast-math build differs from IEEE only in the last bits of divisions,
     square roots and powf: same initial grid (power-of-two extents), errors within
@@ -179,6 +203,26 @@ def test_reference_build_matches_reference_kernels(cuda, refgrid_cls, case):
         assert np.array_equal(d, rd)
     finally:
         ref.close()
+
+
+def test_reference_image_and_rel_mse(cuda):
+    """The FP64 reference image converges, and an MDAS image at 16 spp is close to it."""
+    import torch
+    from tests.parity import rel_mse
+    g, sc, _, p = make("dof4d", P.ARITH_REFERENCE)
+    W, H = p["W"], p["H"]
+    ref = sc.reference_image(W, H, spp=4096).cpu().numpy()
+    ref_lo = sc.reference_image(W, H, spp=1024, seed=7).cpu().numpy()
+    assert np.all(np.isfinite(ref)) and ref.min() >= 0.0 and ref.max() <= 1.0 + 1e-12
+    assert rel_mse(ref_lo, ref) < 5e-4  # Monte Carlo noise of the 1024-spp image at disc edges
+    px = torch.zeros(H, W, 4, device="cuda")
+    P.render(g, sc, p["budget"], px, W, H)
+    img = px[..., :3].cpu().numpy()
+    e = rel_mse(img, ref)
+    assert e < 2e-2, e
+    # a flat image of the mean colour is far worse: the sampler resolves the scene
+    flat = np.broadcast_to(ref.mean(axis=(0, 1)), ref.shape)
+    assert rel_mse(flat, ref) > 10 * e
 
 
 # ---- edge cases ------------------------------------------------------------------
