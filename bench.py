@@ -327,6 +327,72 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     return line, wl
 
 
+def run_batch(args, rank: int, world: int, local_rank: int) -> dict:
+    """Config 3: 64 images of uneven resolution, spp and dimension (seeds
+    200-263) in one batched render (one CUDA graph, device-side loop)."""
+    import torch
+
+    import pmdas_gb300 as P
+    from pmdas_gb300.workloads import batch_workloads
+
+    torch.cuda.set_device(local_rank)
+    wls = batch_workloads(200 + 64 * rank, 64)
+    grids, scenes, pix = [], [], []
+    for wl in wls:
+        grids.append(P.KDGrid(wl.dim, wl.maxSamples, wl.candidatesNum, wl.bitsPerDim, wl.extraImgBits, wl.alpha,
+                              wl.scaleX, wl.scaleY, arith=P.ARITH_REFERENCE))
+        scenes.append(P.Scene(wl.scene_kind, wl.scene_seed, wl.scene_count, wl.scaleX, wl.scaleY, wl.width,
+                              wl.height))
+        pix.append(torch.zeros(wl.height, wl.width, 4, device="cuda"))
+    batch = P.Batch(grids, scenes, [w.budget for w in wls], pix, [w.width for w in wls], [w.height for w in wls])
+    best, tuned_ms = batch.autotune(repeats=1)
+    for _ in range(args.warmup):
+        stats = batch.render()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    time.sleep(0.2)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        stats = batch.render()
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    samples = sum(st.numberOfSamples for st in stats)
+    # the same images one after another, each as its own graph render
+    t_single = 0.0
+    for g, sc, p, wl in zip(grids, scenes, pix, wls):
+        P.render_graph(g, sc, wl.budget, p, wl.width, wl.height)  # build + warm
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record()
+        P.render_graph(g, sc, wl.budget, p, wl.width, wl.height)
+        a1.record()
+        torch.cuda.synchronize()
+        t_single += a0.elapsed_time(a1)
+    ms, _, samples = reduce_across_ranks(ms, ms, samples, world, "cuda")
+    value = samples / (ms / 1e3) / 1e6
+    per_image = sorted(((st.numberOfSamples, wl.width, wl.height, wl.dim, wl.spp) for st, wl in zip(stats, wls)))
+    return {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded analytic integrands)",
+        "config": {"workload": "batch64: 64 images, resolution in {256^2, 512^2, 1280x720, 1920x1080}, spp in "
+                               "{4, 8, 16, 32}, 3-D motion blur or 4-D depth of field, seeds 200-263",
+                   "total_samples": samples, "timing": "whole batched render incl. integrand (one CUDA graph)",
+                   "autotuned_ctas_per_sm": best, "autotune_ms": round(tuned_ms, 3)},
+        "per_image_ms": round(ms / len(wls), 4),
+        "sequential_single_image_ms": round(t_single, 3),
+        "batch_speedup_vs_sequential": round(t_single / ms, 3),
+        "images": {"largest_samples": per_image[-1][0], "smallest_samples": per_image[0][0]},
+        "gpu_launches": int(args.steps),
+        "clocks": clk,
+    }
+
+
 def cpu_baseline(wl, threads: int, budget_s: float = 30.0) -> dict:
     """The oracle (CPU restatement of the reference's MDAS step) on the host cores."""
     import pmdas_gb300 as P
@@ -421,6 +487,14 @@ def main():
     if world > 1:
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     from pmdas_gb300 import build as B  # noqa: F401  (the library must already be built)
+    if args.workload == "batch64":
+        line = run_batch(args, rank, world, local_rank)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        if world > 1:
+            torch.distributed.barrier()
+            torch.distributed.destroy_process_group()
+        return
     line, wl = run_gb300(args, rank, world, local_rank)
     if rank == 0:
         if not args.no_cpu_baseline:

@@ -242,6 +242,27 @@ int mdas_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, in
 int mdas_render_host(mdas_grid* g, mdas_scene* s, const float* hostPrims, int budget, float* hostPixels, int width,
                      int height, mdas_render_stats* stats);
 
+/* ---- batched rendering: many images of uneven size, dimension and budget ----
+ * One render of all images of the batch in one CUDA graph: every stage is one
+ * launch per point dimension present (the work items of all images share
+ * each launch), and a device-side loop runs passes until every image reached
+ * its budget (or its capacity).  Each image's result equals what mdas_render
+ * gives for it alone.  The grids and scenes stay owned by the caller; a grid
+ * may appear once; all grids use the same arithmetic and device; up to 256
+ * images.  pixels[i] is a device float4 buffer of widths[i] * heights[i]. */
+typedef struct mdas_batch mdas_batch;
+int mdas_batch_create(mdas_batch** out, int n, mdas_grid* const* grids, mdas_scene* const* scenes,
+                      const int* budgets, float* const* pixels, const int* widths, const int* heights);
+int mdas_batch_destroy(mdas_batch* b);
+/* Renders every image; stats (n entries, caller order) may be NULL. */
+int mdas_batch_render(mdas_batch* b, mdas_render_stats* stats);
+/* Persistent CTAs per SM of the errors, decide, place and integrate/integrand
+ * launches (rebuilds the graph). */
+int mdas_batch_set_tuning(mdas_batch* b, const int* ctasPerSm4);
+/* Times a set of candidate tunings on this batch (`repeats` renders each),
+ * keeps the fastest and returns it with its time per render. */
+int mdas_batch_autotune(mdas_batch* b, int repeats, int* best4, double* bestMs);
+
 /* ---- env configuration (SDK/sutil/Environment.{h,cpp}; the options the MDAS
  *      apps register, optixMotionBlur.cpp:104-137) ---- */
 typedef struct mdas_config {

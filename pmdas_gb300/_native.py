@@ -94,6 +94,12 @@ SIGNATURES = {
     "mdas_render": (_I, [_P, _P, _I, _P, _I, _I, C.POINTER(RenderStats)]),
     "mdas_render_host": (_I, [_P, _P, _P, _I, _P, _I, _I, C.POINTER(RenderStats)]),
     "mdas_render_graph": (_I, [_P, _P, _I, _P, _I, _I, C.POINTER(RenderStats)]),
+    "mdas_batch_create": (_I, [C.POINTER(_P), _I, C.POINTER(_P), C.POINTER(_P), C.POINTER(_I), C.POINTER(_P),
+                               C.POINTER(_I), C.POINTER(_I)]),
+    "mdas_batch_destroy": (_I, [_P]),
+    "mdas_batch_render": (_I, [_P, C.POINTER(RenderStats)]),
+    "mdas_batch_set_tuning": (_I, [_P, C.POINTER(_I)]),
+    "mdas_batch_autotune": (_I, [_P, _I, C.POINTER(_I), C.POINTER(C.c_double)]),
     "mdas_config_defaults": (_I, [C.POINTER(Config)]),
     "mdas_config_read": (_I, [C.c_char_p, C.POINTER(Config), C.c_char_p, _I]),
 }

@@ -41,7 +41,7 @@ UNITS = [
     ("noalloc.cu", FAST),
 ]
 CXX_UNITS = ["env.cpp"]
-HEADERS = ["grid_types.h", "ieee_math.h", "integrand.h", "kdgrid_kernels.cuh", "scene.h"]
+HEADERS = ["grid_types.h", "ieee_math.h", "integrand.h", "kdgrid_kernels.cuh", "batch_kernels.cuh", "scene.h"]
 
 
 def nvcc() -> str:

@@ -1,0 +1,341 @@
+// batch_kernels.cuh — many images of uneven size, dimension and budget in one
+// launch per stage (compiled inside MDAS_NS after kdgrid_kernels.cuh).
+//
+// Each stage enumerates its work items (initial cells, error leaves, tiles of
+// 1024 leaves, accepted leaves, reconstruction leaves) across all images of the
+// launch: every CTA computes the per-image item counts from the images' device
+// counters and their prefix in shared memory, then walks the global item range
+// with a grid stride, mapping each chunk of items to its image by binary search.
+// A chunk never spans two images, so every block-wide step (scan, reduction)
+// stays within one image.  Per image the work and its results are exactly those
+// of the single-image kernels: the item bodies are the same device functions.
+//
+// Images that reached their budget keep `counts->active == 0` and are skipped;
+// the loop condition kernel clears the flag after a pass.
+#pragma once
+
+#include "kdgrid_kernels.cuh"
+
+namespace MDAS_NS {
+
+#define MDAS_MAX_BATCH 256
+
+// Exclusive prefix of per-image chunk counts (n <= 256) in s_pre[0..n]; returns the total.
+template <class F>
+__device__ __forceinline__ int batch_prefix(int n, int* s_pre, unsigned* s_warp, F chunks_of) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned v = threadIdx.x < (unsigned)n ? (unsigned)chunks_of((int)threadIdx.x) : 0u;
+    unsigned incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = lane < 8 ? s_warp[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < 8) s_warp[lane] = w;
+    }
+    __syncthreads();
+    const unsigned excl = (warp ? s_warp[warp - 1] : 0u) + incl - v;
+    if (threadIdx.x < (unsigned)n) s_pre[threadIdx.x] = (int)excl;
+    if (threadIdx.x == 0) s_pre[n] = (int)s_warp[7];
+    __syncthreads();
+    return s_pre[n];
+}
+
+// The image whose chunk range holds chunk c: the last i with s_pre[i] <= c.
+__device__ __forceinline__ int batch_image_of(const int* s_pre, int n, int c) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_pre[mid] <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; }
+
+// ---- initial sampling of every image
+template <int D>
+__global__ void __launch_bounds__(256) k_batch_init(const MdasBatchImage* __restrict__ imgs, int n) {
+    __shared__ __align__(16) float s_coords[256 * 4 * D];
+    __shared__ int s_pre[MDAS_MAX_BATCH + 1];
+    __shared__ unsigned s_warp[8];
+    const int total = batch_prefix(n, s_pre, s_warp, [&](int i) { return ceil_div(imgs[i].initialLeaves, 256); });
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const int i = batch_image_of(s_pre, n, c);
+        init_chunk<D>(imgs[i].g, imgs[i].initialLeaves, (c - s_pre[i]) * 256, s_coords);
+    }
+}
+
+// Counters after the initial sampling; an image takes passes while N < budget
+// and the next pass fits (optixMotionBlur.cpp:781, 723-724).
+__global__ void k_batch_set_counts(const MdasBatchImage* __restrict__ imgs, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    MdasCounts* c = imgs[i].g.counts;
+    const int L = imgs[i].initialLeaves, N = 4 * L;
+    c->N = N;
+    c->L = L;
+    c->newN = 0;
+    c->newL = 0;
+    c->gerr = 0u;
+    c->recomputed = 0;
+    c->status = 0;
+    c->selected = 0;
+    c->passes = 0;
+    c->gathered = 0u;
+    c->gerrNext = 0u;
+    c->active = (N < imgs[i].budget && (long long)N + L <= imgs[i].g.maxSamples) ? 1 : 0;
+}
+
+// Clears the accumulators of the next stage of the active images:
+// which = 0 before the errors pass, 1 before the adaptive pass.
+__global__ void k_batch_reset(const MdasBatchImage* __restrict__ imgs, int n, int which) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    MdasCounts* c = imgs[i].g.counts;
+    if (!c->active) return;
+    if (which == 0) {
+        c->gerr = 0u;
+        c->recomputed = 0;
+    } else {
+        c->gathered = 0u;
+        c->gerrNext = 0u;
+    }
+}
+
+// ---- errors: full on an image's first pass, its split children after
+template <int D>
+__global__ void __launch_bounds__(256) k_batch_errors(const MdasBatchImage* __restrict__ imgs, int n) {
+    __shared__ int s_pre[MDAS_MAX_BATCH + 1];
+    __shared__ unsigned s_warp[8];
+    __shared__ unsigned s_max[8], s_cnt[8];
+    const int total = batch_prefix(n, s_pre, s_warp, [&](int i) {
+        const MdasCounts* c = imgs[i].g.counts;
+        if (!c->active) return 0;
+        const int items = c->passes == 0 ? c->L : 2 * c->newL;
+        return ceil_div(items, 256) > 0 ? ceil_div(items, 256) : 1;  // one chunk carries gerrNext
+    });
+    for (int ch = blockIdx.x; ch < total; ch += gridDim.x) {
+        const int i = batch_image_of(s_pre, n, ch);
+        const MdasDeviceGrid& g = imgs[i].g;
+        const MdasCounts* cnt = g.counts;
+        const bool dirty = cnt->passes > 0;
+        const int newL = cnt->newL;
+        const int items = dirty ? 2 * newL : cnt->L;
+        const int firstRight = cnt->L - newL;
+        const int k = (ch - s_pre[i]) * 256 + threadIdx.x;
+        float maxError = dirty ? __uint_as_float(cnt->gerrNext) : 0.0f;
+        unsigned recomputed = 0;
+        if (k < items) {
+            const int nodeIndex = dirty ? (k < newL ? g.dirty[k] : firstRight + (k - newL)) : k;
+            float error = g.errors[nodeIndex];
+            if (error < 0.0f) {
+                error = leaf_error<D>(g, nodeIndex);
+                g.errors[nodeIndex] = error;
+                recomputed = 1;
+            }
+            maxError = fmaxf(maxError, error);
+        }
+        unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(maxError));
+        unsigned r = __reduce_add_sync(0xffffffffu, recomputed);
+        if ((threadIdx.x & 31) == 0) {
+            s_max[threadIdx.x >> 5] = m;
+            s_cnt[threadIdx.x >> 5] = r;
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            m = threadIdx.x < 8 ? s_max[threadIdx.x] : 0u;
+            r = threadIdx.x < 8 ? s_cnt[threadIdx.x] : 0u;
+            m = __reduce_max_sync(0xffffffffu, m);
+            r = __reduce_add_sync(0xffffffffu, r);
+            if (threadIdx.x == 0) {
+                atomicMax(&g.counts->gerr, m);
+                if (r) atomicAdd(&g.counts->recomputed, (int)r);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---- adaptive pass: decide
+template <int D>
+__global__ void __launch_bounds__(256) k_batch_decide(const MdasBatchImage* __restrict__ imgs, int n) {
+    __shared__ int s_pre[MDAS_MAX_BATCH + 1];
+    __shared__ unsigned s_warp[8];
+    const int total = batch_prefix(n, s_pre, s_warp, [&](int i) {
+        const MdasCounts* c = imgs[i].g.counts;
+        return c->active ? ceil_div(c->L, MDAS_TILE_LEAVES) : 0;
+    });
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        const int i = batch_image_of(s_pre, n, t);
+        const MdasDeviceGrid& g = imgs[i].g;
+        const int L = g.counts->L;
+        const float gError = __uint_as_float(g.counts->gerr);
+        float keptMax = 0.0f;
+        unsigned gathered = 0;
+        decide_tile<D>(g, t - s_pre[i], L, gError, imgs[i].jumpA, imgs[i].jumpC, s_warp, keptMax, gathered);
+        const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(keptMax));
+        const unsigned c = __reduce_add_sync(0xffffffffu, gathered);
+        if ((threadIdx.x & 31) == 0) {
+            if (m) atomicMax(&g.counts->gerrNext, m);
+            if (c) atomicAdd(&g.counts->gathered, c);
+        }
+    }
+}
+
+// ---- adaptive pass: scan (one CTA of 1024 threads per image)
+__global__ void __launch_bounds__(1024) k_batch_scan(const MdasBatchImage* __restrict__ imgs, int n) {
+    __shared__ unsigned s_sel[32], s_split[32];
+    if ((int)blockIdx.x >= n) return;
+    const MdasDeviceGrid& g = imgs[blockIdx.x].g;
+    if (!g.counts->active) return;
+    scan_image(g, s_sel, s_split);
+}
+
+// ---- adaptive pass: place
+template <int D>
+__global__ void __launch_bounds__(256, 4) k_batch_place(const MdasBatchImage* __restrict__ imgs, int n) {
+    __shared__ int s_pre[MDAS_MAX_BATCH + 1];
+    __shared__ unsigned s_warp[8];
+    const int total = batch_prefix(n, s_pre, s_warp, [&](int i) {
+        const MdasDeviceGrid& g = imgs[i].g;
+        return g.counts->active ? ceil_div(g.ctl->L0, MDAS_TILE_LEAVES) : 0;
+    });
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        const int i = batch_image_of(s_pre, n, t);
+        const MdasDeviceGrid& g = imgs[i].g;
+        const int tile = t - s_pre[i];
+        const int tileSel = (int)g.tileCounts[tile].x;
+        if ((int)threadIdx.x >= tileSel) continue;
+        const uint2 pre = g.tilePrefix[tile];
+        const int N = g.ctl->N0, L = g.ctl->L0;
+        for (int r = threadIdx.x; r < tileSel; r += 256) place_entry<D>(g, tile, r, pre, N, L);
+    }
+}
+
+// ---- loop condition over all images of the batch (one CTA of 256 threads)
+__global__ void __launch_bounds__(256) k_batch_condition(const MdasBatchImage* __restrict__ imgs, int n,
+                                                          cudaGraphConditionalHandle h, int maxPasses) {
+    __shared__ int s_any[8];
+    int act = 0;
+    if (threadIdx.x < (unsigned)n) {
+        MdasCounts* c = imgs[threadIdx.x].g.counts;
+        if (c->active) {
+            const long long N = c->N, L = c->L;
+            act = (N < imgs[threadIdx.x].budget && N + L <= imgs[threadIdx.x].g.maxSamples && c->status == 0 &&
+                   c->passes < maxPasses) ? 1 : 0;
+            c->active = act;
+        }
+    }
+    const int any = __reduce_or_sync(0xffffffffu, (unsigned)act);
+    if ((threadIdx.x & 31) == 0) s_any[threadIdx.x >> 5] = any;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int a = 0;
+        for (int w = 0; w < 8; ++w) a |= s_any[w];
+        cudaGraphSetConditional(h, a ? 1u : 0u);
+    }
+}
+
+// ---- reconstruction of every image
+__global__ void k_batch_clear_pixels(const MdasBatchImage* __restrict__ imgs, int n) {
+    const int i = blockIdx.y;
+    if (i >= n) return;
+    const int P = imgs[i].width * imgs[i].height;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x)
+        imgs[i].pixels[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) k_batch_integrate(const MdasBatchImage* __restrict__ imgs, int n) {
+    __shared__ int s_pre[MDAS_MAX_BATCH + 1];
+    __shared__ unsigned s_warp[8];
+    const int total = batch_prefix(n, s_pre, s_warp, [&](int i) { return ceil_div(imgs[i].g.counts->L, 256); });
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const int i = batch_image_of(s_pre, n, c);
+        const int leaf = (c - s_pre[i]) * 256 + threadIdx.x;
+        if (leaf < imgs[i].g.counts->L)
+            integrate_leaf<D>(imgs[i].g, leaf, imgs[i].pixels, imgs[i].width, imgs[i].height);
+    }
+}
+
+// ---- host launchers (one group of images of one point dimension)
+#define MDAS_BATCH_SWITCH_D(D, EXPR)           \
+    switch (D) {                               \
+        case 3: { constexpr int DD = 3; EXPR; } break; \
+        case 4: { constexpr int DD = 4; EXPR; } break; \
+        case 5: { constexpr int DD = 5; EXPR; } break; \
+        case 6: { constexpr int DD = 6; EXPR; } break; \
+        default: return cudaErrorInvalidValue; \
+    }
+
+cudaError_t batch_init(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s) {
+    MDAS_BATCH_SWITCH_D(D, (k_batch_init<DD><<<grid, 256, 0, s>>>(imgs, n)));
+    return cudaGetLastError();
+}
+
+cudaError_t batch_set_counts(const MdasBatchImage* imgs, int n, cudaStream_t s) {
+    k_batch_set_counts<<<(n + 255) / 256, 256, 0, s>>>(imgs, n);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_errors(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s) {
+    MDAS_BATCH_SWITCH_D(D, (k_batch_errors<DD><<<grid, 256, 0, s>>>(imgs, n)));
+    return cudaGetLastError();
+}
+
+cudaError_t batch_reset(const MdasBatchImage* imgs, int n, int which, cudaStream_t s) {
+    k_batch_reset<<<(n + 255) / 256, 256, 0, s>>>(imgs, n, which);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_decide(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s) {
+    MDAS_BATCH_SWITCH_D(D, (k_batch_decide<DD><<<grid, 256, 0, s>>>(imgs, n)));
+    return cudaGetLastError();
+}
+
+cudaError_t batch_scan(const MdasBatchImage* imgs, int n, cudaStream_t s) {
+    k_batch_scan<<<n, 1024, 0, s>>>(imgs, n);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_place(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s) {
+    MDAS_BATCH_SWITCH_D(D, (k_batch_place<DD><<<grid, 256, 0, s>>>(imgs, n)));
+    return cudaGetLastError();
+}
+
+cudaError_t batch_condition(const MdasBatchImage* imgs, int n, cudaGraphConditionalHandle h, int maxPasses,
+                            cudaStream_t s) {
+    k_batch_condition<<<1, 256, 0, s>>>(imgs, n, h, maxPasses);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_integrate(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s) {
+    MDAS_BATCH_SWITCH_D(D, (k_batch_integrate<DD><<<grid, 256, 0, s>>>(imgs, n)));
+    return cudaGetLastError();
+}
+
+cudaError_t batch_clear_pixels(const MdasBatchImage* imgs, int n, cudaStream_t s) {
+    k_batch_clear_pixels<<<dim3(64, n), 256, 0, s>>>(imgs, n);
+    return cudaGetLastError();
+}
+
+unsigned batch_jump(int candidatesNum, int D, unsigned* C) {
+    unsigned A;
+    lcg_jump((unsigned)(candidatesNum * D), &A, C);
+    return A;
+}
+
+#undef MDAS_BATCH_SWITCH_D
+
+}  // namespace MDAS_NS

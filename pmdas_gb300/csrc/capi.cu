@@ -32,6 +32,7 @@ __global__ void k_set_counts(MdasCounts* c, int N, int L) {
     c->passes = 0;
     c->gathered = 0u;
     c->gerrNext = 0u;
+    c->active = 1;
 }
 
 struct PendingTiming {
@@ -891,6 +892,282 @@ int mdas_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, in
         for (double& x : stats->stageMs) x = 0.0;
     }
     return MDAS_OK;
+}
+
+// ---- batched rendering ------------------------------------------------------------------
+struct mdas_batch {
+    int n = 0;
+    int arith = 0;
+    int numSMs = 1;
+    std::vector<mdas_grid*> grids;  // caller order
+    std::vector<int> order;          // batch slot -> caller index (images grouped by dimension)
+    struct Group {
+        int D, offset, count;
+    };
+    std::vector<Group> groups;
+    std::vector<MdasBatchImage> himgs;
+    std::vector<MdasBatchScene> hscenes;
+    MdasBatchImage* d_imgs = nullptr;
+    MdasBatchScene* d_scenes = nullptr;
+    bool anyActive = false;
+    cudaStream_t stream = nullptr, captureStream = nullptr, bodyStream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int tune[4] = {4, 4, 4, 8};  // persistent CTAs per SM: errors, decide, place, integrate/integrand
+    uint64_t launches = 0;
+};
+
+namespace {
+
+#define MDAS_ARITH_CALL(b, FN, ...) \
+    ((b)->arith == MDAS_ARITH_IEEE ? mdas_ieee::FN(__VA_ARGS__) : mdas_fast::FN(__VA_ARGS__))
+
+// Graph of one batched render: initial sampling and integrand of every image,
+// then a device-side loop of passes over the still-active images, then
+// reconstruction.  Every stage is one launch per point dimension present.
+int build_batch_graph(mdas_batch* b) {
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    cudaStream_t cs = b->captureStream, bs = b->bodyStream;
+    const int gErr = b->numSMs * b->tune[0], gDec = b->numSMs * b->tune[1], gPl = b->numSMs * b->tune[2];
+    const int gInt = b->numSMs * b->tune[3];
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    auto fail = [&]() {
+        cudaGraph_t junk = nullptr;
+        cudaStreamEndCapture(cs, &junk);
+        if (junk) cudaGraphDestroy(junk);
+        cudaGetLastError();
+        return MDAS_ERR_CUDA;
+    };
+    for (const auto& gr : b->groups) {
+        e = MDAS_ARITH_CALL(b, batch_init, b->d_imgs + gr.offset, gr.count, gr.D, gInt, cs);
+        if (e != cudaSuccess) return fail();
+    }
+    e = MDAS_ARITH_CALL(b, batch_set_counts, b->d_imgs, b->n, cs);
+    if (e != cudaSuccess) return fail();
+    for (const auto& gr : b->groups) {
+        e = mdas_launch_evaluate_batch(b->d_scenes + gr.offset, gr.count, gr.D, 1, gInt, cs);
+        if (e != cudaSuccess) return fail();
+    }
+    cudaStreamCaptureStatus status;
+    cudaGraph_t capGraph = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    if (cudaStreamGetCaptureInfo(cs, &status, nullptr, &capGraph, &deps, nullptr, &ndeps) != cudaSuccess) return fail();
+    cudaGraphConditionalHandle handle;
+    if (cudaGraphConditionalHandleCreate(&handle, capGraph, b->anyActive ? 1u : 0u, cudaGraphCondAssignDefault) !=
+        cudaSuccess)
+        return fail();
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t condNode;
+    if (cudaGraphAddNode(&condNode, capGraph, deps, nullptr, ndeps, &cp) != cudaSuccess) return fail();
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if (cudaStreamUpdateCaptureDependencies(cs, &condNode, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess)
+        return fail();
+    if (cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+        return fail();
+    cudaError_t eb = MDAS_ARITH_CALL(b, batch_reset, b->d_imgs, b->n, 0, bs);
+    for (const auto& gr : b->groups)
+        if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_errors, b->d_imgs + gr.offset, gr.count, gr.D, gErr, bs);
+    if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_reset, b->d_imgs, b->n, 1, bs);
+    for (const auto& gr : b->groups)
+        if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_decide, b->d_imgs + gr.offset, gr.count, gr.D, gDec, bs);
+    if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_scan, b->d_imgs, b->n, bs);
+    for (const auto& gr : b->groups)
+        if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_place, b->d_imgs + gr.offset, gr.count, gr.D, gPl, bs);
+    for (const auto& gr : b->groups)
+        if (eb == cudaSuccess) eb = mdas_launch_evaluate_batch(b->d_scenes + gr.offset, gr.count, gr.D, 0, gInt, bs);
+    if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_condition, b->d_imgs, b->n, handle, kMaxGraphPasses, bs);
+    cudaGraph_t bodyOut = nullptr;
+    e = cudaStreamEndCapture(bs, &bodyOut);
+    if (eb != cudaSuccess || e != cudaSuccess) return fail();
+    e = MDAS_ARITH_CALL(b, batch_clear_pixels, b->d_imgs, b->n, cs);
+    for (const auto& gr : b->groups)
+        if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_integrate, b->d_imgs + gr.offset, gr.count, gr.D, gInt, cs);
+    if (e != cudaSuccess) return fail();
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamEndCapture(cs, &graph) != cudaSuccess) return MDAS_ERR_CUDA;
+    e = cudaGraphInstantiate(&b->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        b->exec = nullptr;
+        return MDAS_ERR_CUDA;
+    }
+    return MDAS_OK;
+}
+
+void free_batch(mdas_batch* b) {
+    if (!b) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->captureStream) cudaStreamDestroy(b->captureStream);
+    if (b->bodyStream) cudaStreamDestroy(b->bodyStream);
+    cudaFree(b->d_imgs);
+    cudaFree(b->d_scenes);
+    delete b;
+}
+
+}  // namespace
+
+int mdas_batch_create(mdas_batch** out, int n, mdas_grid* const* grids, mdas_scene* const* scenes,
+                      const int* budgets, float* const* pixels, const int* widths, const int* heights) {
+    if (!out || n < 1 || n > 256 || !grids || !scenes || !budgets || !pixels || !widths || !heights)
+        return MDAS_ERR_INVALID;
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        if (!grids[i] || !scenes[i] || !pixels[i] || widths[i] <= 0 || heights[i] <= 0 ||
+            scenes[i]->desc.dim > grids[i]->dg.D || grids[i]->arith != grids[0]->arith ||
+            grids[i]->device != grids[0]->device)
+            return MDAS_ERR_INVALID;
+        for (int j = 0; j < i; ++j)
+            if (grids[j] == grids[i]) return MDAS_ERR_INVALID;  // one image per grid
+    }
+    mdas_batch* b = new (std::nothrow) mdas_batch();
+    if (!b) return MDAS_ERR_ALLOC;
+    b->n = n;
+    b->arith = grids[0]->arith;
+    b->numSMs = grids[0]->numSMs;
+    b->stream = grids[0]->stream;
+    b->grids.assign(grids, grids + n);
+    for (int D = 3; D <= 6; ++D) {
+        const int off = (int)b->order.size();
+        for (int i = 0; i < n; ++i)
+            if (grids[i]->dg.D == D) b->order.push_back(i);
+        if ((int)b->order.size() > off) b->groups.push_back({D, off, (int)b->order.size() - off});
+    }
+    for (int slot = 0; slot < n; ++slot) {
+        const int i = b->order[slot];
+        mdas_grid* g = grids[i];
+        int rc = scene_upload(scenes[i], g->stream);
+        if (rc) {
+            free_batch(b);
+            return rc;
+        }
+        MdasBatchImage im{};
+        im.g = g->dg;
+        im.pixels = reinterpret_cast<float4*>(pixels[i]);
+        im.width = widths[i];
+        im.height = heights[i];
+        im.budget = budgets[i];
+        const int64_t L0 = ((int64_t)1 << (g->dg.bitsPerDim * g->dg.D)) << (2 * g->dg.extraImgBits);
+        if (4 * L0 > g->dg.maxSamples) {
+            free_batch(b);
+            return MDAS_ERR_CAPACITY;
+        }
+        im.initialLeaves = (int)L0;
+        im.jumpA = (b->arith == MDAS_ARITH_IEEE) ? mdas_ieee::batch_jump(g->dg.candidatesNum, g->dg.D, &im.jumpC)
+                                                 : mdas_fast::batch_jump(g->dg.candidatesNum, g->dg.D, &im.jumpC);
+        if (4 * L0 < budgets[i] && 5 * L0 <= g->dg.maxSamples) b->anyActive = true;
+        b->himgs.push_back(im);
+        MdasBatchScene bs{};
+        bs.sc = scenes[i]->desc;
+        bs.prims = scenes[i]->d_prims;
+        bs.counts = g->dg.counts;
+        bs.coords = g->dg.coords;
+        bs.values = g->dg.values;
+        bs.dim = g->dg.D;
+        bs.initialSamples = (int)(4 * L0);
+        b->hscenes.push_back(bs);
+    }
+    bool ok = cudaMalloc(&b->d_imgs, sizeof(MdasBatchImage) * n) == cudaSuccess &&
+              cudaMalloc(&b->d_scenes, sizeof(MdasBatchScene) * n) == cudaSuccess &&
+              cudaMemcpy(b->d_imgs, b->himgs.data(), sizeof(MdasBatchImage) * n, cudaMemcpyHostToDevice) ==
+                  cudaSuccess &&
+              cudaMemcpy(b->d_scenes, b->hscenes.data(), sizeof(MdasBatchScene) * n, cudaMemcpyHostToDevice) ==
+                  cudaSuccess &&
+              cudaStreamCreateWithFlags(&b->captureStream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&b->bodyStream, cudaStreamNonBlocking) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        free_batch(b);
+        return MDAS_ERR_ALLOC;
+    }
+    int rc = build_batch_graph(b);
+    if (rc) {
+        free_batch(b);
+        return rc;
+    }
+    *out = b;
+    return MDAS_OK;
+}
+
+int mdas_batch_destroy(mdas_batch* b) {
+    if (!b) return MDAS_ERR_INVALID;
+    cudaStreamSynchronize(b->stream);
+    free_batch(b);
+    return MDAS_OK;
+}
+
+int mdas_batch_render(mdas_batch* b, mdas_render_stats* stats) {
+    if (!b || !b->exec) return MDAS_ERR_INVALID;
+    cudaError_t e = cudaGraphLaunch(b->exec, b->stream);
+    b->launches += 1;
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess) return MDAS_ERR_CUDA;
+    int status = MDAS_OK;
+    for (int i = 0; i < b->n; ++i) {
+        mdas_grid* g = b->grids[i];
+        const int rc = read_counts(g);
+        if (rc && !status) status = rc;
+        g->initialized = true;
+        g->errorsClean = false;
+        g->dirtyValid = g->hcounts->passes > 0;
+        if (stats) {
+            stats[i].numberOfSamples = g->N;
+            stats[i].numberOfNodes = g->L;
+            stats[i].passes = g->hcounts->passes;
+            stats[i].reserved = 0;
+            for (double& x : stats[i].stageMs) x = 0.0;
+        }
+    }
+    return status;
+}
+
+int mdas_batch_set_tuning(mdas_batch* b, const int* ctasPerSm4) {
+    if (!b || !ctasPerSm4) return MDAS_ERR_INVALID;
+    for (int k = 0; k < 4; ++k)
+        if (ctasPerSm4[k] < 1 || ctasPerSm4[k] > 32) return MDAS_ERR_INVALID;
+    for (int k = 0; k < 4; ++k) b->tune[k] = ctasPerSm4[k];
+    return build_batch_graph(b);
+}
+
+int mdas_batch_autotune(mdas_batch* b, int repeats, int* best4, double* bestMs) {
+    if (!b || repeats < 1) return MDAS_ERR_INVALID;
+    // candidate persistent-grid sizes (CTAs per SM) for errors, decide, place, integrate/integrand
+    static const int cand[][4] = {{2, 2, 2, 4}, {4, 4, 4, 8}, {6, 6, 4, 8}, {8, 8, 4, 16}, {4, 8, 2, 8},
+                                  {6, 8, 3, 12}};
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return MDAS_ERR_CUDA;
+    double best = 1e30;
+    int bi = 1;
+    for (int c = 0; c < (int)(sizeof(cand) / sizeof(cand[0])); ++c) {
+        int rc = mdas_batch_set_tuning(b, cand[c]);
+        if (rc) return rc;
+        cudaGraphLaunch(b->exec, b->stream);  // warm
+        cudaEventRecord(e0, b->stream);
+        for (int r = 0; r < repeats; ++r) cudaGraphLaunch(b->exec, b->stream);
+        cudaEventRecord(e1, b->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) return MDAS_ERR_CUDA;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        b->launches += repeats + 1;
+        if (ms / repeats < best) {
+            best = ms / repeats;
+            bi = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int rc = mdas_batch_set_tuning(b, cand[bi]);
+    if (best4)
+        for (int k = 0; k < 4; ++k) best4[k] = cand[bi][k];
+    if (bestMs) *bestMs = best;
+    return rc;
 }
 
 int mdas_render_host(mdas_grid* g, mdas_scene* s, const float* hostPrims, int budget, float* hostPixels, int width,

@@ -19,7 +19,7 @@ struct MdasCounts {
     int passes;      // adaptive passes since the initial sampling
     unsigned gathered;  // sample coordinates read by the last adaptive pass
     unsigned gerrNext;  // max error of the leaves the last adaptive pass did not split (reset with gathered)
-    int pad;
+    int active;         // batched rendering: 1 while this image still takes passes
 };
 
 // Scratch of one adaptive pass: the counts before it, for the place kernel.
@@ -56,6 +56,17 @@ struct MdasDeviceGrid {
     int* dirty;           // [maxNodes/2 + 1], slots of the left children of the last pass's splits
 };
 
+// One image of a batched render (device-side descriptor).
+struct MdasBatchImage {
+    MdasDeviceGrid g;
+    float4* pixels;
+    int width, height;
+    int budget;
+    int initialLeaves;
+    unsigned jumpA, jumpC;  // LCG jump-ahead over the candidate draws of one accepted leaf
+    int pad[2];
+};
+
 // Leaves per thread and per tile of the adaptive pass.
 #define MDAS_LEAVES_PER_THREAD 8
 #define MDAS_TILE_LEAVES (256 * MDAS_LEAVES_PER_THREAD)
@@ -82,6 +93,18 @@ struct MdasDeviceGrid {
                              cudaStream_t s);                                                               \
     int record_floats(int D);                                                                               \
     cudaError_t compute_errors_auto(const MdasDeviceGrid& g, int grid, cudaStream_t s);                     \
+    cudaError_t batch_init(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s);              \
+    cudaError_t batch_set_counts(const MdasBatchImage* imgs, int n, cudaStream_t s);                         \
+    cudaError_t batch_errors(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s);            \
+    cudaError_t batch_reset(const MdasBatchImage* imgs, int n, int which, cudaStream_t s);                   \
+    cudaError_t batch_decide(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s);            \
+    cudaError_t batch_scan(const MdasBatchImage* imgs, int n, cudaStream_t s);                               \
+    cudaError_t batch_place(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s);             \
+    cudaError_t batch_condition(const MdasBatchImage* imgs, int n, cudaGraphConditionalHandle h,             \
+                                int maxPasses, cudaStream_t s);                                              \
+    cudaError_t batch_integrate(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s);         \
+    cudaError_t batch_clear_pixels(const MdasBatchImage* imgs, int n, cudaStream_t s);                       \
+    unsigned batch_jump(int candidatesNum, int D, unsigned* C);                                              \
     cudaError_t loop_condition(const MdasDeviceGrid& g, cudaGraphConditionalHandle h, int budget,           \
                                int maxPasses, cudaStream_t s);                                              \
     int max_blocks_per_sm(int D, int which);                                                                \

@@ -41,6 +41,65 @@ __global__ void __launch_bounds__(256) k_evaluate(MdasScene sc, const float* __r
     }
 }
 
+// Batched integrand: chunks of 256 samples across the images of one launch
+// (same enumeration scheme as the batched MDAS kernels); primitives are read
+// from global memory (L1/L2-resident), as several scenes share a launch.
+template <int D>
+__global__ void __launch_bounds__(256) k_evaluate_batch(const MdasBatchScene* __restrict__ scenes, int n, int all) {
+    __shared__ int s_pre[257];
+    __shared__ unsigned s_warp[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned v = 0;
+    if (threadIdx.x < (unsigned)n) {
+        const MdasCounts* c = scenes[threadIdx.x].counts;
+        const int items = all ? scenes[threadIdx.x].initialSamples : (c->active ? c->newN : 0);
+        v = (unsigned)((items + 255) / 256);
+    }
+    unsigned incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = lane < 8 ? s_warp[lane] : 0u;
+        for (int o = 1; o < 8; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < 8) s_warp[lane] = w;
+    }
+    __syncthreads();
+    if (threadIdx.x < (unsigned)n) s_pre[threadIdx.x] = (int)((warp ? s_warp[warp - 1] : 0u) + incl - v);
+    if (threadIdx.x == 0) s_pre[n] = (int)s_warp[7];
+    __syncthreads();
+    const int total = s_pre[n];
+    for (int ch = blockIdx.x; ch < total; ch += gridDim.x) {
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_pre[mid] <= ch) lo = mid;
+            else hi = mid - 1;
+        }
+        const MdasBatchScene& b = scenes[lo];
+        const int offset = all ? 0 : b.counts->N - b.counts->newN;
+        const int count = all ? b.initialSamples : b.counts->newN;
+        const int k = (ch - s_pre[lo]) * 256 + threadIdx.x;
+        if (k < count) {
+            const size_t s = (size_t)offset + k;
+            float c[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) c[d] = b.coords[s * D + d];
+            float out[3];
+            mdas_shade(&b.sc, b.prims, c, out);
+            b.values[3 * s + 0] = out[0];
+            b.values[3 * s + 1] = out[1];
+            b.values[3 * s + 2] = out[2];
+        }
+    }
+}
+
 // Reference image of an integrand: `spp` samples per pixel, the image plane
 // stratified on a sqrt(spp) x sqrt(spp) grid with jitter, the other dimensions
 // uniform, radiance accumulated in FP64 (the only FP64 work on the GPU).  One
@@ -116,6 +175,17 @@ cudaError_t mdas_launch_evaluate(const MdasScene& sc, const float* d_prims, cons
         case 4: k_evaluate<4><<<grid, 256, smem, s>>>(sc, d_prims, coords, values, counts, offset, count); break;
         case 5: k_evaluate<5><<<grid, 256, smem, s>>>(sc, d_prims, coords, values, counts, offset, count); break;
         case 6: k_evaluate<6><<<grid, 256, smem, s>>>(sc, d_prims, coords, values, counts, offset, count); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t mdas_launch_evaluate_batch(const MdasBatchScene* scenes, int n, int D, int all, int grid, cudaStream_t s) {
+    switch (D) {
+        case 3: k_evaluate_batch<3><<<grid, 256, 0, s>>>(scenes, n, all); break;
+        case 4: k_evaluate_batch<4><<<grid, 256, 0, s>>>(scenes, n, all); break;
+        case 5: k_evaluate_batch<5><<<grid, 256, 0, s>>>(scenes, n, all); break;
+        case 6: k_evaluate_batch<6><<<grid, 256, 0, s>>>(scenes, n, all); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

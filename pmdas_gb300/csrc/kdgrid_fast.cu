@@ -5,3 +5,4 @@
 #define MDAS_NS mdas_fast
 #define MDAS_REFERENCE_ARITH 1
 #include "kdgrid_kernels.cuh"
+#include "batch_kernels.cuh"

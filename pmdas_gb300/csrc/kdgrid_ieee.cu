@@ -4,3 +4,4 @@
 // -ffp-contract=off reproduces every bit of every pass.
 #define MDAS_NS mdas_ieee
 #include "kdgrid_kernels.cuh"
+#include "batch_kernels.cuh"

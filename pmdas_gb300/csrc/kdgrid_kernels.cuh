@@ -192,71 +192,75 @@ __device__ __forceinline__ int node_get(const int4 n, int i) {
 // The AoS sample coordinates are staged in shared memory and written out as
 // contiguous 16-byte vectors.
 // =====================================================================================
+// initial sampling of the 256 leaves [base, base + 256) of a grid with L initial leaves
 template <int D>
-__global__ void __launch_bounds__(256) k_initial_sampling(MdasDeviceGrid g, int L) {
+__device__ __forceinline__ void init_chunk(const MdasDeviceGrid& g, int L, int base, float* s_coords) {
     constexpr int NB = NbLayout<D>::FLOATS;
-    __shared__ __align__(16) float s_coords[256 * 4 * D];
     const int bpd = g.bitsPerDim, eib = g.extraImgBits;
-    for (int base = blockIdx.x * 256; base < L; base += gridDim.x * 256) {
-        const int nodeIndex = base + threadIdx.x;
-        const int n = min(256, L - base);
-        if (nodeIndex < L) {
-            float offset[D], extent[D];
+    const int nodeIndex = base + threadIdx.x;
+    const int n = min(256, L - base);
+    if (nodeIndex < L) {
+        float offset[D], extent[D];
 #pragma unroll
-            for (int j = 0; j < D; ++j) {
-                unsigned xq = 0;
-                unsigned extentInv = 1u << bpd;
-                for (int k = 0; k < bpd; ++k) {
-                    const int i = D * k + (D - j - 1);
+        for (int j = 0; j < D; ++j) {
+            unsigned xq = 0;
+            unsigned extentInv = 1u << bpd;
+            for (int k = 0; k < bpd; ++k) {
+                const int i = D * k + (D - j - 1);
+                xq |= (unsigned)((nodeIndex >> i) & 1) << k;
+            }
+            if (j < 2) {
+                for (int k = bpd; k < bpd + eib; ++k) {
+                    const int i = D * bpd + 2 * (k - bpd) + 1 - j;
                     xq |= (unsigned)((nodeIndex >> i) & 1) << k;
                 }
-                if (j < 2) {
-                    for (int k = bpd; k < bpd + eib; ++k) {
-                        const int i = D * bpd + 2 * (k - bpd) + 1 - j;
-                        xq |= (unsigned)((nodeIndex >> i) & 1) << k;
-                    }
-                    extentInv <<= eib;
-                }
-                extent[j] = 1.0f / float(extentInv);
-                offset[j] = xq * extent[j];
+                extentInv <<= eib;
             }
-            offset[0] *= g.scaleX;
-            offset[1] *= g.scaleY;
-            extent[0] *= g.scaleX;
-            extent[1] *= g.scaleY;
+            extent[j] = 1.0f / float(extentInv);
+            offset[j] = xq * extent[j];
+        }
+        offset[0] *= g.scaleX;
+        offset[1] *= g.scaleY;
+        extent[0] *= g.scaleX;
+        extent[1] *= g.scaleY;
 
-            unsigned seed = tea4((unsigned)nodeIndex, 0);
+        unsigned seed = tea4((unsigned)nodeIndex, 0);
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                float r[D];
+        for (int j = 0; j < 4; ++j) {
+            float r[D];
 #pragma unroll
-                for (int i = 0; i < D; ++i) r[i] = rnd(seed);
+            for (int i = 0; i < D; ++i) r[i] = rnd(seed);
 #pragma unroll
-                for (int i = 0; i < D; ++i) s_coords[(threadIdx.x * 4 + j) * D + i] = offset[i] + r[i] * extent[i];
-            }
-            g.seeds[nodeIndex] = seed;
-            g.errors[nodeIndex] = -1.0f;
-            const int s0 = 4 * nodeIndex;
-            float mx[D];
-#pragma unroll
-            for (int i = 0; i < D; ++i) mx[i] = offset[i] + extent[i];
-            nb_store<D>(g.nb + (size_t)nodeIndex * NB, make_int4(s0, s0 + 1, s0 + 2, s0 + 3), offset, mx);
+            for (int i = 0; i < D; ++i) s_coords[(threadIdx.x * 4 + j) * D + i] = offset[i] + r[i] * extent[i];
         }
-        __syncthreads();
-        {
-            // 4*D floats per leaf, leaf `base` starts at a 16*D-byte boundary; an initial
-            // leaf's private sample copy has the same layout as its 4 AoS samples
-            float4* dst = reinterpret_cast<float4*>(g.coords + (size_t)base * 4 * D);
-            float4* dsl = reinterpret_cast<float4*>(g.lsc + (size_t)base * 4 * D);
-            const float4* src = reinterpret_cast<const float4*>(s_coords);
-            for (int k = threadIdx.x; k < n * D; k += 256) {
-                const float4 v = src[k];
-                dst[k] = v;
-                dsl[k] = v;
-            }
-        }
-        __syncthreads();
+        g.seeds[nodeIndex] = seed;
+        g.errors[nodeIndex] = -1.0f;
+        const int s0 = 4 * nodeIndex;
+        float mx[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) mx[i] = offset[i] + extent[i];
+        nb_store<D>(g.nb + (size_t)nodeIndex * NB, make_int4(s0, s0 + 1, s0 + 2, s0 + 3), offset, mx);
     }
+    __syncthreads();
+    {
+        // 4*D floats per leaf, leaf `base` starts at a 16*D-byte boundary; an initial
+        // leaf's private sample copy has the same layout as its 4 AoS samples
+        float4* dst = reinterpret_cast<float4*>(g.coords + (size_t)base * 4 * D);
+        float4* dsl = reinterpret_cast<float4*>(g.lsc + (size_t)base * 4 * D);
+        const float4* src = reinterpret_cast<const float4*>(s_coords);
+        for (int k = threadIdx.x; k < n * D; k += 256) {
+            const float4 v = src[k];
+            dst[k] = v;
+            dsl[k] = v;
+        }
+    }
+    __syncthreads();
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) k_initial_sampling(MdasDeviceGrid g, int L) {
+    __shared__ __align__(16) float s_coords[256 * 4 * D];
+    for (int base = blockIdx.x * 256; base < L; base += gridDim.x * 256) init_chunk<D>(g, L, base, s_coords);
 }
 
 // =====================================================================================
@@ -399,118 +403,124 @@ __device__ __forceinline__ unsigned acc_pack(unsigned local, unsigned splitRank,
     return local | (splitRank << 11) | (split << 22) | (cnt << 23);
 }
 
+// decide, one tile: acceptance of the tile's leaves, final seeds, the tile's
+// counts and its compacted accepted list (shared by the single-image and the
+// batched kernels).
 template <int D>
-__global__ void __launch_bounds__(256) k_adaptive_decide(MdasDeviceGrid g, unsigned jumpA, unsigned jumpC) {
+__device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, int L, float gError, unsigned jumpA,
+                                            unsigned jumpC, unsigned* s_warp, float& keptMax, unsigned& gathered) {
     constexpr int kMaxNodeSize = 4;  // KDGrid ctor: maxNodeSize(4), kdgrid.cu:611
     constexpr int K = MDAS_LEAVES_PER_THREAD;
     constexpr int TILE = MDAS_TILE_LEAVES;
     constexpr int NB = NbLayout<D>::FLOATS;
     static_assert(TILE == 256 * K && TILE <= 2048, "tile = 256 threads x K leaves, local index in 11 bits");
-    __shared__ unsigned s_warp[8];
-
-    const int L = g.counts->L;
-    const float gError = __uint_as_float(g.counts->gerr);
-    const int ntiles = (L + TILE - 1) / TILE;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
+    const int i0 = tile * TILE + threadIdx.x * K;
+    const bool full = i0 + K <= L;
+    float err[K];
+    unsigned sd[K];
+    if (full) {
+#pragma unroll
+        for (int q = 0; q < K; q += 4) {
+            const float4 e4 = *reinterpret_cast<const float4*>(g.errors + i0 + q);
+            const uint4 s4 = *reinterpret_cast<const uint4*>(g.seeds + i0 + q);
+            err[q] = e4.x; err[q + 1] = e4.y; err[q + 2] = e4.z; err[q + 3] = e4.w;
+            sd[q] = s4.x; sd[q + 1] = s4.y; sd[q + 2] = s4.z; sd[q + 3] = s4.w;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            const bool v = i0 + j < L;
+            err[j] = v ? g.errors[i0 + j] : 0.0f;
+            sd[j] = v ? g.seeds[i0 + j] : 0u;
+        }
+    }
+    unsigned accMask = 0;
+    unsigned seedAcc[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        const int leaf = i0 + j;
+        unsigned seed = sd[j];
+        if (seed == 0) seed = tea4((unsigned)leaf, 0);
+        bool a = false;
+        if (leaf < L) a = mdas_pow(err[j] / gError, g.alpha) >= rnd(seed);
+        seedAcc[j] = seed;
+        sd[j] = a ? jumpA * seed + jumpC : seed;  // the seed after the candidate draws
+        if (a) accMask |= 1u << j;
+    }
+    int cnt[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) cnt[j] = ((accMask >> j) & 1u) ? node_count(nb_node(g.nb + (size_t)(i0 + j) * NB)) : 0;
+    unsigned splitMask = 0;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        gathered += (unsigned)cnt[j];
+        if (cnt[j] >= kMaxNodeSize) splitMask |= 1u << j;
+        if (i0 + j < L && !((splitMask >> j) & 1u)) keptMax = fmaxf(keptMax, err[j]);
+    }
+    if (full) {
+#pragma unroll
+        for (int q = 0; q < K; q += 4)
+            *reinterpret_cast<uint4*>(g.seeds + i0 + q) = make_uint4(sd[q], sd[q + 1], sd[q + 2], sd[q + 3]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < K; ++j)
+            if (i0 + j < L) g.seeds[i0 + j] = sd[j];
+    }
+
+    // block scan of (accepted, split) counts, packed lo16 | hi16
+    const unsigned flag = (unsigned)__popc(accMask) | ((unsigned)__popc(splitMask) << 16);
+    unsigned incl = flag;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = lane < 8 ? s_warp[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < 8) s_warp[lane] = w;
+    }
+    __syncthreads();
+    const unsigned excl = (warp ? s_warp[warp - 1] : 0u) + incl - flag;
+    const unsigned tileTotal = s_warp[7];
+    {
+        unsigned r = excl & 0xffffu, rp = excl >> 16;
+        uint2* acc = g.accepted + (size_t)tile * TILE;
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            if ((accMask >> j) & 1u) {
+                const unsigned sp = (splitMask >> j) & 1u;
+                acc[r] = make_uint2(acc_pack((unsigned)(threadIdx.x * K + j), rp, sp, (unsigned)cnt[j]), seedAcc[j]);
+                r++;
+                rp += sp;
+            }
+        }
+    }
+    if (threadIdx.x == 0) g.tileCounts[tile] = make_uint2(tileTotal & 0xffffu, tileTotal >> 16);
+    __syncthreads();  // s_warp is reused by the next tile
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) k_adaptive_decide(MdasDeviceGrid g, unsigned jumpA, unsigned jumpC) {
+    __shared__ unsigned s_warp[8];
+    const int L = g.counts->L;
+    const float gError = __uint_as_float(g.counts->gerr);
+    const int ntiles = (L + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
     float keptMax = 0.0f;   // max error of the leaves this CTA does not split
     unsigned gathered = 0;  // sample coordinates read
-
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int i0 = tile * TILE + threadIdx.x * K;
-        const bool full = i0 + K <= L;
-        float err[K];
-        unsigned sd[K];
-        if (full) {
-#pragma unroll
-            for (int q = 0; q < K; q += 4) {
-                const float4 e4 = *reinterpret_cast<const float4*>(g.errors + i0 + q);
-                const uint4 s4 = *reinterpret_cast<const uint4*>(g.seeds + i0 + q);
-                err[q] = e4.x; err[q + 1] = e4.y; err[q + 2] = e4.z; err[q + 3] = e4.w;
-                sd[q] = s4.x; sd[q + 1] = s4.y; sd[q + 2] = s4.z; sd[q + 3] = s4.w;
-            }
-        } else {
-#pragma unroll
-            for (int j = 0; j < K; ++j) {
-                const bool v = i0 + j < L;
-                err[j] = v ? g.errors[i0 + j] : 0.0f;
-                sd[j] = v ? g.seeds[i0 + j] : 0u;
-            }
-        }
-        unsigned accMask = 0;
-        unsigned seedAcc[K];
-#pragma unroll
-        for (int j = 0; j < K; ++j) {
-            const int leaf = i0 + j;
-            unsigned seed = sd[j];
-            if (seed == 0) seed = tea4((unsigned)leaf, 0);
-            bool a = false;
-            if (leaf < L) a = mdas_pow(err[j] / gError, g.alpha) >= rnd(seed);
-            seedAcc[j] = seed;
-            sd[j] = a ? jumpA * seed + jumpC : seed;  // the seed after the candidate draws
-            if (a) accMask |= 1u << j;
-        }
-        int cnt[K];
-#pragma unroll
-        for (int j = 0; j < K; ++j) cnt[j] = ((accMask >> j) & 1u) ? node_count(nb_node(g.nb + (size_t)(i0 + j) * NB)) : 0;
-        unsigned splitMask = 0;
-#pragma unroll
-        for (int j = 0; j < K; ++j) {
-            gathered += (unsigned)cnt[j];
-            if (cnt[j] >= kMaxNodeSize) splitMask |= 1u << j;
-            if (i0 + j < L && !((splitMask >> j) & 1u)) keptMax = fmaxf(keptMax, err[j]);
-        }
-        if (full) {
-#pragma unroll
-            for (int q = 0; q < K; q += 4)
-                *reinterpret_cast<uint4*>(g.seeds + i0 + q) = make_uint4(sd[q], sd[q + 1], sd[q + 2], sd[q + 3]);
-        } else {
-#pragma unroll
-            for (int j = 0; j < K; ++j)
-                if (i0 + j < L) g.seeds[i0 + j] = sd[j];
-        }
-
-        // block scan of (accepted, split) counts, packed lo16 | hi16
-        const unsigned flag = (unsigned)__popc(accMask) | ((unsigned)__popc(splitMask) << 16);
-        unsigned incl = flag;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        if (lane == 31) s_warp[warp] = incl;
-        __syncthreads();
-        if (warp == 0) {
-            unsigned w = lane < 8 ? s_warp[lane] : 0u;
-#pragma unroll
-            for (int o = 1; o < 8; o <<= 1) {
-                const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
-                if (lane >= o) w += y;
-            }
-            if (lane < 8) s_warp[lane] = w;
-        }
-        __syncthreads();
-        const unsigned excl = (warp ? s_warp[warp - 1] : 0u) + incl - flag;
-        const unsigned tileTotal = s_warp[7];
-        {
-            unsigned r = excl & 0xffffu, rp = excl >> 16;
-            uint2* acc = g.accepted + (size_t)tile * TILE;
-#pragma unroll
-            for (int j = 0; j < K; ++j) {
-                if ((accMask >> j) & 1u) {
-                    const unsigned sp = (splitMask >> j) & 1u;
-                    acc[r] = make_uint2(acc_pack((unsigned)(threadIdx.x * K + j), rp, sp, (unsigned)cnt[j]), seedAcc[j]);
-                    r++;
-                    rp += sp;
-                }
-            }
-        }
-        if (threadIdx.x == 0) g.tileCounts[tile] = make_uint2(tileTotal & 0xffffu, tileTotal >> 16);
-        __syncthreads();  // s_warp is reused by the next tile
-    }
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+        decide_tile<D>(g, tile, L, gError, jumpA, jumpC, s_warp, keptMax, gathered);
     unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(keptMax));
     unsigned c = __reduce_add_sync(0xffffffffu, gathered);
-    if (lane == 0) {
+    if ((threadIdx.x & 31) == 0) {
         if (m) atomicMax(&g.counts->gerrNext, m);
         if (c) atomicAdd(&g.counts->gathered, c);
     }
@@ -518,8 +528,7 @@ __global__ void __launch_bounds__(256) k_adaptive_decide(MdasDeviceGrid g, unsig
 
 // One CTA of 1024 threads: exclusive prefix over the tile counts, then the
 // counters (N, L as the place kernel must see them go to ctl).
-__global__ void __launch_bounds__(1024) k_adaptive_scan(MdasDeviceGrid g) {
-    __shared__ unsigned s_sel[32], s_split[32];
+__device__ __forceinline__ void scan_image(const MdasDeviceGrid& g, unsigned* s_sel, unsigned* s_split) {
     const int N = g.counts->N;
     const int L = g.counts->L;
     const int ntiles = (L + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
@@ -584,155 +593,165 @@ __global__ void __launch_bounds__(1024) k_adaptive_scan(MdasDeviceGrid g) {
     }
 }
 
+__global__ void __launch_bounds__(1024) k_adaptive_scan(MdasDeviceGrid g) {
+    __shared__ unsigned s_sel[32], s_split[32];
+    scan_image(g, s_sel, s_split);
+}
+
+// place, one accepted leaf (entry r of `tile`): best candidate, append or split.
 template <int D>
-__global__ void __launch_bounds__(256, 4) k_adaptive_place(MdasDeviceGrid g) {
+__device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, int r, uint2 pre, int N, int L) {
     constexpr int kMaxNodeSize = 4;
     constexpr int TILE = MDAS_TILE_LEAVES;
     constexpr int NB = NbLayout<D>::FLOATS;
+    (void)kMaxNodeSize;
+    const uint2 e = g.accepted[(size_t)tile * TILE + r];
+    const int nodeIndex = tile * TILE + (int)(e.x & 0x7ffu);
+    const int splitRankInTile = (int)((e.x >> 11) & 0x7ffu);
+    const bool split = (e.x >> 22) & 1u;
+    const int sampleCount = (int)((e.x >> 23) & 7u);
+    unsigned seed = e.y;
+    float* nb = g.nb + (size_t)nodeIndex * NB;
+    float* sc = g.lsc + (size_t)nodeIndex * 4 * D;
+    float mn[D], mx[D];
+    int4 node = nb_load<D>(nb, mn, mx);
+    float scv[4 * D];
+    ld_floats<4 * D>(sc, scv);
+    float samples[4][D];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int i = 0; i < D; ++i) samples[k][i] = scv[k * D + i];
+
+    // best candidate (kdgrid.cu:332-361)
+    float best[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) best[i] = 0.0f;
+    float maxDistance = -1.0f;
+    float diag[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) diag[i] = mx[i] - mn[i];
+    for (int j = 0; j < g.candidatesNum; ++j) {
+        float rr[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) rr[i] = rnd(seed);
+        float candidate[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) candidate[i] = mn[i] + rr[i] * diag[i];
+        float minDistance = FLT_MAX;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (k < sampleCount) {
+                const float distance_k = distance<D>(candidate, samples[k]);
+                if (minDistance > distance_k) minDistance = distance_k;
+            }
+        }
+        if (maxDistance < minDistance) {
+            maxDistance = minDistance;
+#pragma unroll
+            for (int i = 0; i < D; ++i) best[i] = candidate[i];
+        }
+    }
+
+    const int sampleIndex = N + (int)pre.x + r;
+    store_point<D>(g.coords + (size_t)sampleIndex * D, best);
+    if (!split) {
+        // room left: append the index (and its coordinates), the error stays as it was
+        if (sampleCount == 0) node.x = sampleIndex;
+        else if (sampleCount == 1) node.y = sampleIndex;
+        else if (sampleCount == 2) node.z = sampleIndex;
+        else node.w = sampleIndex;
+        nb_set_node(nb, node);
+        store_point<D>(sc + sampleCount * D, best);
+    } else {
+        // split dimension: AABB::LargestAxis, ties to the highest index (aabb.h:34-45)
+        int axis = -1;
+        float maxExtent = -FLT_MAX;
+#pragma unroll
+        for (int i = D - 1; i >= 0; --i) {
+            const float ext = mx[i] - mn[i];
+            if (maxExtent < ext) {
+                maxExtent = ext;
+                axis = i;
+            }
+        }
+        // The reference bubble-sorts the 5 samples (4 old in slot order, then the
+        // new one) by the split coordinate (kdgrid.cu:408-417); the sort is stable,
+        // so sample k lands at rank[k] = #{m : key[m] < key[k], or key[m] == key[k]
+        // and m < k}.  Each sample is written straight to its ranked slot.
+        float key[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            float v = 0.0f;
+#pragma unroll
+            for (int i = 0; i < D; ++i) {
+                const float c = k < 4 ? samples[k < 4 ? k : 0][i] : best[i];
+                if (i == axis) v = c;
+            }
+            key[k] = v;
+        }
+        int rank[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            int rk = 0;
+#pragma unroll
+            for (int m = 0; m < 5; ++m)
+                if (m != k) rk += (key[m] < key[k] || (key[m] == key[k] && m < k)) ? 1 : 0;
+            rank[k] = rk;
+        }
+        const int idx5[5] = {node.x, node.y, node.z, node.w, sampleIndex};
+        float k1 = 0.0f, k2 = 0.0f;
+        int l0 = 0, l1 = 0, r0 = 0, r1 = 0, r2 = 0;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const int rk = rank[k];
+            if (rk == 1) k1 = key[k];
+            if (rk == 2) k2 = key[k];
+            if (rk == 0) l0 = idx5[k];
+            if (rk == 1) l1 = idx5[k];
+            if (rk == 2) r0 = idx5[k];
+            if (rk == 3) r1 = idx5[k];
+            if (rk == 4) r2 = idx5[k];
+        }
+        const float splitPosition = 0.5f * (k1 + k2);  // md = 5 >> 1 = 2
+        const int rank_ = (int)pre.y + splitRankInTile;
+        const int nodeOffset = L + rank_;
+        float* rnb = g.nb + (size_t)nodeOffset * NB;
+        float* rsc = g.lsc + (size_t)nodeOffset * 4 * D;
+        // left child keeps the slot: node, mx[axis], its 2 sample coordinates;
+        // right child: node, box, its 3 sample coordinates
+        nb_set_node(nb, make_int4(l0, l1, ~D, ~D));
+        nb[NbLayout<D>::BOX + D + axis] = splitPosition;
+        float rmn[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) rmn[i] = (i == axis) ? splitPosition : mn[i];
+        nb_store<D>(rnb, make_int4(r0, r1, r2, ~D), rmn, mx);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            float* dst = rank[k] < 2 ? sc + rank[k] * D : rsc + (rank[k] - 2) * D;
+            if (k < 4) store_point<D>(dst, samples[k < 4 ? k : 0]);
+            else store_point<D>(dst, best);
+        }
+        g.errors[nodeIndex] = -1.0f;
+        g.errors[nodeOffset] = -1.0f;
+        // a new slot starts without a seed: the reference's seed buffer is zeroed
+        // once at InitialSampling (kdgrid.cu:637) and right-child slots are never
+        // written before; writing the 0 here makes that memset unnecessary
+        g.seeds[nodeOffset] = 0u;
+        g.dirty[rank_] = nodeIndex;  // for the next errors pass
+    }
+}
+
+template <int D>
+__global__ void __launch_bounds__(256, 4) k_adaptive_place(MdasDeviceGrid g) {
     const int N = g.ctl->N0;
     const int L = g.ctl->L0;
-    const int ntiles = (L + TILE - 1) / TILE;
+    const int ntiles = (L + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int tileSel = (int)g.tileCounts[tile].x;
         if ((int)threadIdx.x >= tileSel) continue;
         const uint2 pre = g.tilePrefix[tile];
-        for (int r = threadIdx.x; r < tileSel; r += 256) {
-            const uint2 e = g.accepted[(size_t)tile * TILE + r];
-            const int nodeIndex = tile * TILE + (int)(e.x & 0x7ffu);
-            const int splitRankInTile = (int)((e.x >> 11) & 0x7ffu);
-            const bool split = (e.x >> 22) & 1u;
-            const int sampleCount = (int)((e.x >> 23) & 7u);
-            unsigned seed = e.y;
-            float* nb = g.nb + (size_t)nodeIndex * NB;
-            float* sc = g.lsc + (size_t)nodeIndex * 4 * D;
-            float mn[D], mx[D];
-            int4 node = nb_load<D>(nb, mn, mx);
-            float scv[4 * D];
-            ld_floats<4 * D>(sc, scv);
-            float samples[4][D];
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-#pragma unroll
-                for (int i = 0; i < D; ++i) samples[k][i] = scv[k * D + i];
-
-            // best candidate (kdgrid.cu:332-361)
-            float best[D];
-#pragma unroll
-            for (int i = 0; i < D; ++i) best[i] = 0.0f;
-            float maxDistance = -1.0f;
-            float diag[D];
-#pragma unroll
-            for (int i = 0; i < D; ++i) diag[i] = mx[i] - mn[i];
-            for (int j = 0; j < g.candidatesNum; ++j) {
-                float rr[D];
-#pragma unroll
-                for (int i = 0; i < D; ++i) rr[i] = rnd(seed);
-                float candidate[D];
-#pragma unroll
-                for (int i = 0; i < D; ++i) candidate[i] = mn[i] + rr[i] * diag[i];
-                float minDistance = FLT_MAX;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    if (k < sampleCount) {
-                        const float distance_k = distance<D>(candidate, samples[k]);
-                        if (minDistance > distance_k) minDistance = distance_k;
-                    }
-                }
-                if (maxDistance < minDistance) {
-                    maxDistance = minDistance;
-#pragma unroll
-                    for (int i = 0; i < D; ++i) best[i] = candidate[i];
-                }
-            }
-
-            const int sampleIndex = N + (int)pre.x + r;
-            store_point<D>(g.coords + (size_t)sampleIndex * D, best);
-            if (!split) {
-                // room left: append the index (and its coordinates), the error stays as it was
-                if (sampleCount == 0) node.x = sampleIndex;
-                else if (sampleCount == 1) node.y = sampleIndex;
-                else if (sampleCount == 2) node.z = sampleIndex;
-                else node.w = sampleIndex;
-                nb_set_node(nb, node);
-                store_point<D>(sc + sampleCount * D, best);
-            } else {
-                // split dimension: AABB::LargestAxis, ties to the highest index (aabb.h:34-45)
-                int axis = -1;
-                float maxExtent = -FLT_MAX;
-#pragma unroll
-                for (int i = D - 1; i >= 0; --i) {
-                    const float ext = mx[i] - mn[i];
-                    if (maxExtent < ext) {
-                        maxExtent = ext;
-                        axis = i;
-                    }
-                }
-                // The reference bubble-sorts the 5 samples (4 old in slot order, then the
-                // new one) by the split coordinate (kdgrid.cu:408-417); the sort is stable,
-                // so sample k lands at rank[k] = #{m : key[m] < key[k], or key[m] == key[k]
-                // and m < k}.  Each sample is written straight to its ranked slot.
-                float key[5];
-#pragma unroll
-                for (int k = 0; k < 5; ++k) {
-                    float v = 0.0f;
-#pragma unroll
-                    for (int i = 0; i < D; ++i) {
-                        const float c = k < 4 ? samples[k < 4 ? k : 0][i] : best[i];
-                        if (i == axis) v = c;
-                    }
-                    key[k] = v;
-                }
-                int rank[5];
-#pragma unroll
-                for (int k = 0; k < 5; ++k) {
-                    int rk = 0;
-#pragma unroll
-                    for (int m = 0; m < 5; ++m)
-                        if (m != k) rk += (key[m] < key[k] || (key[m] == key[k] && m < k)) ? 1 : 0;
-                    rank[k] = rk;
-                }
-                const int idx5[5] = {node.x, node.y, node.z, node.w, sampleIndex};
-                float k1 = 0.0f, k2 = 0.0f;
-                int l0 = 0, l1 = 0, r0 = 0, r1 = 0, r2 = 0;
-#pragma unroll
-                for (int k = 0; k < 5; ++k) {
-                    const int rk = rank[k];
-                    if (rk == 1) k1 = key[k];
-                    if (rk == 2) k2 = key[k];
-                    if (rk == 0) l0 = idx5[k];
-                    if (rk == 1) l1 = idx5[k];
-                    if (rk == 2) r0 = idx5[k];
-                    if (rk == 3) r1 = idx5[k];
-                    if (rk == 4) r2 = idx5[k];
-                }
-                const float splitPosition = 0.5f * (k1 + k2);  // md = 5 >> 1 = 2
-                const int rank_ = (int)pre.y + splitRankInTile;
-                const int nodeOffset = L + rank_;
-                float* rnb = g.nb + (size_t)nodeOffset * NB;
-                float* rsc = g.lsc + (size_t)nodeOffset * 4 * D;
-                // left child keeps the slot: node, mx[axis], its 2 sample coordinates;
-                // right child: node, box, its 3 sample coordinates
-                nb_set_node(nb, make_int4(l0, l1, ~D, ~D));
-                nb[NbLayout<D>::BOX + D + axis] = splitPosition;
-                float rmn[D];
-#pragma unroll
-                for (int i = 0; i < D; ++i) rmn[i] = (i == axis) ? splitPosition : mn[i];
-                nb_store<D>(rnb, make_int4(r0, r1, r2, ~D), rmn, mx);
-#pragma unroll
-                for (int k = 0; k < 5; ++k) {
-                    float* dst = rank[k] < 2 ? sc + rank[k] * D : rsc + (rank[k] - 2) * D;
-                    if (k < 4) store_point<D>(dst, samples[k < 4 ? k : 0]);
-                    else store_point<D>(dst, best);
-                }
-                g.errors[nodeIndex] = -1.0f;
-                g.errors[nodeOffset] = -1.0f;
-                // a new slot starts without a seed: the reference's seed buffer is zeroed
-                // once at InitialSampling (kdgrid.cu:637) and right-child slots are never
-                // written before; writing the 0 here makes that memset unnecessary
-                g.seeds[nodeOffset] = 0u;
-                g.dirty[rank_] = nodeIndex;  // for the next errors pass
-            }
-        }
+        for (int r = threadIdx.x; r < tileSel; r += 256) place_entry<D>(g, tile, r, pre, N, L);
     }
 }
 
@@ -742,74 +761,80 @@ __global__ void __launch_bounds__(256, 4) k_adaptive_place(MdasDeviceGrid g) {
 // the pixels its box covers; pixel edges advance incrementally as in the
 // reference so that the footprint is the same to the bit.
 // =====================================================================================
+// reconstruction splat of one leaf
+template <int D>
+__device__ __forceinline__ void integrate_leaf(const MdasDeviceGrid& g, int nodeIndex, float4* __restrict__ pixels,
+                                               int width, int height) {
+    constexpr int NB = NbLayout<D>::FLOATS;
+    const float scaleX = g.scaleX, scaleY = g.scaleY;
+    float2 pixelStep;
+    pixelStep.x = scaleX / width;
+    pixelStep.y = scaleY / height;
+    float mn[D], mx[D];
+    const int4 node = nb_load<D>(g.nb + (size_t)nodeIndex * NB, mn, mx);
+    float3 sampleValue = make_float3(0.0f, 0.0f, 0.0f);
+    int sampleCount = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int idx = node_get(node, i);
+        if (idx >= 0) {
+            const float* v = g.values + 3 * (size_t)idx;
+            sampleValue.x += __ldg(v);
+            sampleValue.y += __ldg(v + 1);
+            sampleValue.z += __ldg(v + 2);
+            sampleCount++;
+        }
+    }
+    {
+        const float inv = 1.0f / float(sampleCount);
+        sampleValue.x *= inv;
+        sampleValue.y *= inv;
+        sampleValue.z *= inv;
+    }
+    const float boxVolume = box_volume<D>(mn, mx);
+
+    const int x0 = mn[0] * width / scaleX;
+    int x1 = mx[0] * width / scaleX;
+    const int y0 = mn[1] * height / scaleY;
+    int y1 = mx[1] * height / scaleY;
+    x1 = min(x1 + 1, width);
+    y1 = min(y1 + 1, height);
+    const float pixArea = (scaleX * scaleY) / float(width * height);
+    const float invPixArea = 1.0f / pixArea;  // float3 / float (sutil/vec_math.h:483-487)
+
+    float pMinX, pMaxX, pMinY, pMaxY;
+    pMinY = y0 * scaleY / float(height);
+    pMaxY = pMinY + pixelStep.y;
+    for (int y = y0; y < y1; ++y) {
+        pMinX = x0 * scaleX / float(width);
+        pMaxX = pMinX + pixelStep.x;
+        for (int x = x0; x < x1; ++x) {
+            const float clox = fmaxf(pMinX, mn[0]);
+            const float chix = fminf(pMaxX, mx[0]);
+            const float cloy = fmaxf(pMinY, mn[1]);
+            const float chiy = fminf(pMaxY, mx[1]);
+            if (clox < chix && cloy < chiy) {
+                const float volume = (chix - clox) * (chiy - cloy) * boxVolume / ((mx[0] - mn[0]) * (mx[1] - mn[1]));
+                const float4 value = make_float4((sampleValue.x * volume) * invPixArea,
+                                                 (sampleValue.y * volume) * invPixArea,
+                                                 (sampleValue.z * volume) * invPixArea, 0.0f);
+                atomicAdd(pixels + (size_t)y * width + x, value);
+            }
+            pMinX = pMaxX;
+            pMaxX += pixelStep.x;
+        }
+        pMinY = pMaxY;
+        pMaxY += pixelStep.y;
+    }
+}
+
 template <int D>
 __global__ void __launch_bounds__(256) k_integrate(MdasDeviceGrid g, float4* __restrict__ pixels, int width,
                                                     int height) {
-    constexpr int NB = NbLayout<D>::FLOATS;
     const int L = g.counts->L;
-    const float scaleX = g.scaleX, scaleY = g.scaleY;
     for (int nodeIndex = blockIdx.x * blockDim.x + threadIdx.x; nodeIndex < L;
-         nodeIndex += gridDim.x * blockDim.x) {
-        float2 pixelStep;
-        pixelStep.x = scaleX / width;
-        pixelStep.y = scaleY / height;
-        float mn[D], mx[D];
-        const int4 node = nb_load<D>(g.nb + (size_t)nodeIndex * NB, mn, mx);
-        float3 sampleValue = make_float3(0.0f, 0.0f, 0.0f);
-        int sampleCount = 0;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const int idx = node_get(node, i);
-            if (idx >= 0) {
-                const float* v = g.values + 3 * (size_t)idx;
-                sampleValue.x += __ldg(v);
-                sampleValue.y += __ldg(v + 1);
-                sampleValue.z += __ldg(v + 2);
-                sampleCount++;
-            }
-        }
-        {
-            const float inv = 1.0f / float(sampleCount);
-            sampleValue.x *= inv;
-            sampleValue.y *= inv;
-            sampleValue.z *= inv;
-        }
-        const float boxVolume = box_volume<D>(mn, mx);
-
-        const int x0 = mn[0] * width / scaleX;
-        int x1 = mx[0] * width / scaleX;
-        const int y0 = mn[1] * height / scaleY;
-        int y1 = mx[1] * height / scaleY;
-        x1 = min(x1 + 1, width);
-        y1 = min(y1 + 1, height);
-        const float pixArea = (scaleX * scaleY) / float(width * height);
-        const float invPixArea = 1.0f / pixArea;  // float3 / float (sutil/vec_math.h:483-487)
-
-        float pMinX, pMaxX, pMinY, pMaxY;
-        pMinY = y0 * scaleY / float(height);
-        pMaxY = pMinY + pixelStep.y;
-        for (int y = y0; y < y1; ++y) {
-            pMinX = x0 * scaleX / float(width);
-            pMaxX = pMinX + pixelStep.x;
-            for (int x = x0; x < x1; ++x) {
-                const float clox = fmaxf(pMinX, mn[0]);
-                const float chix = fminf(pMaxX, mx[0]);
-                const float cloy = fmaxf(pMinY, mn[1]);
-                const float chiy = fminf(pMaxY, mx[1]);
-                if (clox < chix && cloy < chiy) {
-                    const float volume = (chix - clox) * (chiy - cloy) * boxVolume / ((mx[0] - mn[0]) * (mx[1] - mn[1]));
-                    const float4 value = make_float4((sampleValue.x * volume) * invPixArea,
-                                                     (sampleValue.y * volume) * invPixArea,
-                                                     (sampleValue.z * volume) * invPixArea, 0.0f);
-                    atomicAdd(pixels + (size_t)y * width + x, value);
-                }
-                pMinX = pMaxX;
-                pMaxX += pixelStep.x;
-            }
-            pMinY = pMaxY;
-            pMaxY += pixelStep.y;
-        }
-    }
+         nodeIndex += gridDim.x * blockDim.x)
+        integrate_leaf<D>(g, nodeIndex, pixels, width, height);
 }
 
 // =====================================================================================

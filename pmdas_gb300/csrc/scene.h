@@ -21,6 +21,22 @@ cudaError_t mdas_launch_reference_image(const MdasScene& sc, const float* d_prim
 int mdas_generate_scene(int kind, uint64_t seed, int count, float scaleX, float scaleY, int width, int height,
                         MdasScene* sc, std::vector<float>* prims);
 
+// The integrand side of one image of a batched render (device-side descriptor).
+struct MdasBatchScene {
+    MdasScene sc;
+    const float* prims;
+    const MdasCounts* counts;
+    const float* coords;
+    float* values;
+    int dim;
+    int initialSamples;
+};
+
+// Batched integrand: every image's initial samples (all = 1) or the samples the
+// last pass added to each still-active image (all = 0).  Images of one launch
+// share the coordinate stride D.
+cudaError_t mdas_launch_evaluate_batch(const MdasBatchScene* scenes, int n, int D, int all, int grid, cudaStream_t s);
+
 struct mdas_scene {
     MdasScene desc;
     std::vector<float> prims;  // host copy

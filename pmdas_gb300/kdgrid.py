@@ -305,3 +305,50 @@ def render_host(grid: KDGrid, scene: Scene, budget: int, host_pixels: np.ndarray
     N.check(grid._lib.mdas_render_host(grid.handle, scene.handle, _ptr(host_prims), int(budget), _ptr(host_pixels),
                                        width, height, C.byref(st)), "mdas_render_host")
     return st
+
+
+class Batch:
+    """Many images rendered together: one CUDA graph, one launch per stage and
+    point dimension, a device-side loop until every image reached its budget."""
+
+    def __init__(self, grids, scenes, budgets, pixels, widths, heights):
+        lib = N.load()
+        n = len(grids)
+        self._keep = (list(grids), list(scenes), list(pixels))
+        G = (C.c_void_p * n)(*[g.handle.value for g in grids])
+        S = (C.c_void_p * n)(*[sc.handle.value for sc in scenes])
+        B = (C.c_int * n)(*[int(b) for b in budgets])
+        Pp = (C.c_void_p * n)(*[_ptr(p) for p in pixels])
+        W = (C.c_int * n)(*[int(w) for w in widths])
+        H = (C.c_int * n)(*[int(h) for h in heights])
+        h = C.c_void_p()
+        N.check(lib.mdas_batch_create(C.byref(h), n, G, S, B, Pp, W, H), "mdas_batch_create")
+        self._lib = lib
+        self._h = h
+        self.n = n
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mdas_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render(self):
+        st = (N.RenderStats * self.n)()
+        N.check(self._lib.mdas_batch_render(self._h, st), "mdas_batch_render")
+        return list(st)
+
+    def set_tuning(self, ctas_per_sm):
+        a = (C.c_int * 4)(*ctas_per_sm)
+        N.check(self._lib.mdas_batch_set_tuning(self._h, a), "mdas_batch_set_tuning")
+
+    def autotune(self, repeats: int = 2):
+        a = (C.c_int * 4)()
+        ms = C.c_double()
+        N.check(self._lib.mdas_batch_autotune(self._h, repeats, a, C.byref(ms)), "mdas_batch_autotune")
+        return list(a), ms.value

@@ -6,9 +6,8 @@ Every workload runs the reference's budget loop
 sampling passes while ``N < spp * width * height``, then integrate.
 
 ``maxSamples`` is the apps' hard-coded cap of 30,000,000 samples
-(optixMotionBlur.cpp:81) where the budget fits under it; above it, the cap is
-raised to 1.5x the budget so that the last pass (which can add up to one
-sample per leaf) still fits.
+(optixMotionBlur.cpp:81), raised to 1.5x the budget where that is larger, so
+that the last pass (which can add up to one sample per leaf) still fits.
 """
 from __future__ import annotations
 
@@ -53,10 +52,9 @@ class Workload:
 
     @property
     def maxSamples(self) -> int:
+        # the last pass can add one sample per leaf (<= N/2), so 1.5x the budget always fits
         need = max(self.budget, 4 * self.initial_leaves)
-        if need <= APP_MAX_SAMPLES:
-            return APP_MAX_SAMPLES
-        return min((need * 3 + 1) // 2, (1 << 30) - 1)
+        return min(max(APP_MAX_SAMPLES, (need * 3 + 1) // 2), (1 << 30) - 1)
 
     def scaled(self, width: int, height: int, **kw) -> "Workload":
         return replace(self, width=width, height=height, **kw)
@@ -74,3 +72,27 @@ WORKLOADS = {
     # 4-D direct lighting (x, y, light u, v), 3840x2160 at 64 spp
     "dl4k": Workload("dl4k", 4, 3840, 2160, 64, N.SCENE_DIRECT_LIGHT, 7, 4),
 }
+
+
+# ---- the batched workload: 64 images of uneven resolution, budget and dimension
+BATCH_RESOLUTIONS = ((256, 256), (512, 512), (1280, 720), (1920, 1080))
+BATCH_SPP = (4, 8, 16, 32)
+BATCH_KINDS = ((3, N.SCENE_DISCS_MB, 64), (4, N.SCENE_DISCS_DOF, 256))  # (dim, scene, primitives)
+
+
+def batch_image(seed: int) -> Workload:
+    """Image `seed` of the batch: resolution, spp and dimension drawn from the
+    seed (numpy PCG64 stream, in that order); extraImgBits chosen so that the
+    initial grid holds at most 1 sample per pixel, so every image takes passes."""
+    import math
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    W, H = BATCH_RESOLUTIONS[int(rng.integers(4))]
+    spp = BATCH_SPP[int(rng.integers(4))]
+    dim, kind, count = BATCH_KINDS[int(rng.integers(2))]
+    eib = max(0, int(math.floor(math.log(W * H / (4 * 2 ** dim), 4))))
+    return Workload(f"batch-{seed}", dim, W, H, spp, kind, seed, count, extraImgBits=eib)
+
+
+def batch_workloads(first_seed: int = 200, n: int = 64) -> list:
+    return [batch_image(first_seed + k) for k in range(n)]

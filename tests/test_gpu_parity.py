@@ -121,6 +121,48 @@ def test_render_graph_equals_host_loop(cuda, arith, case):
     assert g2.Validate()
 
 
+@pytest.mark.parametrize("arith", [P.ARITH_REFERENCE, P.ARITH_IEEE])
+def test_batch_equals_single_renders(cuda, arith):
+    """A batch of images of different dimension, size and budget (one launch per
+    stage and dimension, device-side loop) leaves every image exactly as its
+    own render would; a second render and a retuned graph do too."""
+    import torch
+    specs = [  # (kind, D, W, H, spp, bpd, eib, alpha, cand, seed, prims)
+        (P.SCENE_DISCS_MB, 3, 64, 48, 8, 1, 3, 0.25, 4, 11, 32),
+        (P.SCENE_DISCS_DOF, 4, 96, 64, 16, 1, 3, 0.25, 4, 12, 64),
+        (P.SCENE_DISCS_MBDOF, 5, 40, 40, 12, 1, 2, 0.0625, 3, 13, 32),
+        (P.SCENE_DISCS_MB, 3, 128, 128, 4, 1, 4, 0.5, 2, 14, 64),
+        (P.SCENE_DIRECT_LIGHT, 4, 80, 60, 32, 0, 5, 0.015625, 4, 15, 4),
+        (P.SCENE_DISCS_DOF, 4, 32, 32, 2, 1, 3, 0.25, 4, 16, 16),  # budget below the initial grid: no pass
+    ]
+    grids, scenes, pix, budgets, singles = [], [], [], [], []
+    for kind, D, W, H, spp, bpd, eib, alpha, cand, seed, prims in specs:
+        budget = spp * W * H
+        ms = 2 * budget + 8 * ((1 << (bpd * D)) << (2 * eib))
+        sc = P.Scene(kind, seed, prims, W, H, W, H)
+        ref = P.KDGrid(D, ms, cand, bpd, eib, alpha, W, H, arith=arith)
+        rpx = torch.zeros(H, W, 4, device="cuda")
+        st = P.render(ref, sc, budget, rpx, W, H)
+        singles.append((ref.dump_state(), rpx.cpu().numpy(), st.passes))
+        grids.append(P.KDGrid(D, ms, cand, bpd, eib, alpha, W, H, arith=arith))
+        scenes.append(sc)
+        pix.append(torch.zeros(H, W, 4, device="cuda"))
+        budgets.append(budget)
+    batch = P.Batch(grids, scenes, budgets, pix, [sp[2] for sp in specs], [sp[3] for sp in specs])
+    for rnd in range(3):
+        if rnd == 2:
+            batch.set_tuning([2, 3, 1, 5])
+        stats = batch.render()
+        for i, (want, img, passes) in enumerate(singles):
+            assert stats[i].passes == passes, (rnd, i)
+            assert_states_equal(grids[i].dump_state(), want,
+                                keys=("coords", "values", "nodes", "boxes", "errors", "seeds"), what=f"image {i}")
+            ok, worst = rel_close(pix[i].cpu().numpy(), img)
+            assert ok, (i, worst)
+    assert singles[-1][2] == 0 and singles[0][2] > 0
+    batch.close()
+
+
 def test_reference_build_close_to_oracle(cuda):
     """The fast-math build differs from IEEE only in the last bits of divisions,
     square roots and powf: same initial grid (power-of-two extents), errors within
