@@ -33,6 +33,7 @@ class Workload:
     bitsPerDim: int = 1
     extraImgBits: int = 8
     candidatesNum: int = 4
+    capacity: int = 0  # sample capacity; 0 = the apps' cap, raised to 1.5x the budget where larger
 
     @property
     def scaleX(self) -> float:
@@ -53,6 +54,8 @@ class Workload:
     @property
     def maxSamples(self) -> int:
         # the last pass can add one sample per leaf (<= N/2), so 1.5x the budget always fits
+        if self.capacity:
+            return self.capacity
         need = max(self.budget, 4 * self.initial_leaves)
         return min(max(APP_MAX_SAMPLES, (need * 3 + 1) // 2), (1 << 30) - 1)
 
@@ -91,7 +94,10 @@ def batch_image(seed: int) -> Workload:
     spp = BATCH_SPP[int(rng.integers(4))]
     dim, kind, count = BATCH_KINDS[int(rng.integers(2))]
     eib = max(0, int(math.floor(math.log(W * H / (4 * 2 ** dim), 4))))
-    return Workload(f"batch-{seed}", dim, W, H, spp, kind, seed, count, extraImgBits=eib)
+    budget = spp * W * H
+    # every image of the batch holds its own state: size it to its budget (1.5x, see maxSamples)
+    return Workload(f"batch-{seed}", dim, W, H, spp, kind, seed, count, extraImgBits=eib,
+                    capacity=(max(budget, 4 * ((1 << dim) << (2 * eib))) * 3 + 1) // 2)
 
 
 def batch_workloads(first_seed: int = 200, n: int = 64) -> list:
