@@ -202,24 +202,20 @@ __global__ void __launch_bounds__(1024) k_batch_scan(const MdasBatchImage* __res
     scan_image(g, s_sel, s_split);
 }
 
-// ---- adaptive pass: place
+// ---- adaptive pass: place (one thread per accepted leaf)
 template <int D>
 __global__ void __launch_bounds__(256, 4) k_batch_place(const MdasBatchImage* __restrict__ imgs, int n) {
     __shared__ int s_pre[MDAS_MAX_BATCH + 1];
     __shared__ unsigned s_warp[8];
     const int total = batch_prefix(n, s_pre, s_warp, [&](int i) {
         const MdasDeviceGrid& g = imgs[i].g;
-        return g.counts->active ? ceil_div(g.ctl->L0, MDAS_TILE_LEAVES) : 0;
+        return g.counts->active ? ceil_div(g.counts->newN, 256) : 0;
     });
-    for (int t = blockIdx.x; t < total; t += gridDim.x) {
-        const int i = batch_image_of(s_pre, n, t);
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const int i = batch_image_of(s_pre, n, c);
         const MdasDeviceGrid& g = imgs[i].g;
-        const int tile = t - s_pre[i];
-        const int tileSel = (int)g.tileCounts[tile].x;
-        if ((int)threadIdx.x >= tileSel) continue;
-        const uint2 pre = g.tilePrefix[tile];
-        const int N = g.ctl->N0, L = g.ctl->L0;
-        for (int r = threadIdx.x; r < tileSel; r += 256) place_entry<D>(g, tile, r, pre, N, L);
+        const int k = (c - s_pre[i]) * 256 + threadIdx.x;
+        if (k < g.counts->newN) place_rank<D>(g, k, g.ctl->N0, g.ctl->L0);
     }
 }
 

@@ -192,6 +192,7 @@ void free_grid(mdas_grid* g) {
     cudaFree(g->dg.tileCounts);
     cudaFree(g->dg.tilePrefix);
     cudaFree(g->dg.accepted);
+    cudaFree(g->dg.chunkTile);
     cudaFree(g->dg.dirty);
     if (g->scratch) cudaFree(g->scratch);
     if (g->hcounts) cudaFreeHost(g->hcounts);
@@ -278,6 +279,7 @@ int mdas_create_ex(mdas_grid** out, int dim, int maxSamples, int candidatesNum, 
               cudaMalloc(&d.tileCounts, sizeof(uint2) * (size_t)d.maxTiles) == cudaSuccess &&
               cudaMalloc(&d.tilePrefix, sizeof(uint2) * (size_t)d.maxTiles) == cudaSuccess &&
               cudaMalloc(&d.accepted, sizeof(uint2) * (size_t)d.maxTiles * MDAS_TILE_LEAVES) == cudaSuccess &&
+              cudaMalloc(&d.chunkTile, sizeof(int) * ((size_t)d.maxNodes / 256 + 2)) == cudaSuccess &&
               cudaMalloc(&d.dirty, sizeof(int) * ((size_t)d.maxNodes / 2 + 1)) == cudaSuccess &&
               cudaMallocHost(&g->hcounts, sizeof(MdasCounts)) == cudaSuccess;
     if (ok) {
@@ -375,7 +377,7 @@ int mdas_adaptive_sampling(mdas_grid* g) {
     // one CTA iteration per tile of MDAS_TILE_LEAVES leaves
     const int64_t tiles = ((int64_t)g->L + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
     const int gridDecide = grid_for(g, MDAS_K_DECIDE, tiles * 256);
-    const int gridPlace = grid_for(g, MDAS_K_ADAPTIVE, tiles * 256);
+    const int gridPlace = grid_for(g, MDAS_K_ADAPTIVE, g->L);  // one thread per accepted leaf (<= L)
     int rc = timed(g, 2, [&]() { return launch_adaptive(g, gridDecide, gridPlace); });
     g->dirtyValid = g->errorsClean;
     g->errorsClean = false;

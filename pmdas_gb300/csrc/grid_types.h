@@ -52,6 +52,7 @@ struct MdasDeviceGrid {
     uint2* tileCounts;    // [maxTiles] (accepted, split) per tile of MDAS_TILE_LEAVES leaves
     uint2* tilePrefix;    // [maxTiles] exclusive prefix of tileCounts
     uint2* accepted;      // [maxTiles * MDAS_TILE_LEAVES] accepted leaves, compacted per tile
+    int* chunkTile;       // [maxNodes/256 + 2] tile of the first entry of each 256-entry chunk of accepted leaves
     int maxTiles;
     int* dirty;           // [maxNodes/2 + 1], slots of the left children of the last pass's splits
 };

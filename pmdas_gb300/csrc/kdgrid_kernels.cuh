@@ -389,9 +389,11 @@ __global__ void __launch_bounds__(256) k_compute_errors(MdasDeviceGrid g) {
 //            number of LCG steps, applied by jump-ahead), and writes the tile's
 //            (accepted, split) counts and its accepted leaves, compacted in leaf
 //            order, to scratch;
-//   scan   — one CTA: exclusive prefix of the tile counts, and the new counts;
-//   place  — one thread per accepted leaf: best candidate from the leaf's box
-//            and private sample copy, append or split, writes.
+//   scan   — one CTA: exclusive prefix of the tile counts, the new counts, and
+//            for every chunk of 256 accepted leaves the tile of its first one;
+//   place  — one thread per accepted leaf, in accepted-rank order (every lane
+//            busy): best candidate from the leaf's box and private sample copy,
+//            append or split, writes.
 // decide also takes the max error of the leaves the pass does not split (their
 // error is final for the next errors pass); place lists the split leaves.
 // =====================================================================================
@@ -577,6 +579,8 @@ __device__ __forceinline__ void scan_image(const MdasDeviceGrid& g, unsigned* s_
     for (int t = t0; t < t1; ++t) {
         const uint2 c = g.tileCounts[t];
         g.tilePrefix[t] = make_uint2(ps, pp);
+        // chunks of 256 accepted entries whose first entry lies in this tile
+        for (unsigned ch = (ps + 255u) >> 8; (ch << 8) < ps + c.x; ++ch) g.chunkTile[ch] = t;
         ps += c.x;
         pp += c.y;
     }
@@ -598,7 +602,8 @@ __global__ void __launch_bounds__(1024) k_adaptive_scan(MdasDeviceGrid g) {
     scan_image(g, s_sel, s_split);
 }
 
-// place, one accepted leaf (entry r of `tile`): best candidate, append or split.
+// place, one accepted leaf (entry r of `tile`, whose prefix is `pre`): best
+// candidate, append or split.
 template <int D>
 __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, int r, uint2 pre, int N, int L) {
     constexpr int kMaxNodeSize = 4;
@@ -742,17 +747,29 @@ __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, i
     }
 }
 
+// Entry k of the pass's accepted list (its new sample is N + k), found from
+// the first tile of its 256-entry chunk.
+template <int D>
+__device__ __forceinline__ void place_rank(const MdasDeviceGrid& g, int k, int N, int L) {
+    const int ntiles = (L + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
+    int tile = g.chunkTile[k >> 8];
+    uint2 pre = g.tilePrefix[tile];
+    while (tile + 1 < ntiles) {
+        const uint2 next = g.tilePrefix[tile + 1];
+        if ((int)next.x > k) break;
+        ++tile;
+        pre = next;
+    }
+    place_entry<D>(g, tile, k - (int)pre.x, pre, N, L);
+}
+
+// One thread per accepted leaf, in accepted-rank order.
 template <int D>
 __global__ void __launch_bounds__(256, 4) k_adaptive_place(MdasDeviceGrid g) {
     const int N = g.ctl->N0;
     const int L = g.ctl->L0;
-    const int ntiles = (L + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int tileSel = (int)g.tileCounts[tile].x;
-        if ((int)threadIdx.x >= tileSel) continue;
-        const uint2 pre = g.tilePrefix[tile];
-        for (int r = threadIdx.x; r < tileSel; r += 256) place_entry<D>(g, tile, r, pre, N, L);
-    }
+    const int accepted = g.counts->newN;
+    for (int k = blockIdx.x * 256 + threadIdx.x; k < accepted; k += gridDim.x * 256) place_rank<D>(g, k, N, L);
 }
 
 // =====================================================================================
