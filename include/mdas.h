@@ -22,6 +22,7 @@
 #ifndef PMDAS_GB300_MDAS_H
 #define PMDAS_GB300_MDAS_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -262,6 +263,68 @@ int mdas_batch_set_tuning(mdas_batch* b, const int* ctasPerSm4);
 /* Times a set of candidate tunings on this batch (`repeats` renders each),
  * keeps the fastest and returns it with its time per render. */
 int mdas_batch_autotune(mdas_batch* b, int repeats, int* best4, double* bestMs);
+
+/* ---- Leaf ordering: Morton keys, radix sort, Karras hierarchy, point location.
+ *
+ * No reference counterpart (the reference keeps its leaves in allocation order
+ * and stores no tree); none of these calls changes the grid.  A key numbers the
+ * cells of a finer grid the way the reference numbers its initial cells
+ * (uniformSamplingKernel, kdgrid.cu:144-160), at bitsPerDim + fineBits bits per
+ * dimension (+ extraImgBits for the two image dimensions):
+ *   bit k < bitsPerDim + fineBits of the cell coordinate of dimension j is key
+ *   bit dim*k + (dim-1-j); image bit k >= bitsPerDim + fineBits is key bit
+ *   dim*(bitsPerDim + fineBits) + 2*(k - bitsPerDim - fineBits) + 1-j.
+ * So key >> (dim * fineBits) is the reference's index of the initial cell
+ * holding the point, and keys sort points along a Z-order curve whose top
+ * levels are the image plane.  The cell coordinate of coordinate x of
+ * dimension j is floor(x / scale_j * 2^bits_j) clamped to the grid (scale =
+ * scaleX, scaleY, then 1). */
+
+/* Bits of a key (<= 64), or -1 if the parameters need more. */
+int mdas_morton_key_bits(int dim, int bitsPerDim, int extraImgBits, int fineBits);
+
+/* Keys of n points (device pointers: points [n * dim] floats, keys [n]). */
+int mdas_morton_encode(int dim, int bitsPerDim, int extraImgBits, int fineBits, float scaleX, float scaleY,
+                       const float* points, int n, uint64_t* keys, void* stream);
+
+/* The boxes (mn[dim], mx[dim]) of n cells at bitsPerDim bits per dimension,
+ * computed as uniformSamplingKernel computes the initial cells' boxes
+ * (kdgrid.cu:142-164, 191-196).  Device pointers. */
+int mdas_morton_decode(int dim, int bitsPerDim, int extraImgBits, float scaleX, float scaleY, const uint64_t* cells,
+                       int n, float* boxes, void* stream);
+
+/* Stable LSD radix sort of (key, value) pairs on key bits [beginBit, endBit),
+ * 8 bits per pass.  Device pointers; valuesIn == NULL sorts the values 0..n-1;
+ * keysIn must not be keysOut.  Call with temp == NULL to get *tempBytes.
+ * Synchronises `stream`; MDAS_ERR_TIMEOUT if a bounded inter-CTA wait gave up
+ * (the output is then incomplete). */
+int mdas_radix_sort_pairs(void* temp, size_t* tempBytes, const uint64_t* keysIn, uint64_t* keysOut,
+                          const uint32_t* valuesIn, uint32_t* valuesOut, int n, int beginBit, int endBit,
+                          void* stream);
+
+/* The grid's leaves in key order: key of each leaf's box centre (fineBits < 0:
+ * the most that fit in 64 bits), sorted; `order` receives the leaf slots, ties
+ * in slot order.  Device pointers of numberOfNodes entries, each optional. */
+int mdas_leaf_order(mdas_grid* g, int fineBits, uint64_t* keys, uint32_t* order);
+
+/* Orders the leaves (as mdas_leaf_order) and builds a Karras radix tree over
+ * them: numberOfNodes - 1 internal nodes, root 0, with boxes that bound their
+ * leaves.  Valid until the grid changes. */
+int mdas_build_hierarchy(mdas_grid* g, int fineBits);
+
+/* Host copies of the hierarchy, each pointer optional: n = numberOfNodes sorted
+ * keys and leaf slots; children [2 (n-1)] (c >= 0: internal node c, c < 0: the
+ * leaf at sorted position ~c); parents [2n - 1] (internal nodes, then leaves by
+ * sorted position; -1 for the root); boxes [(n-1) * 2 dim] of the internal
+ * nodes.  MDAS_ERR_STATE if the grid changed since mdas_build_hierarchy. */
+int mdas_get_hierarchy(mdas_grid* g, int* numLeaves, uint64_t* keys, uint32_t* order, int* children, int* parents,
+                       float* boxes);
+
+/* For each of n points (device [n * dim]) the leaf slot whose box holds it
+ * (mn <= x < mx per dimension, x <= mx on the domain's upper faces), the first
+ * in key order if several do, -1 if none (device [n]).  Needs a current
+ * hierarchy (MDAS_ERR_STATE otherwise).  Synchronises the grid's stream. */
+int mdas_locate(mdas_grid* g, const float* points, int n, int* leaves);
 
 /* ---- env configuration (SDK/sutil/Environment.{h,cpp}; the options the MDAS
  *      apps register, optixMotionBlur.cpp:104-137) ---- */

@@ -582,4 +582,210 @@ int orc_render(int D, int bpd, int eib, int candidatesNum, float alpha, float sx
     return 0;
 }
 
+
+// ---- Leaf ordering (no reference counterpart) ----------------------------------
+// Keys number the cells of a finer grid the way uniformSamplingKernel numbers
+// its initial cells (kdgrid.cu:144-157), with K = bitsPerDim + fineBits bits
+// per dimension: key bit pos < D*K holds bit pos/D of dimension D-1 - pos%D;
+// key bit D*K + r holds bit K + r/2 of image dimension 1 - r%2.  Restated here
+// position by position (the CUDA kernels place coordinate bits instead).
+
+static uint32_t orc_cell_coord(float x, float scale, bool image, int B) {
+    const float u = image ? x / scale : x;
+    const float top = (float)(1u << B);
+    const float s = u * top;
+    if (!(s > 0.0f)) return 0u;
+    if (s >= top) return (1u << B) - 1u;
+    return (uint32_t)s;
+}
+
+static uint64_t orc_key(const float* p, int D, int bpd, int eib, int F, float sx, float sy) {
+    const int K = bpd + F;
+    uint32_t q[8];
+    for (int j = 0; j < D; ++j)
+        q[j] = orc_cell_coord(p[j], j == 0 ? sx : sy, j < 2, K + (j < 2 ? eib : 0));
+    uint64_t key = 0;
+    const int total = D * K + 2 * eib;
+    for (int pos = 0; pos < total; ++pos) {
+        int j, k;
+        if (pos < D * K) {
+            k = pos / D;
+            j = D - 1 - pos % D;
+        } else {
+            const int r = pos - D * K;
+            k = K + r / 2;
+            j = 1 - r % 2;
+        }
+        key |= (uint64_t)((q[j] >> k) & 1u) << pos;
+    }
+    return key;
+}
+
+// Prefix length of sorted keys i and j, positions breaking ties.
+static int orc_prefix(const uint64_t* k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    if (k[i] == k[j]) {
+        const uint32_t x = (uint32_t)(i ^ j);
+        return 64 + (x ? __builtin_clz(x) : 32);
+    }
+    return __builtin_clzll(k[i] ^ k[j]);
+}
+
+int orc_morton_encode(int D, int bpd, int eib, int F, float sx, float sy, const float* points, int n,
+                      uint64_t* keys) {
+    if (D > 8 || D * (bpd + F) + 2 * eib > 64 || bpd + F + eib > 31) return -1;
+    for (int i = 0; i < n; ++i) keys[i] = orc_key(points + (size_t)i * D, D, bpd, eib, F, sx, sy);
+    return 0;
+}
+
+// Cell boxes as uniformSamplingKernel computes them (kdgrid.cu:142-164, 191-196).
+int orc_morton_decode(int D, int bpd, int eib, float sx, float sy, const uint64_t* cells, int n, float* boxes) {
+    if (D > 8 || D * bpd + 2 * eib > 64 || bpd + eib > 31) return -1;
+    for (int i = 0; i < n; ++i) {
+        uint32_t xq[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        const int total = D * bpd + 2 * eib;
+        for (int pos = 0; pos < total; ++pos) {
+            int j, k;
+            if (pos < D * bpd) {
+                k = pos / D;
+                j = D - 1 - pos % D;
+            } else {
+                const int r = pos - D * bpd;
+                k = bpd + r / 2;
+                j = 1 - r % 2;
+            }
+            xq[j] |= (uint32_t)((cells[i] >> pos) & 1u) << k;
+        }
+        float* b = boxes + (size_t)i * 2 * D;
+        for (int j = 0; j < D; ++j) {
+            const unsigned extentInv = (1u << bpd) << (j < 2 ? eib : 0);
+            float extent = 1.0f / float(extentInv);
+            float offset = xq[j] * extent;
+            if (j < 2) {
+                const float sc = j == 0 ? sx : sy;
+                offset *= sc;
+                extent *= sc;
+            }
+            b[j] = offset;
+            b[D + j] = offset + extent;
+        }
+    }
+    return 0;
+}
+
+// Key of each leaf's box centre (boxes: L x (mn[D], mx[D])).
+int orc_leaf_keys(int D, int bpd, int eib, int F, float sx, float sy, const float* boxes, int L, uint64_t* keys) {
+    if (D > 8 || D * (bpd + F) + 2 * eib > 64 || bpd + F + eib > 31) return -1;
+    float c[8];
+    for (int i = 0; i < L; ++i) {
+        const float* b = boxes + (size_t)i * 2 * D;
+        for (int j = 0; j < D; ++j) c[j] = 0.5f * (b[j] + b[D + j]);
+        keys[i] = orc_key(c, D, bpd, eib, F, sx, sy);
+    }
+    return 0;
+}
+
+// Stable sort by key bits [beginBit, endBit): sorted keys and the permutation.
+int orc_sort_pairs(const uint64_t* keys, int n, int beginBit, int endBit, uint64_t* sortedKeys, uint32_t* order) {
+    if (beginBit < 0 || endBit > 64 || beginBit > endBit) return -1;
+    const int w = endBit - beginBit;
+    const uint64_t mask = w == 64 ? ~0ull : ((1ull << w) - 1ull);
+    std::vector<uint32_t> idx((size_t)n);
+    for (int i = 0; i < n; ++i) idx[i] = (uint32_t)i;
+    std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) {
+        const uint64_t ka = w ? (keys[a] >> beginBit) & mask : 0, kb = w ? (keys[b] >> beginBit) & mask : 0;
+        return ka < kb;
+    });
+    for (int i = 0; i < n; ++i) {
+        order[i] = idx[i];
+        sortedKeys[i] = keys[idx[i]];
+    }
+    return 0;
+}
+
+// Radix tree over n sorted keys, built top-down: a node spanning [first, last]
+// splits after the last position whose prefix with `first` is longer than the
+// node's own prefix; its children are the leaf or the internal node numbered
+// by the split (gamma, gamma + 1), the numbering of Karras (HPG 2012).
+int orc_karras(const uint64_t* k, int n, int* children, int* parents) {
+    if (n <= 0) return 0;
+    parents[0] = -1;
+    if (n == 1) return 0;
+    struct Span { int node, first, last; };
+    std::vector<Span> stack;
+    stack.push_back({0, 0, n - 1});
+    while (!stack.empty()) {
+        const Span s = stack.back();
+        stack.pop_back();
+        const int dnode = orc_prefix(k, n, s.first, s.last);
+        int lo = s.first, hi = s.last - 1;  // largest g in [first, last-1] with prefix(first, g) > dnode
+        while (lo < hi) {
+            const int mid = lo + (hi - lo + 1) / 2;
+            if (orc_prefix(k, n, s.first, mid) > dnode) lo = mid;
+            else hi = mid - 1;
+        }
+        const int g = lo;
+        const int left = g == s.first ? ~g : g;
+        const int right = g + 1 == s.last ? ~(g + 1) : g + 1;
+        children[2 * s.node] = left;
+        children[2 * s.node + 1] = right;
+        parents[left >= 0 ? left : (n - 1) + ~left] = s.node;
+        parents[right >= 0 ? right : (n - 1) + ~right] = s.node;
+        if (left >= 0) stack.push_back({left, s.first, g});
+        if (right >= 0) stack.push_back({right, g + 1, s.last});
+    }
+    return 0;
+}
+
+// Internal node boxes: componentwise min / max over each node's leaves
+// (leafBoxes by leaf slot, order = slots by sorted position).
+int orc_refit(int D, const float* leafBoxes, const uint32_t* order, int n, const int* children, float* boxes) {
+    if (n <= 1) return 0;
+    // children have larger spans' sub-ranges; a post-order walk from the root
+    std::vector<int> post;
+    std::vector<int> st{0};
+    while (!st.empty()) {
+        const int v = st.back();
+        st.pop_back();
+        post.push_back(v);
+        for (int c = 0; c < 2; ++c)
+            if (children[2 * v + c] >= 0) st.push_back(children[2 * v + c]);
+    }
+    for (size_t t = post.size(); t-- > 0;) {
+        const int v = post[t];
+        float* out = boxes + (size_t)v * 2 * D;
+        for (int c = 0; c < 2; ++c) {
+            const int ch = children[2 * v + c];
+            const float* b = ch >= 0 ? boxes + (size_t)ch * 2 * D : leafBoxes + (size_t)order[~ch] * 2 * D;
+            for (int j = 0; j < D; ++j) {
+                out[j] = c == 0 ? b[j] : std::min(out[j], b[j]);
+                out[D + j] = c == 0 ? b[D + j] : std::max(out[D + j], b[D + j]);
+            }
+        }
+    }
+    return 0;
+}
+
+// For each point the first leaf in key order whose box holds it (mn <= p < mx,
+// p <= mx on the domain's upper faces), -1 if none; brute force.
+int orc_locate(int D, const float* leafBoxes, const uint32_t* order, int n, const float* points, int m, int* out) {
+    std::vector<float> dom((size_t)D, -INFINITY);
+    for (int p = 0; p < n; ++p)
+        for (int j = 0; j < D; ++j) dom[j] = std::max(dom[j], leafBoxes[(size_t)p * 2 * D + D + j]);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int q = 0; q < m; ++q) {
+        const float* x = points + (size_t)q * D;
+        int found = -1;
+        for (int p = 0; p < n && found < 0; ++p) {
+            const float* b = leafBoxes + (size_t)order[p] * 2 * D;
+            bool in = true;
+            for (int j = 0; j < D && in; ++j)
+                in = b[j] <= x[j] && (x[j] < b[D + j] || (x[j] == b[D + j] && b[D + j] >= dom[j]));
+            if (in) found = (int)order[p];
+        }
+        out[q] = found;
+    }
+    return 0;
+}
+
 }  // extern "C"

@@ -48,6 +48,13 @@ def load():
             "orc_sincos": (None, [_F, C.POINTER(_F), C.POINTER(_F)]),
             "orc_render": (_I, [_I, _I, _I, _I, _F, _F, _F, _I, _I, _I, _P, _P, _I, _I, _P, _P, _P, _P, _P, _P, _P,
                                 _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_double)]),
+            "orc_morton_encode": (_I, [_I, _I, _I, _I, _F, _F, _P, _I, _P]),
+            "orc_morton_decode": (_I, [_I, _I, _I, _F, _F, _P, _I, _P]),
+            "orc_leaf_keys": (_I, [_I, _I, _I, _I, _F, _F, _P, _I, _P]),
+            "orc_sort_pairs": (_I, [_P, _I, _I, _I, _P, _P]),
+            "orc_karras": (_I, [_P, _I, _P, _P]),
+            "orc_refit": (_I, [_I, _P, _P, _I, _P, _P]),
+            "orc_locate": (_I, [_I, _P, _P, _I, _P, _I, _P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -194,6 +201,71 @@ def render(dim, bpd, eib, cand, alpha, sx, sy, budget, maxSamples, scene, width,
     wall = time.perf_counter() - t0
     assert rc == 0, rc
     return px, n.value, l.value, p.value, list(t), wall
+
+
+# ---- leaf ordering (Morton keys, stable sort, radix tree, point location) -----------
+def morton_encode(points, bpd, eib, fine, sx, sy) -> np.ndarray:
+    pts = np.ascontiguousarray(points, np.float32)
+    n, dim = pts.shape
+    keys = np.zeros(max(n, 1), np.uint64)
+    assert load().orc_morton_encode(dim, bpd, eib, fine, np.float32(sx), np.float32(sy), _p(pts), n, _p(keys)) == 0
+    return keys[:n]
+
+
+def morton_decode(cells, dim, bpd, eib, sx, sy) -> np.ndarray:
+    c = np.ascontiguousarray(cells, np.uint64)
+    boxes = np.zeros((max(c.size, 1), 2 * dim), np.float32)
+    assert load().orc_morton_decode(dim, bpd, eib, np.float32(sx), np.float32(sy), _p(c), c.size, _p(boxes)) == 0
+    return boxes[:c.size]
+
+
+def leaf_keys(boxes, dim, bpd, eib, fine, sx, sy) -> np.ndarray:
+    b = np.ascontiguousarray(boxes, np.float32)
+    L = b.shape[0]
+    keys = np.zeros(max(L, 1), np.uint64)
+    assert load().orc_leaf_keys(dim, bpd, eib, fine, np.float32(sx), np.float32(sy), _p(b), L, _p(keys)) == 0
+    return keys[:L]
+
+
+def sort_pairs(keys, begin=0, end=64):
+    """(sorted keys, permutation) of a stable sort on key bits [begin, end)."""
+    k = np.ascontiguousarray(keys, np.uint64)
+    n = k.size
+    sk = np.zeros(max(n, 1), np.uint64)
+    order = np.zeros(max(n, 1), np.uint32)
+    assert load().orc_sort_pairs(_p(k), n, begin, end, _p(sk), _p(order)) == 0
+    return sk[:n], order[:n]
+
+
+def karras(sorted_keys):
+    """(children [n-1, 2], parents [2n-1]) of the radix tree over sorted keys."""
+    k = np.ascontiguousarray(sorted_keys, np.uint64)
+    n = k.size
+    children = np.zeros((max(n - 1, 1), 2), np.int32)
+    parents = np.zeros(max(2 * n - 1, 1), np.int32)
+    assert load().orc_karras(_p(k), n, _p(children), _p(parents)) == 0
+    return children[:max(n - 1, 0)], parents[:max(2 * n - 1, 0)]
+
+
+def refit(leaf_boxes, order, children):
+    b = np.ascontiguousarray(leaf_boxes, np.float32)
+    o = np.ascontiguousarray(order, np.uint32)
+    ch = np.ascontiguousarray(children, np.int32)
+    n = o.size
+    dim = b.shape[1] // 2
+    boxes = np.zeros((max(n - 1, 1), 2 * dim), np.float32)
+    assert load().orc_refit(dim, _p(b), _p(o), n, _p(ch) if ch.size else None, _p(boxes)) == 0
+    return boxes[:max(n - 1, 0)]
+
+
+def locate(leaf_boxes, order, points) -> np.ndarray:
+    b = np.ascontiguousarray(leaf_boxes, np.float32)
+    o = np.ascontiguousarray(order, np.uint32)
+    pts = np.ascontiguousarray(points, np.float32)
+    m = pts.shape[0]
+    out = np.zeros(max(m, 1), np.int32)
+    assert load().orc_locate(b.shape[1] // 2, _p(b), _p(o), o.size, _p(pts), m, _p(out)) == 0
+    return out[:m]
 
 
 # ---- the reference's own kernels (patched copy built into oracle/_ref) ---------------

@@ -100,6 +100,14 @@ SIGNATURES = {
     "mdas_batch_render": (_I, [_P, C.POINTER(RenderStats)]),
     "mdas_batch_set_tuning": (_I, [_P, C.POINTER(_I)]),
     "mdas_batch_autotune": (_I, [_P, _I, C.POINTER(_I), C.POINTER(C.c_double)]),
+    "mdas_morton_key_bits": (_I, [_I, _I, _I, _I]),
+    "mdas_morton_encode": (_I, [_I, _I, _I, _I, _F, _F, _P, _I, _P, _P]),
+    "mdas_morton_decode": (_I, [_I, _I, _I, _F, _F, _P, _I, _P, _P]),
+    "mdas_radix_sort_pairs": (_I, [_P, C.POINTER(C.c_size_t), _P, _P, _P, _P, _I, _I, _I, _P]),
+    "mdas_leaf_order": (_I, [_P, _I, _P, _P]),
+    "mdas_build_hierarchy": (_I, [_P, _I]),
+    "mdas_get_hierarchy": (_I, [_P, C.POINTER(_I), _P, _P, _P, _P, _P]),
+    "mdas_locate": (_I, [_P, _P, _I, _P]),
     "mdas_config_defaults": (_I, [C.POINTER(Config)]),
     "mdas_config_read": (_I, [C.c_char_p, C.POINTER(Config), C.c_char_p, _I]),
 }

@@ -4,7 +4,7 @@ Each translation unit is compiled with the flags its arithmetic needs:
 
 * ``kdgrid_fast.cu`` — ``--use_fast_math``, the reference's flags
   (SDK/CMakeLists.txt:163-180), so results match the reference's kernels;
-* ``kdgrid_ieee.cu`` and ``integrand.cu`` — strict IEEE binary32 (no FMA
+* ``kdgrid_ieee.cu``, ``integrand.cu`` and ``order.cu`` — strict IEEE binary32 (no FMA
   contraction, IEEE division and square root, subnormals kept), so results
   match a CPU restatement bit for bit;
 * host code — ``-ffp-contract=off`` so scene generation gives the same floats
@@ -39,9 +39,10 @@ UNITS = [
     ("integrand.cu", IEEE),
     ("capi.cu", []),
     ("noalloc.cu", FAST),
+    ("order.cu", IEEE),
 ]
 CXX_UNITS = ["env.cpp"]
-HEADERS = ["grid_types.h", "ieee_math.h", "integrand.h", "kdgrid_kernels.cuh", "batch_kernels.cuh", "scene.h"]
+HEADERS = ["grid_types.h", "ieee_math.h", "integrand.h", "kdgrid_kernels.cuh", "batch_kernels.cuh", "scene.h", "order.h"]
 
 
 def nvcc() -> str:

@@ -17,6 +17,7 @@
 #include "../../include/mdas.h"
 #include "grid_types.h"
 #include "scene.h"
+#include "order.h"
 
 namespace {
 
@@ -77,6 +78,19 @@ struct mdas_grid {
     std::vector<PendingTiming> pending;
     RenderGraph graph;
     cudaStream_t captureStream = nullptr, bodyStream = nullptr;
+    // leaf order and hierarchy (mdas_leaf_order, mdas_build_hierarchy)
+    uint64_t version = 0;             // bumped by every call that changes the leaves
+    uint64_t hierVersion = ~0ull;     // version the hierarchy was built for
+    int hierN = 0, hierCap = 0, hierFineBits = 0;
+    uint64_t* hKeys = nullptr;        // [cap] key of each leaf slot
+    uint64_t* hSorted = nullptr;      // [cap] keys in ascending order
+    uint32_t* hOrder = nullptr;       // [cap] leaf slots in key order
+    int2* hChildren = nullptr;        // [cap] children of the internal nodes
+    int* hParents = nullptr;          // [2 cap] parents of the internal nodes, then of the leaves
+    float* hBoxes = nullptr;          // [cap * 2D] boxes of the internal nodes
+    unsigned* hVisits = nullptr;      // [cap + 1] refit arrival counters, then the locate status word
+    void* sortTemp = nullptr;
+    size_t sortTempBytes = 0;
 };
 
 namespace {
@@ -169,6 +183,7 @@ int read_counts(mdas_grid* g) {
     if (e != cudaSuccess) return MDAS_ERR_CUDA;
     g->N = g->hcounts->N;
     g->L = g->hcounts->L;
+    g->version += 1;
     g->newN = g->hcounts->newN;
     g->newL = g->hcounts->newL;
     return g->hcounts->status ? g->hcounts->status : MDAS_OK;
@@ -194,6 +209,14 @@ void free_grid(mdas_grid* g) {
     cudaFree(g->dg.accepted);
     cudaFree(g->dg.chunkTile);
     cudaFree(g->dg.dirty);
+    cudaFree(g->hKeys);
+    cudaFree(g->hSorted);
+    cudaFree(g->hOrder);
+    cudaFree(g->hChildren);
+    cudaFree(g->hParents);
+    cudaFree(g->hBoxes);
+    cudaFree(g->hVisits);
+    cudaFree(g->sortTemp);
     if (g->scratch) cudaFree(g->scratch);
     if (g->hcounts) cudaFreeHost(g->hcounts);
     delete g->log;
@@ -342,6 +365,7 @@ int mdas_initial_sampling(mdas_grid* g) {
     if (rc) return rc;
     g->N = (int)N;
     g->L = (int)L;
+    g->version += 1;
     g->newN = 0;
     g->newL = 0;
     g->initialized = true;
@@ -557,6 +581,7 @@ int mdas_load_state(mdas_grid* g, int numberOfSamples, int numberOfNodes, const 
     if (e != cudaSuccess) return MDAS_ERR_CUDA;
     g->N = (int)N;
     g->L = (int)L;
+    g->version += 1;
     g->newN = 0;
     g->newL = 0;
     g->initialized = true;
@@ -1190,6 +1215,186 @@ int mdas_render_host(mdas_grid* g, mdas_scene* s, const float* hostPrims, int bu
     cudaError_t e = cudaMemcpyAsync(hostPixels, g->scratch, bytes, cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     return status_of(e);
+}
+
+// ---- Morton keys, radix sort, leaf order, hierarchy, point location
+
+int mdas_morton_key_bits(int dim, int bitsPerDim, int extraImgBits, int fineBits) {
+    return mdas_order::key_bits(dim, bitsPerDim, extraImgBits, fineBits);
+}
+
+int mdas_morton_encode(int dim, int bitsPerDim, int extraImgBits, int fineBits, float scaleX, float scaleY,
+                       const float* points, int n, uint64_t* keys, void* stream) {
+    if (dim < 1 || n < 0 || (n > 0 && (!points || !keys)) || !(scaleX > 0.0f) || !(scaleY > 0.0f) ||
+        mdas_order::key_bits(dim, bitsPerDim, extraImgBits, fineBits) < 0)
+        return MDAS_ERR_INVALID;
+    return status_of(mdas_order::morton_encode(points, n, dim, bitsPerDim, extraImgBits, fineBits, scaleX, scaleY,
+                                               keys, static_cast<cudaStream_t>(stream)));
+}
+
+int mdas_morton_decode(int dim, int bitsPerDim, int extraImgBits, float scaleX, float scaleY, const uint64_t* cells,
+                       int n, float* boxes, void* stream) {
+    if (dim < 1 || n < 0 || (n > 0 && (!cells || !boxes)) || mdas_order::key_bits(dim, bitsPerDim, extraImgBits, 0) < 0 ||
+        bitsPerDim + extraImgBits > 31)
+        return MDAS_ERR_INVALID;
+    return status_of(mdas_order::morton_decode(cells, n, dim, bitsPerDim, extraImgBits, scaleX, scaleY, boxes,
+                                               static_cast<cudaStream_t>(stream)));
+}
+
+int mdas_radix_sort_pairs(void* temp, size_t* tempBytes, const uint64_t* keysIn, uint64_t* keysOut,
+                          const uint32_t* valuesIn, uint32_t* valuesOut, int n, int beginBit, int endBit,
+                          void* stream) {
+    if (!tempBytes || n < 0 || beginBit < 0 || endBit > 64 || beginBit > endBit) return MDAS_ERR_INVALID;
+    const size_t need = mdas_order::sort_temp_bytes(n, beginBit, endBit);
+    if (!temp) {
+        *tempBytes = need;
+        return MDAS_OK;
+    }
+    if (*tempBytes < need || (n > 0 && (!keysIn || !keysOut || !valuesOut)) || (n > 0 && keysIn == keysOut))
+        return MDAS_ERR_INVALID;
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned* status = nullptr;
+    cudaError_t e = mdas_order::radix_sort(temp, *tempBytes, keysIn, keysOut, valuesIn, valuesOut, n, beginBit, endBit,
+                                           s, &status);
+    unsigned h = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, status, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    return h ? MDAS_ERR_TIMEOUT : MDAS_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+int ensure_hierarchy(mdas_grid* g, int n) {
+    if (g->hierCap >= n && g->hKeys) return MDAS_OK;
+    const int cap = n > 1 ? n : 1;
+    cudaFree(g->hKeys);
+    cudaFree(g->hSorted);
+    cudaFree(g->hOrder);
+    cudaFree(g->hChildren);
+    cudaFree(g->hParents);
+    cudaFree(g->hBoxes);
+    cudaFree(g->hVisits);
+    cudaFree(g->sortTemp);
+    g->hKeys = g->hSorted = nullptr;
+    g->hOrder = nullptr;
+    g->hChildren = nullptr;
+    g->hParents = nullptr;
+    g->hBoxes = nullptr;
+    g->hVisits = nullptr;
+    g->sortTemp = nullptr;
+    g->hierCap = 0;
+    g->hierVersion = ~0ull;
+    const size_t c = (size_t)cap;
+    g->sortTempBytes = mdas_order::sort_temp_bytes(cap, 0, 64);
+    const bool ok = cudaMalloc(&g->hKeys, sizeof(uint64_t) * c) == cudaSuccess &&
+                    cudaMalloc(&g->hSorted, sizeof(uint64_t) * c) == cudaSuccess &&
+                    cudaMalloc(&g->hOrder, sizeof(uint32_t) * c) == cudaSuccess &&
+                    cudaMalloc(&g->hChildren, sizeof(int2) * c) == cudaSuccess &&
+                    cudaMalloc(&g->hParents, sizeof(int) * 2 * c) == cudaSuccess &&
+                    cudaMalloc(&g->hBoxes, sizeof(float) * 2 * g->dg.D * c) == cudaSuccess &&
+                    cudaMalloc(&g->hVisits, sizeof(unsigned) * (c + 1)) == cudaSuccess &&
+                    cudaMalloc(&g->sortTemp, g->sortTempBytes) == cudaSuccess;
+    if (!ok) return MDAS_ERR_ALLOC;
+    g->hierCap = cap;
+    return MDAS_OK;
+}
+
+// Leaf keys and their order (sorted keys in hSorted, slots in hOrder).
+int order_leaves(mdas_grid* g, int fineBits) {
+    if (!g->initialized) return MDAS_ERR_STATE;
+    const MdasDeviceGrid& d = g->dg;
+    if (fineBits < 0) fineBits = mdas_order::max_fine_bits(d.D, d.bitsPerDim, d.extraImgBits);
+    const int bits = mdas_order::key_bits(d.D, d.bitsPerDim, d.extraImgBits, fineBits);
+    if (bits < 0) return MDAS_ERR_INVALID;
+    int rc = ensure_hierarchy(g, g->L);
+    if (rc) return rc;
+    cudaError_t e = mdas_order::leaf_keys(d, g->L, fineBits, g->hKeys, g->stream);
+    unsigned* status = nullptr;
+    if (e == cudaSuccess)
+        e = mdas_order::radix_sort(g->sortTemp, g->sortTempBytes, g->hKeys, g->hSorted, nullptr, g->hOrder, g->L, 0,
+                                   bits, g->stream, &status);
+    g->launches += 1 + mdas_order::sort_launches(g->L, 0, bits);
+    unsigned h = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, status, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    if (h) return MDAS_ERR_TIMEOUT;
+    g->hierFineBits = fineBits;
+    g->hierN = g->L;
+    return MDAS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mdas_leaf_order(mdas_grid* g, int fineBits, uint64_t* keys, uint32_t* order) {
+    if (!g) return MDAS_ERR_INVALID;
+    g->hierVersion = ~0ull;  // the hierarchy buffers are reused
+    int rc = order_leaves(g, fineBits);
+    if (rc) return rc;
+    cudaError_t e = cudaSuccess;
+    if (keys && g->L) e = cudaMemcpyAsync(keys, g->hSorted, sizeof(uint64_t) * g->L, cudaMemcpyDeviceToDevice, g->stream);
+    if (order && g->L && e == cudaSuccess)
+        e = cudaMemcpyAsync(order, g->hOrder, sizeof(uint32_t) * g->L, cudaMemcpyDeviceToDevice, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    return status_of(e);
+}
+
+int mdas_build_hierarchy(mdas_grid* g, int fineBits) {
+    if (!g) return MDAS_ERR_INVALID;
+    g->hierVersion = ~0ull;
+    int rc = order_leaves(g, fineBits);
+    if (rc) return rc;
+    const int n = g->L;
+    cudaError_t e = mdas_order::karras_build(g->hSorted, n, g->hChildren, g->hParents, g->stream);
+    if (e == cudaSuccess)
+        e = mdas_order::karras_refit(g->dg, g->hOrder, n, g->hChildren, g->hParents, g->hVisits, g->hBoxes, g->stream);
+    g->launches += 2;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    g->hierVersion = g->version;
+    return MDAS_OK;
+}
+
+int mdas_get_hierarchy(mdas_grid* g, int* numLeaves, uint64_t* keys, uint32_t* order, int* children, int* parents,
+                       float* boxes) {
+    if (!g) return MDAS_ERR_INVALID;
+    if (g->hierVersion != g->version) return MDAS_ERR_STATE;
+    const size_t n = (size_t)g->hierN;
+    if (numLeaves) *numLeaves = (int)n;
+    cudaError_t e = cudaSuccess;
+    auto cp = [&](void* dst, const void* src, size_t bytes) {
+        if (dst && bytes && e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, g->stream);
+    };
+    cp(keys, g->hSorted, sizeof(uint64_t) * n);
+    cp(order, g->hOrder, sizeof(uint32_t) * n);
+    if (n > 1) {
+        cp(children, g->hChildren, sizeof(int2) * (n - 1));
+        cp(boxes, g->hBoxes, sizeof(float) * 2 * g->dg.D * (n - 1));
+    }
+    cp(parents, g->hParents, sizeof(int) * (2 * n - 1));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    return status_of(e);
+}
+
+int mdas_locate(mdas_grid* g, const float* points, int n, int* leaves) {
+    if (!g || n < 0 || (n > 0 && (!points || !leaves))) return MDAS_ERR_INVALID;
+    if (g->hierVersion != g->version) return MDAS_ERR_STATE;
+    unsigned* status = g->hVisits + g->hierCap;
+    cudaError_t e = cudaMemsetAsync(status, 0, sizeof(unsigned), g->stream);
+    if (e == cudaSuccess)
+        e = mdas_order::locate(g->dg, g->hOrder, g->hierN, g->hChildren, g->hBoxes, points, n, leaves, status,
+                               g->stream);
+    g->launches += 1;
+    unsigned h = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, status, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    return h ? MDAS_ERR_CAPACITY : MDAS_OK;
 }
 
 }  // extern "C"

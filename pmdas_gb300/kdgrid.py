@@ -215,6 +215,87 @@ class KDGrid:
         N.check(self._lib.mdas_get_launch_count(self._h, C.byref(v)), "launch_count")
         return v.value
 
+    # ---- leaf order and hierarchy (no reference counterpart)
+    def LeafOrder(self, fineBits: int = -1):
+        """(sorted keys, leaf slots in key order) as torch CUDA tensors (int64 holding
+        uint64 keys, int32 holding uint32 slots)."""
+        import torch
+        n = self.GetNumberOfNodes()
+        keys = torch.empty(max(n, 1), dtype=torch.int64, device="cuda")
+        order = torch.empty(max(n, 1), dtype=torch.int32, device="cuda")
+        N.check(self._lib.mdas_leaf_order(self._h, fineBits, _ptr(keys), _ptr(order)), "leaf_order")
+        return keys[:n], order[:n]
+
+    def BuildHierarchy(self, fineBits: int = -1):
+        N.check(self._lib.mdas_build_hierarchy(self._h, fineBits), "build_hierarchy")
+
+    def Hierarchy(self) -> dict:
+        """Host copy of the hierarchy: keys (uint64), order (uint32), children
+        [n-1, 2], parents [2n-1], boxes [n-1, 2*dim]."""
+        n = self.GetNumberOfNodes()
+        h = dict(keys=np.empty(n, np.uint64), order=np.empty(n, np.uint32),
+                 children=np.empty((max(n - 1, 0), 2), np.int32), parents=np.empty(max(2 * n - 1, 0), np.int32),
+                 boxes=np.empty((max(n - 1, 0), 2 * self.dim), np.float32))
+        cnt = C.c_int()
+        N.check(self._lib.mdas_get_hierarchy(self._h, C.byref(cnt), _ptr(h["keys"]), _ptr(h["order"]),
+                                             _ptr(h["children"]), _ptr(h["parents"]), _ptr(h["boxes"])), "hierarchy")
+        return h
+
+    def Locate(self, points):
+        """Leaf slot holding each point (torch CUDA float32 [n, dim]) -> int32 [n], -1 outside."""
+        import torch
+        pts = points.contiguous()
+        out = torch.empty(max(pts.shape[0], 1), dtype=torch.int32, device="cuda")
+        N.check(self._lib.mdas_locate(self._h, _ptr(pts), int(pts.shape[0]), _ptr(out)), "locate")
+        return out[:pts.shape[0]]
+
+
+def morton_key_bits(dim: int, bitsPerDim: int, extraImgBits: int, fineBits: int) -> int:
+    return N.load().mdas_morton_key_bits(dim, bitsPerDim, extraImgBits, fineBits)
+
+
+def morton_encode(points, bitsPerDim: int, extraImgBits: int, fineBits: int, scaleX: float, scaleY: float):
+    """Keys (torch int64 holding uint64) of points (torch CUDA float32 [n, dim])."""
+    import torch
+    pts = points.contiguous()
+    n, dim = pts.shape
+    keys = torch.empty(max(n, 1), dtype=torch.int64, device="cuda")
+    N.check(N.load().mdas_morton_encode(dim, bitsPerDim, extraImgBits, fineBits, float(scaleX), float(scaleY),
+                                        _ptr(pts), n, _ptr(keys), None), "morton_encode")
+    torch.cuda.synchronize()
+    return keys[:n]
+
+
+def morton_decode(cells, dim: int, bitsPerDim: int, extraImgBits: int, scaleX: float, scaleY: float):
+    """Boxes [n, 2*dim] (mn, mx) of cells (torch CUDA int64 holding uint64)."""
+    import torch
+    c = cells.contiguous()
+    n = c.shape[0]
+    boxes = torch.empty((max(n, 1), 2 * dim), dtype=torch.float32, device="cuda")
+    N.check(N.load().mdas_morton_decode(dim, bitsPerDim, extraImgBits, float(scaleX), float(scaleY), _ptr(c), n,
+                                        _ptr(boxes), None), "morton_decode")
+    torch.cuda.synchronize()
+    return boxes[:n]
+
+
+def radix_sort_pairs(keys, values=None, beginBit: int = 0, endBit: int = 64):
+    """Stable sort of (keys, values) on key bits [beginBit, endBit): torch CUDA int64
+    keys (read as uint64) and int32 values (uint32; None = 0..n-1)."""
+    import torch
+    lib = N.load()
+    k = keys.contiguous()
+    n = k.shape[0]
+    v = values.contiguous() if values is not None else None
+    need = C.c_size_t(0)
+    N.check(lib.mdas_radix_sort_pairs(None, C.byref(need), None, None, None, None, n, beginBit, endBit, None),
+            "radix_sort_pairs")
+    temp = torch.empty(max(need.value, 1), dtype=torch.uint8, device="cuda")
+    ko = torch.empty(max(n, 1), dtype=torch.int64, device="cuda")
+    vo = torch.empty(max(n, 1), dtype=torch.int32, device="cuda")
+    N.check(lib.mdas_radix_sort_pairs(_ptr(temp), C.byref(need), _ptr(k), _ptr(ko), _ptr(v), _ptr(vo), n, beginBit,
+                                      endBit, None), "radix_sort_pairs")
+    return ko[:n], vo[:n]
+
 
 @dataclass
 class SceneDesc:
