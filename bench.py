@@ -50,6 +50,7 @@ def parse_args():
     ap.add_argument("--no-reference-cuda", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-quality", action="store_true")
+    ap.add_argument("--no-order", action="store_true", help="skip the leaf-order / hierarchy / locate timings")
     return ap.parse_args()
 
 
@@ -299,6 +300,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
                "d2h_bytes_per_step": int(W * H * 16 + 56 * (st.passes + 1)),
                "ms_per_step": round(e2e_s * 1e3, 3), "includes": "integrand, host syncs per pass, copies"}
 
+    order = None if args.no_order else order_block(grid, wl, peak)
+
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(mdas_ms / args.steps, 4), "higher_is_better": True,
@@ -321,10 +324,59 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         "stage_bytes_per_step": by,
         "e2e": e2e,
         "quality": quality,
+        "leaf_order": order,
         "gpu_launches": int(launches),
         "clocks": clk,
     }
     return line, wl
+
+
+def order_block(grid, wl, peak: float, reps: int = 5) -> dict:
+    """Leaf ordering on the final leaves of a render: keys + radix sort, the Karras
+    hierarchy, the radix sort alone (with its HBM roofline) and point location."""
+    import torch
+
+    import pmdas_gb300 as P
+
+    D, bpd, eib = wl.dim, wl.bitsPerDim, wl.extraImgBits
+    fine = min((64 - D * bpd - 2 * eib) // D, 31 - bpd - eib)
+    bits = P.morton_key_bits(D, bpd, eib, fine)
+    L = grid.GetNumberOfNodes()
+    sorted_keys, order = grid.LeafOrder(-1)
+    slot_keys = torch.empty_like(sorted_keys)
+    slot_keys[order.long()] = sorted_keys  # keys in slot order: the sort's real input
+    pts = torch.rand(1 << 22, D, device="cuda")
+    pts[:, 0] *= wl.scaleX
+    pts[:, 1] *= wl.scaleY
+
+    def timed(fn):
+        ts = []
+        for _ in range(reps + 1):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.median(ts[1:])
+
+    leaf_order_ms = timed(lambda: grid.LeafOrder(-1))
+    sort_ms = timed(lambda: P.radix_sort_pairs(slot_keys, None, 0, bits))
+    hier_ms = timed(lambda: grid.BuildHierarchy(-1))
+    loc_ms = timed(lambda: grid.Locate(pts))
+    passes = (bits + 7) // 8
+    # histogram reads the keys once; each pass reads key (+ value after the first) and writes both
+    sort_bytes = L * (8 + passes * 24 - 4)
+    achieved = sort_bytes / (sort_ms / 1e3) / 1e9
+    return {"leaves": L, "key_bits": bits, "fine_bits_per_dim": fine,
+            "leaf_order_ms": round(leaf_order_ms, 4), "hierarchy_ms": round(hier_ms, 4),
+            "sort_ms": round(sort_ms, 4), "sort_mkeys_per_s": round(L / (sort_ms / 1e3) / 1e6, 1),
+            "sort_roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                              "frac": round(achieved / peak, 4), "algorithmic_bytes": int(sort_bytes),
+                              "passes": passes, "note": "whole sort (histogram + passes) incl. launch gaps"},
+            "locate_points": int(pts.shape[0]), "locate_ms": round(loc_ms, 4),
+            "locate_mpoints_per_s": round(pts.shape[0] / (loc_ms / 1e3) / 1e6, 1)}
 
 
 def run_batch(args, rank: int, world: int, local_rank: int) -> dict:
