@@ -326,6 +326,51 @@ int mdas_get_hierarchy(mdas_grid* g, int* numLeaves, uint64_t* keys, uint32_t* o
  * hierarchy (MDAS_ERR_STATE otherwise).  Synchronises the grid's stream. */
 int mdas_locate(mdas_grid* g, const float* points, int n, int* leaves);
 
+/* ---- Learned acceptance: a leaf-priority MLP on the tensor cores.
+ *
+ * No reference counterpart.  The reference accepts a leaf with probability
+ * powf(error / g_error, alpha) (kdgrid.cu:326).  In learned mode the ratio is
+ * 2^prediction / g_error (at most 1), where the prediction is a
+ * 16 -> 64 -> 64 -> 1 ReLU MLP (BF16 tcgen05 GEMMs, FP32 accumulation) of
+ * per-leaf features: log2 box extents (image axes relative to the image), their
+ * mean, the sample count, log2(1 + mean value) and log2(1 + mean absolute
+ * deviation) per colour channel.  The plain error is the judge: every pass the
+ * model takes `trainSteps` Adam steps on `batch` leaves against
+ * log2(error) / 32, and a fixed hashed `fallback` fraction of the leaves keeps
+ * the plain ratio.  Learned mode runs in mdas_sampling_pass / mdas_render
+ * (not in mdas_render_graph, which returns MDAS_ERR_STATE while it is on). */
+#define MDAS_MLP_PARAMS 5313 /* W1[64][16], b1[64], W2[64][64], b2[64], w3[64], b3 */
+
+typedef struct mdas_learned_config {
+    int trainSteps;     /* Adam steps per pass (default 4) */
+    int batch;          /* leaves per step (default 16384) */
+    float learningRate; /* default 2e-3 */
+    float fallback;     /* fraction of leaves that keep the plain ratio (default 0.05) */
+    uint64_t seed;      /* weight initialisation (default 1) */
+} mdas_learned_config;
+
+int mdas_learned_defaults(mdas_learned_config* cfg);
+/* Turns learned mode on with freshly initialised weights (cfg == NULL: off). */
+int mdas_learned_enable(mdas_grid* g, const mdas_learned_config* cfg);
+/* Trains on the current leaves (needs their errors: after mdas_compute_errors)
+ * and predicts every leaf; *loss (host, optional) = the last step's mean
+ * squared error.  mdas_sampling_pass calls it between its two halves. */
+int mdas_learned_update(mdas_grid* g, float* loss);
+/* Host copies of the FP32 parameters (MDAS_MLP_PARAMS floats). */
+int mdas_learned_get_params(mdas_grid* g, float* params);
+int mdas_learned_set_params(mdas_grid* g, const float* params);
+/* Device copy of the current predictions (numberOfNodes floats). */
+int mdas_learned_predictions(mdas_grid* g, float* pred);
+/* Device copy of the leaves' features (numberOfNodes x 16 floats). */
+int mdas_leaf_features(mdas_grid* g, float* features);
+
+/* The MLP on its own (device pointers): pred[m] of features[m x 16];
+ * gradients of mean((pred - target)^2) into grads[MDAS_MLP_PARAMS] and the
+ * loss into *loss (host). */
+int mdas_mlp_forward(const float* params, const float* features, int m, float* pred, void* stream);
+int mdas_mlp_gradients(const float* params, const float* features, const float* targets, int m, float* grads,
+                       float* loss, void* stream);
+
 /* ---- env configuration (SDK/sutil/Environment.{h,cpp}; the options the MDAS
  *      apps register, optixMotionBlur.cpp:104-137) ---- */
 typedef struct mdas_config {

@@ -36,6 +36,14 @@ class MdasError(RuntimeError):
         super().__init__(f"{what}: {status_string(status)} (status {status})")
 
 
+MLP_PARAMS = 5313
+
+
+class LearnedConfig(C.Structure):
+    _fields_ = [("trainSteps", C.c_int), ("batch", C.c_int), ("learningRate", C.c_float), ("fallback", C.c_float),
+                ("seed", C.c_uint64)]
+
+
 class RenderStats(C.Structure):
     _fields_ = [("numberOfSamples", C.c_int), ("numberOfNodes", C.c_int), ("passes", C.c_int),
                 ("reserved", C.c_int), ("stageMs", C.c_double * 5)]
@@ -108,6 +116,15 @@ SIGNATURES = {
     "mdas_build_hierarchy": (_I, [_P, _I]),
     "mdas_get_hierarchy": (_I, [_P, C.POINTER(_I), _P, _P, _P, _P, _P]),
     "mdas_locate": (_I, [_P, _P, _I, _P]),
+    "mdas_learned_defaults": (_I, [C.POINTER(LearnedConfig)]),
+    "mdas_learned_enable": (_I, [_P, C.POINTER(LearnedConfig)]),
+    "mdas_learned_update": (_I, [_P, C.POINTER(_F)]),
+    "mdas_learned_get_params": (_I, [_P, _P]),
+    "mdas_learned_set_params": (_I, [_P, _P]),
+    "mdas_learned_predictions": (_I, [_P, _P]),
+    "mdas_leaf_features": (_I, [_P, _P]),
+    "mdas_mlp_forward": (_I, [_P, _P, _I, _P, _P]),
+    "mdas_mlp_gradients": (_I, [_P, _P, _P, _I, _P, C.POINTER(_F), _P]),
     "mdas_config_defaults": (_I, [C.POINTER(Config)]),
     "mdas_config_read": (_I, [C.c_char_p, C.POINTER(Config), C.c_char_p, _I]),
 }

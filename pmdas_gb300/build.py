@@ -40,9 +40,10 @@ UNITS = [
     ("capi.cu", []),
     ("noalloc.cu", FAST),
     ("order.cu", IEEE),
+    ("mlp.cu", []),
 ]
 CXX_UNITS = ["env.cpp"]
-HEADERS = ["grid_types.h", "ieee_math.h", "integrand.h", "kdgrid_kernels.cuh", "batch_kernels.cuh", "scene.h", "order.h"]
+HEADERS = ["grid_types.h", "ieee_math.h", "integrand.h", "kdgrid_kernels.cuh", "batch_kernels.cuh", "scene.h", "order.h", "mlp.h"]
 
 
 def nvcc() -> str:

@@ -18,6 +18,7 @@
 #include "grid_types.h"
 #include "scene.h"
 #include "order.h"
+#include "mlp.h"
 
 namespace {
 
@@ -91,6 +92,14 @@ struct mdas_grid {
     unsigned* hVisits = nullptr;      // [cap + 1] refit arrival counters, then the locate status word
     void* sortTemp = nullptr;
     size_t sortTempBytes = 0;
+    // learned acceptance (mdas_learned_enable)
+    bool learned = false;
+    mdas_learned_config lcfg{};
+    float* lState = nullptr;            // params, Adam m1, m2, grads (MDAS_MLP_PARAMS each), loss sum, status
+    mdas_mlp::Packed* lPacked = nullptr;
+    float* lPred = nullptr;             // [maxNodes] predicted log2(error) / MDAS_MLP_TARGET_SCALE
+    uint64_t lPredVersion = ~0ull;      // grid version the predictions belong to
+    int lStep = 0;
 };
 
 namespace {
@@ -217,6 +226,9 @@ void free_grid(mdas_grid* g) {
     cudaFree(g->hBoxes);
     cudaFree(g->hVisits);
     cudaFree(g->sortTemp);
+    cudaFree(g->lState);
+    cudaFree(g->lPacked);
+    cudaFree(g->lPred);
     if (g->scratch) cudaFree(g->scratch);
     if (g->hcounts) cudaFreeHost(g->hcounts);
     delete g->log;
@@ -402,7 +414,9 @@ int mdas_adaptive_sampling(mdas_grid* g) {
     const int64_t tiles = ((int64_t)g->L + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
     const int gridDecide = grid_for(g, MDAS_K_DECIDE, tiles * 256);
     const int gridPlace = grid_for(g, MDAS_K_ADAPTIVE, g->L);  // one thread per accepted leaf (<= L)
+    g->dg.priority = g->learned && g->lPredVersion == g->version ? g->lPred : nullptr;
     int rc = timed(g, 2, [&]() { return launch_adaptive(g, gridDecide, gridPlace); });
+    g->dg.priority = nullptr;
     g->dirtyValid = g->errorsClean;
     g->errorsClean = false;
     g->launches += 3;
@@ -419,6 +433,10 @@ int mdas_adaptive_sampling(mdas_grid* g) {
 int mdas_sampling_pass(mdas_grid* g) {
     int rc = mdas_compute_errors(g);
     if (rc) return rc;
+    if (g->learned) {
+        rc = mdas_learned_update(g, nullptr);
+        if (rc) return rc;
+    }
     return mdas_adaptive_sampling(g);
 }
 
@@ -894,6 +912,7 @@ int build_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, i
 int mdas_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, int width, int height,
                       mdas_render_stats* stats) {
     if (!g || !s || !pixels || width <= 0 || height <= 0 || s->desc.dim > g->dg.D) return MDAS_ERR_INVALID;
+    if (g->learned) return MDAS_ERR_STATE;  // learned mode trains between passes: mdas_render runs it
     int rc = scene_upload(s, g->stream);
     if (rc) return rc;
     flush_timing(g);
@@ -1077,6 +1096,7 @@ int mdas_batch_create(mdas_batch** out, int n, mdas_grid* const* grids, mdas_sce
         }
         MdasBatchImage im{};
         im.g = g->dg;
+        im.g.priority = nullptr;  // batched renders use the plain acceptance
         im.pixels = reinterpret_cast<float4*>(pixels[i]);
         im.width = widths[i];
         im.height = heights[i];
@@ -1395,6 +1415,223 @@ int mdas_locate(mdas_grid* g, const float* points, int n, int* leaves) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     if (e != cudaSuccess) return MDAS_ERR_CUDA;
     return h ? MDAS_ERR_CAPACITY : MDAS_OK;
+}
+
+
+// ---- learned acceptance: the tcgen05 MLP
+
+int mdas_learned_defaults(mdas_learned_config* cfg) {
+    if (!cfg) return MDAS_ERR_INVALID;
+    cfg->trainSteps = 4;
+    cfg->batch = 16384;
+    cfg->learningRate = 2e-3f;
+    cfg->fallback = 0.05f;
+    cfg->seed = 1;
+    return MDAS_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+uint64_t splitmix(uint64_t& x) {
+    uint64_t z = (x += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+// Uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) for every weight and bias of a layer.
+void mlp_init(std::vector<float>& p, uint64_t seed) {
+    p.assign(MDAS_MLP_PARAMS, 0.0f);
+    uint64_t st = seed;
+    auto fill = [&](int off, int n, int fanIn) {
+        const float b = 1.0f / sqrtf((float)fanIn);
+        for (int i = 0; i < n; ++i) {
+            const double u = (double)(splitmix(st) >> 11) * (1.0 / 9007199254740992.0);
+            p[off + i] = (float)((2.0 * u - 1.0) * b);
+        }
+    };
+    fill(MDAS_MLP_OFF_W1, MDAS_MLP_HIDDEN * MDAS_MLP_IN, MDAS_MLP_IN);
+    fill(MDAS_MLP_OFF_B1, MDAS_MLP_HIDDEN, MDAS_MLP_IN);
+    fill(MDAS_MLP_OFF_W2, MDAS_MLP_HIDDEN * MDAS_MLP_HIDDEN, MDAS_MLP_HIDDEN);
+    fill(MDAS_MLP_OFF_B2, MDAS_MLP_HIDDEN, MDAS_MLP_HIDDEN);
+    fill(MDAS_MLP_OFF_W3, MDAS_MLP_HIDDEN, MDAS_MLP_HIDDEN);
+    fill(MDAS_MLP_OFF_B3, 1, MDAS_MLP_HIDDEN);
+}
+
+constexpr size_t kStateFloats = 4 * (size_t)MDAS_MLP_PARAMS + 4;  // params, m1, m2, grads, loss sum, status
+
+int learned_upload(mdas_grid* g, const float* hostParams) {
+    const size_t P = MDAS_MLP_PARAMS;
+    cudaError_t e = cudaMemsetAsync(g->lState, 0, sizeof(float) * kStateFloats, g->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(g->lState, hostParams, sizeof(float) * P, cudaMemcpyHostToDevice, g->stream);
+    if (e == cudaSuccess) e = mdas_mlp::pack(g->lState, g->lPacked, g->stream);
+    g->launches += 1;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    g->lStep = 0;
+    g->lPredVersion = ~0ull;
+    return status_of(e);
+}
+
+}  // namespace
+
+extern "C" {
+
+int mdas_learned_enable(mdas_grid* g, const mdas_learned_config* cfg) {
+    if (!g) return MDAS_ERR_INVALID;
+    if (!cfg) {
+        g->learned = false;
+        g->lPredVersion = ~0ull;
+        return MDAS_OK;
+    }
+    if (cfg->trainSteps < 0 || cfg->batch < 1 || !(cfg->learningRate >= 0.0f) || !(cfg->fallback >= 0.0f) ||
+        cfg->fallback > 1.0f)
+        return MDAS_ERR_INVALID;
+    if (!g->lState) {
+        const bool ok = cudaMalloc(&g->lState, sizeof(float) * kStateFloats) == cudaSuccess &&
+                        cudaMalloc(&g->lPacked, sizeof(mdas_mlp::Packed)) == cudaSuccess &&
+                        cudaMalloc(&g->lPred, sizeof(float) * (size_t)g->dg.maxNodes) == cudaSuccess;
+        if (!ok) return MDAS_ERR_ALLOC;
+    }
+    g->lcfg = *cfg;
+    std::vector<float> p;
+    mlp_init(p, cfg->seed);
+    const int rc = learned_upload(g, p.data());
+    if (rc) return rc;
+    g->dg.priorityScale = MDAS_MLP_TARGET_SCALE;
+    g->dg.fallback1024 = (int)lrintf(cfg->fallback * 1024.0f);
+    g->learned = true;
+    return MDAS_OK;
+}
+
+int mdas_learned_update(mdas_grid* g, float* loss) {
+    if (!g || !g->learned) return MDAS_ERR_INVALID;
+    if (!g->initialized || !g->errorsClean) return MDAS_ERR_STATE;  // needs current leaf errors
+    const size_t P = MDAS_MLP_PARAMS;
+    float* params = g->lState;
+    float* m1 = params + P;
+    float* m2 = m1 + P;
+    float* grads = m2 + P;
+    float* lossSum = grads + P;
+    unsigned* status = reinterpret_cast<unsigned*>(lossSum + 1);
+    const int L = g->L;
+    const int m = g->lcfg.batch < L ? g->lcfg.batch : L;
+    const int stride = L / m > 0 ? L / m : 1;
+    cudaError_t e = cudaMemsetAsync(lossSum, 0, sizeof(float) * 2, g->stream);
+    for (int k = 0; k < g->lcfg.trainSteps && e == cudaSuccess; ++k) {
+        const int step = ++g->lStep;
+        const int offset = (int)(((uint64_t)step * 2654435761ull) % (uint64_t)stride);
+        e = cudaMemsetAsync(lossSum, 0, sizeof(float), g->stream);
+        if (e == cudaSuccess)
+            e = mdas_mlp::gradients(g->lPacked, nullptr, nullptr, &g->dg, L, offset, stride, m, grads, lossSum, status,
+                                    g->stream);
+        if (e == cudaSuccess) e = mdas_mlp::adam(params, m1, m2, grads, step, g->lcfg.learningRate, g->lPacked, g->stream);
+        g->launches += 3;
+    }
+    if (e == cudaSuccess) e = mdas_mlp::predict_leaves(g->dg, L, g->lPacked, g->lPred, status, g->stream);
+    g->launches += 1;
+    float h[2] = {0.0f, 0.0f};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, lossSum, sizeof(h), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    unsigned st;
+    memcpy(&st, &h[1], sizeof(st));
+    if (st) return MDAS_ERR_TIMEOUT;
+    if (loss) *loss = g->lcfg.trainSteps > 0 ? h[0] / (float)m : 0.0f;
+    g->lPredVersion = g->version;
+    return MDAS_OK;
+}
+
+int mdas_learned_get_params(mdas_grid* g, float* params) {
+    if (!g || !g->lState || !params) return MDAS_ERR_INVALID;
+    cudaError_t e = cudaMemcpyAsync(params, g->lState, sizeof(float) * MDAS_MLP_PARAMS, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    return status_of(e);
+}
+
+int mdas_learned_set_params(mdas_grid* g, const float* params) {
+    if (!g || !g->lState || !params) return MDAS_ERR_INVALID;
+    return learned_upload(g, params);
+}
+
+int mdas_learned_predictions(mdas_grid* g, float* pred) {
+    if (!g || !pred) return MDAS_ERR_INVALID;
+    if (!g->learned || g->lPredVersion != g->version) return MDAS_ERR_STATE;
+    cudaError_t e = cudaMemcpyAsync(pred, g->lPred, sizeof(float) * (size_t)g->L, cudaMemcpyDeviceToDevice, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    return status_of(e);
+}
+
+int mdas_leaf_features(mdas_grid* g, float* features) {
+    if (!g || !features) return MDAS_ERR_INVALID;
+    if (!g->initialized) return MDAS_ERR_STATE;
+    cudaError_t e = mdas_mlp::leaf_features(g->dg, g->L, features, g->stream);
+    g->launches += 1;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    return status_of(e);
+}
+
+}  // extern "C"
+
+namespace {
+
+// scratch of the standalone MLP calls: packed weights + status word
+struct MlpScratch {
+    mdas_mlp::Packed* packed = nullptr;
+    unsigned* status = nullptr;
+    float* loss = nullptr;
+    ~MlpScratch() {
+        cudaFree(packed);
+        cudaFree(status);
+    }
+    bool open() {
+        if (cudaMalloc(&packed, sizeof(mdas_mlp::Packed)) != cudaSuccess) return false;
+        if (cudaMalloc(&status, 2 * sizeof(unsigned)) != cudaSuccess) return false;
+        loss = reinterpret_cast<float*>(status + 1);
+        return true;
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+int mdas_mlp_forward(const float* params, const float* features, int m, float* pred, void* stream) {
+    if (!params || m < 0 || (m > 0 && (!features || !pred))) return MDAS_ERR_INVALID;
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    MlpScratch sc;
+    if (!sc.open()) return MDAS_ERR_ALLOC;
+    cudaError_t e = cudaMemsetAsync(sc.status, 0, 2 * sizeof(unsigned), s);
+    if (e == cudaSuccess) e = mdas_mlp::pack(params, sc.packed, s);
+    if (e == cudaSuccess) e = mdas_mlp::forward(sc.packed, features, m, pred, sc.status, s);
+    unsigned st = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, sc.status, sizeof(st), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    return st ? MDAS_ERR_TIMEOUT : MDAS_OK;
+}
+
+int mdas_mlp_gradients(const float* params, const float* features, const float* targets, int m, float* grads,
+                       float* loss, void* stream) {
+    if (!params || !grads || m < 1 || !features || !targets) return MDAS_ERR_INVALID;
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    MlpScratch sc;
+    if (!sc.open()) return MDAS_ERR_ALLOC;
+    cudaError_t e = cudaMemsetAsync(sc.status, 0, 2 * sizeof(unsigned), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(grads, 0, sizeof(float) * MDAS_MLP_PARAMS, s);
+    if (e == cudaSuccess) e = mdas_mlp::pack(params, sc.packed, s);
+    if (e == cudaSuccess)
+        e = mdas_mlp::gradients(sc.packed, features, targets, nullptr, 0, 0, 1, m, grads, sc.loss, sc.status, s);
+    unsigned h[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, sc.status, sizeof(h), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    if (h[0]) return MDAS_ERR_TIMEOUT;
+    float l;
+    memcpy(&l, &h[1], sizeof(l));
+    if (loss) *loss = l / (float)m;
+    return MDAS_OK;
 }
 
 }  // extern "C"

@@ -55,6 +55,12 @@ struct MdasDeviceGrid {
     int* chunkTile;       // [maxNodes/256 + 2] tile of the first entry of each 256-entry chunk of accepted leaves
     int maxTiles;
     int* dirty;           // [maxNodes/2 + 1], slots of the left children of the last pass's splits
+    // learned acceptance (nullptr: the reference's plain error ratio): predicted
+    // log2(error) / priorityScale per leaf; leaves whose hash falls below
+    // fallback1024 / 1024 keep the plain ratio
+    const float* priority;
+    float priorityScale;
+    int fallback1024;
 };
 
 // One image of a batched render (device-side descriptor).

@@ -405,6 +405,15 @@ __device__ __forceinline__ unsigned acc_pack(unsigned local, unsigned splitRank,
     return local | (splitRank << 11) | (split << 22) | (cnt << 23);
 }
 
+// Learned acceptance ratio (no reference counterpart): 2^(predicted log2 error)
+// / g_error, at most 1; a fixed hashed fraction of the leaves keeps the plain
+// error ratio of kdgrid.cu:326.
+__device__ __forceinline__ float learned_ratio(const MdasDeviceGrid& g, int leaf, float err, float gError) {
+    const unsigned h = ((unsigned)leaf * 2654435761u) >> 22;  // 10-bit multiplicative hash
+    if ((int)h < g.fallback1024) return err / gError;
+    return fminf(exp2f(g.priority[leaf] * g.priorityScale - log2f(gError)), 1.0f);
+}
+
 // decide, one tile: acceptance of the tile's leaves, final seeds, the tile's
 // counts and its compacted accepted list (shared by the single-image and the
 // batched kernels).
@@ -446,7 +455,10 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
         unsigned seed = sd[j];
         if (seed == 0) seed = tea4((unsigned)leaf, 0);
         bool a = false;
-        if (leaf < L) a = mdas_pow(err[j] / gError, g.alpha) >= rnd(seed);
+        if (leaf < L) {
+            if (!g.priority) a = mdas_pow(err[j] / gError, g.alpha) >= rnd(seed);
+            else a = mdas_pow(learned_ratio(g, leaf, err[j], gError), g.alpha) >= rnd(seed);
+        }
         seedAcc[j] = seed;
         sd[j] = a ? jumpA * seed + jumpC : seed;  // the seed after the candidate draws
         if (a) accMask |= 1u << j;

@@ -1,0 +1,610 @@
+// mlp.cu — the learned leaf priority on the tcgen05 tensor cores.
+//
+// One CTA of 128 threads works on tiles of 128 rows (leaves).  Per tile:
+//   features (FP32 -> BF16) into a shared-memory A tile;
+//   layer 1: one tcgen05.mma (M 128, N 64, K 16) into 64 TMEM columns;
+//   tcgen05.ld of the accumulators (thread t = row t), + b1, ReLU, BF16 into
+//   the shared-memory A tile of layer 2;
+//   layer 2: four tcgen05.mma (K 64 in steps of 16) into the same columns;
+//   tcgen05.ld, + b2, ReLU, dot with w3 (+ b3) on the CUDA cores.
+// The MMAs are issued by one thread and tracked by an mbarrier
+// (tcgen05.commit); every wait on it is bounded and records a timeout in
+// `status`.  Operands use the no-swizzle K-major layout: 8x8 BF16 core
+// matrices of 128 contiguous bytes, K-blocks of one row group adjacent.
+//
+// Training (gradients) runs the same forward, then on the tensor cores
+// dH1 = dZ2 . W2 (M 128, N 64, K 64, W2 transposed as the K-major B operand),
+// and the weight gradients dW2 = dZ2^T H1, dW1 = dZ1^T X as per-CTA reductions
+// over the tile's 128 rows on the CUDA cores, added to the global gradient
+// with atomics.
+#include "mlp.h"
+
+#include <cuda_bf16.h>
+
+namespace mdas_mlp {
+
+namespace {
+
+constexpr int kRows = 128;
+constexpr int kThreads = 128;
+constexpr int kH = MDAS_MLP_HIDDEN;
+constexpr int kIn = MDAS_MLP_IN;
+constexpr uint32_t kTmemCols = 64;
+constexpr int kWaitLimit = 1 << 20;
+
+// shared-memory map (bytes from the 1024-aligned base)
+constexpr int SM_X = 0;          // 128 x 16 BF16, core matrices, 2 K-blocks per row group
+constexpr int SM_H = 4096;       // 128 x 64 BF16, 8 K-blocks per row group
+constexpr int SM_W1 = 20480;     // 64 x 16 BF16
+constexpr int SM_W2 = 22528;     // 64 x 64 BF16 (B of layer 2: n = output, k = input)
+constexpr int SM_W2T = 30720;    // 64 x 64 BF16 (B of dH1: n = input, k = output)
+constexpr int SM_VEC = 38912;    // b1, b2, w3 (64 floats each), b3
+constexpr int SM_BAR = 39744;    // mbarrier (8 B), TMEM address slot (4 B)
+constexpr int SM_FWD = 39808;    // end of what the forward needs
+// training only
+constexpr int SM_Z2F = 39936;                    // dZ2, FP32 [128][65]
+constexpr int SM_D = SM_Z2F + kRows * 65 * 4;    // dZ2, BF16 core matrices (A of dH1)
+constexpr int SM_Z1F = SM_D + kRows * kH * 2;    // dZ1, FP32 [128][65]
+constexpr int SM_G = SM_Z1F + kRows * 65 * 4;    // per-CTA gradient, FP32 [MDAS_MLP_PARAMS]
+constexpr int SM_TRAIN = SM_G + ((MDAS_MLP_PARAMS * 4 + 127) / 128) * 128;
+constexpr int kFwdSmem = 40960 + 1024;           // also bounds residency: <= 5 CTAs x 64 TMEM columns per SM
+constexpr int kTrainSmem = SM_TRAIN + 1024;
+
+static_assert(SM_W2T + kH * kH * 2 == SM_VEC, "map");
+static_assert(SM_VEC + (3 * kH + 4) * 4 <= SM_BAR, "map");
+static_assert(SM_FWD <= SM_Z2F, "map");
+
+// ---- PTX wrappers ---------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Shared-memory matrix descriptor, K-major without swizzle: start address,
+// leading byte offset (next core matrix along K), stride byte offset (next
+// 8-row group), the fixed constant 0b001 at bits 46-48, swizzle mode 0.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3fffu) | ((uint64_t)((lbo >> 4) & 0x3fffu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3fffu) << 32) | ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A
+// and B (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
+// 17-22, M >> 4 at bits 24-28.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+constexpr uint32_t kIdesc = idesc_bf16(kRows, kH);
+
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// 16 FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+        "[%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// element (r, k) of a BF16 tile with KB K-blocks per row group, in elements
+__host__ __device__ __forceinline__ int core_off(int r, int k, int KB) {
+    return (((r >> 3) * KB + (k >> 3)) << 6) + ((r & 7) << 3) + (k & 7);
+}
+
+__device__ __forceinline__ uint16_t bf16_bits(float x) { return __bfloat16_as_ushort(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ float bf16_val(uint16_t b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
+
+// 8 consecutive K-elements of row r (one core-matrix row, 16 bytes)
+__device__ __forceinline__ void st_row8(uint8_t* tile, int r, int kb, int KB, const float* v) {
+    uint4 q;
+    q.x = (uint32_t)bf16_bits(v[0]) | ((uint32_t)bf16_bits(v[1]) << 16);
+    q.y = (uint32_t)bf16_bits(v[2]) | ((uint32_t)bf16_bits(v[3]) << 16);
+    q.z = (uint32_t)bf16_bits(v[4]) | ((uint32_t)bf16_bits(v[5]) << 16);
+    q.w = (uint32_t)bf16_bits(v[6]) | ((uint32_t)bf16_bits(v[7]) << 16);
+    *reinterpret_cast<uint4*>(tile + 2 * core_off(r, kb * 8, KB)) = q;
+}
+__device__ __forceinline__ void ld_row8(const uint8_t* tile, int r, int kb, int KB, float* v) {
+    const uint4 q = *reinterpret_cast<const uint4*>(tile + 2 * core_off(r, kb * 8, KB));
+    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        v[2 * i] = bf16_val((uint16_t)(w[i] & 0xffffu));
+        v[2 * i + 1] = bf16_val((uint16_t)(w[i] >> 16));
+    }
+}
+
+// ---- per-CTA setup / teardown -------------------------------------------------------
+struct Ctx {
+    uint8_t* sm;
+    uint32_t base, bar, tmem, phase;
+    unsigned* status;
+};
+
+__device__ __forceinline__ uint8_t* aligned_smem() {
+    extern __shared__ uint8_t dyn[];
+    return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dyn) + 1023) & ~(uintptr_t)1023);
+}
+
+__device__ void ctx_open(Ctx& c, const Packed* w, unsigned* status) {
+    c.sm = aligned_smem();
+    c.base = smem_u32(c.sm);
+    c.bar = c.base + SM_BAR;
+    c.phase = 0;
+    c.status = status;
+    // weights: W1, W2, W2^T tiles and the vectors (Packed keeps them contiguous)
+    const uint4* src = reinterpret_cast<const uint4*>(w);
+    uint4* dst = reinterpret_cast<uint4*>(c.sm + SM_W1);
+    constexpr int n16 = (int)(sizeof(Packed) / 16);
+    static_assert(sizeof(Packed) % 16 == 0, "Packed is copied in 16-byte pieces");
+    static_assert(SM_W1 + (int)sizeof(Packed) <= SM_BAR, "Packed fits before the barrier");
+    for (int i = threadIdx.x; i < n16; i += kThreads) dst[i] = src[i];
+    if (threadIdx.x == 0) {
+        mbar_init(c.bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (threadIdx.x < 32) {
+        tmem_alloc(c.base + SM_BAR + 8, kTmemCols);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    c.tmem = *reinterpret_cast<volatile uint32_t*>(c.sm + SM_BAR + 8);
+}
+
+__device__ void ctx_close(Ctx& c) {
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        tc_fence_after();
+        tmem_dealloc(c.tmem, kTmemCols);
+    }
+}
+
+__device__ __forceinline__ void mma_wait(Ctx& c) {
+    bool ok = false;
+    for (int i = 0; i < kWaitLimit && !ok; ++i) ok = mbar_try_wait(c.bar, c.phase);
+    if (!ok) atomicOr(c.status, 1u);
+    c.phase ^= 1u;
+    tc_fence_after();
+}
+
+// this thread's row of the 64 accumulator columns
+__device__ __forceinline__ void tmem_row(const Ctx& c, float (&acc)[kH]) {
+    const uint32_t lane = (threadIdx.x & ~31u) << 16;
+#pragma unroll
+    for (int q = 0; q < kH / 16; ++q) tmem_ld16(c.tmem + lane + 16 * q, acc + 16 * q);
+    tmem_wait_ld();
+}
+
+// Issue `steps` MMAs over K (16 each) of A at aOff (KB K-blocks) x B at bOff, then wait.
+__device__ __forceinline__ void run_mma(Ctx& c, int aOff, int bOff, int KB, int steps) {
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tc_fence_after();
+        const uint32_t sbo = (uint32_t)KB * 128u;
+        for (int s = 0; s < steps; ++s)
+            mma_bf16(c.tmem, smem_desc(c.base + aOff + 256 * s, 128, sbo), smem_desc(c.base + bOff + 256 * s, 128, sbo),
+                     s > 0 ? 1u : 0u);
+        mma_commit(c.bar);
+    }
+    mma_wait(c);
+}
+
+// Forward of the tile whose features this thread wrote as row threadIdx.x of SM_X:
+// z2 = the layer-2 pre-activations (b2 added).
+__device__ void tile_forward(Ctx& c, float (&z2)[kH]) {
+    const float* b1 = reinterpret_cast<const float*>(c.sm + SM_VEC);
+    const float* b2 = b1 + kH;
+    run_mma(c, SM_X, SM_W1, 2, 1);
+    float acc[kH];
+    tmem_row(c, acc);
+#pragma unroll
+    for (int i = 0; i < kH; ++i) acc[i] = fmaxf(acc[i] + b1[i], 0.0f);
+#pragma unroll
+    for (int kb = 0; kb < kH / 8; ++kb) st_row8(c.sm + SM_H, threadIdx.x, kb, 8, acc + 8 * kb);
+    run_mma(c, SM_H, SM_W2, 8, kH / 16);
+    tmem_row(c, z2);
+#pragma unroll
+    for (int i = 0; i < kH; ++i) z2[i] += b2[i];
+}
+
+__device__ __forceinline__ float head(const Ctx& c, const float (&z2)[kH]) {
+    const float* w3 = reinterpret_cast<const float*>(c.sm + SM_VEC) + 2 * kH;
+    float p = w3[kH];  // b3
+#pragma unroll
+    for (int i = 0; i < kH; ++i) p += fmaxf(z2[i], 0.0f) * w3[i];
+    return p;
+}
+
+__device__ __forceinline__ void put_features(const Ctx& c, const float (&f)[kIn]) {
+    st_row8(c.sm + SM_X, threadIdx.x, 0, 2, f);
+    st_row8(c.sm + SM_X, threadIdx.x, 1, 2, f + 8);
+}
+
+// ---- features --------------------------------------------------------------------
+// Per leaf: log2 extents (image axes relative to the image), their mean, the
+// sample count, and log2(1 + x) of the mean and of the mean absolute deviation
+// of the sample values per channel.
+template <int D>
+__device__ void leaf_feats(const MdasDeviceGrid& g, int leaf, float (&f)[kIn], float* err) {
+    const float* nb = g.nb + (size_t)leaf * g.nbFloats;
+    const int4 node = *reinterpret_cast<const int4*>(nb);
+    float depth = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        float l = 0.0f;
+        if (j < D) {
+            float e = nb[4 + D + j] - nb[4 + j];
+            if (j == 0) e /= g.scaleX;
+            if (j == 1) e /= g.scaleY;
+            l = log2f(fmaxf(e, 1e-30f));
+            depth += l;
+        }
+        f[j] = l * (1.0f / 16.0f);
+    }
+    f[6] = depth * (1.0f / (16.0f * D));
+    const int idx[4] = {node.x, node.y, node.z, node.w};
+    float v[4][3];
+    float mean[3] = {0.0f, 0.0f, 0.0f};
+    int n = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (idx[i] >= 0) {
+            const float* p = g.values + 3 * (size_t)idx[i];
+            v[i][0] = __ldg(p);
+            v[i][1] = __ldg(p + 1);
+            v[i][2] = __ldg(p + 2);
+            mean[0] += v[i][0];
+            mean[1] += v[i][1];
+            mean[2] += v[i][2];
+            ++n;
+        }
+    }
+    const float inv = n ? 1.0f / (float)n : 0.0f;
+    float dev[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) mean[c] *= inv;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        if (idx[i] >= 0)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) dev[c] += fabsf(v[i][c] - mean[c]);
+    f[7] = (float)n * 0.25f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        f[8 + c] = log2f(1.0f + fabsf(mean[c]));
+        f[11 + c] = log2f(1.0f + dev[c] * inv);
+    }
+    f[14] = 0.0f;
+    f[15] = 0.0f;
+    if (err) *err = g.errors[leaf];
+}
+
+__device__ __forceinline__ float target_of(float err) {
+    return log2f(fmaxf(err, 1e-30f)) * (1.0f / MDAS_MLP_TARGET_SCALE);
+}
+
+// ---- kernels ---------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_forward_rows(const Packed* __restrict__ w, const float* __restrict__ feats,
+                                                           int m, float* __restrict__ pred, unsigned* status) {
+    Ctx c;
+    ctx_open(c, w, status);
+    const int tiles = (m + kRows - 1) / kRows;
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int r = tile * kRows + threadIdx.x;
+        float f[kIn];
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) f[i] = r < m ? feats[(size_t)r * kIn + i] : 0.0f;
+        put_features(c, f);
+        float z2[kH];
+        tile_forward(c, z2);
+        const float p = head(c, z2);
+        if (r < m) pred[r] = p;
+    }
+    ctx_close(c);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_predict_leaves(MdasDeviceGrid g, int L, const Packed* __restrict__ w,
+                                                             float* __restrict__ pred, unsigned* status) {
+    Ctx c;
+    ctx_open(c, w, status);
+    const int tiles = (L + kRows - 1) / kRows;
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int r = tile * kRows + threadIdx.x;
+        float f[kIn];
+        if (r < L) leaf_feats<D>(g, r, f, nullptr);
+        else
+#pragma unroll
+            for (int i = 0; i < kIn; ++i) f[i] = 0.0f;
+        put_features(c, f);
+        float z2[kH];
+        tile_forward(c, z2);
+        const float p = head(c, z2);
+        if (r < L) pred[r] = p;
+    }
+    ctx_close(c);
+}
+
+template <int D>
+__global__ void k_leaf_features(MdasDeviceGrid g, int L, float* __restrict__ out) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < L; r += gridDim.x * blockDim.x) {
+        float f[kIn];
+        leaf_feats<D>(g, r, f, nullptr);
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) out[(size_t)r * kIn + i] = f[i];
+    }
+}
+
+// One CTA per tile of 128 rows: forward, backward, per-CTA gradient, atomics.
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_gradients(const Packed* __restrict__ w, const float* __restrict__ feats,
+                                                        const float* __restrict__ targets, MdasDeviceGrid g, int L,
+                                                        int offset, int stride, int m, float* __restrict__ grads,
+                                                        float* __restrict__ lossSum, unsigned* status) {
+    Ctx c;
+    ctx_open(c, w, status);
+    float* sg = reinterpret_cast<float*>(c.sm + SM_G);
+    for (int i = threadIdx.x; i < MDAS_MLP_PARAMS; i += kThreads) sg[i] = 0.0f;
+    const float* vec = reinterpret_cast<const float*>(c.sm + SM_VEC);
+    const float* w3 = vec + 2 * kH;
+    float* z2f = reinterpret_cast<float*>(c.sm + SM_Z2F);
+    float* z1f = reinterpret_cast<float*>(c.sm + SM_Z1F);
+    const int t = threadIdx.x;
+    const int r = blockIdx.x * kRows + t;
+    const bool valid = r < m;
+    float f[kIn];
+    float y = 0.0f;
+    if (!valid) {
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) f[i] = 0.0f;
+    } else if (feats) {
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) f[i] = feats[(size_t)r * kIn + i];
+        y = targets[r];
+    } else {
+        const int leaf = (int)(((long long)offset + (long long)r * stride) % L);
+        float err;
+        leaf_feats<D>(g, leaf, f, &err);
+        y = target_of(err);
+    }
+    put_features(c, f);
+    float z2[kH];
+    tile_forward(c, z2);
+    const float e = valid ? head(c, z2) - y : 0.0f;
+    const float dpred = 2.0f * e / (float)m;
+    __syncthreads();  // sg zeroed
+    float dz[kH];
+#pragma unroll
+    for (int j = 0; j < kH; ++j) {
+        const float h2 = fmaxf(z2[j], 0.0f);
+        dz[j] = z2[j] > 0.0f ? dpred * w3[j] : 0.0f;
+        if (valid) {
+            atomicAdd(&sg[MDAS_MLP_OFF_W3 + j], dpred * h2);
+            atomicAdd(&sg[MDAS_MLP_OFF_B2 + j], dz[j]);
+        }
+        z2f[t * 65 + j] = dz[j];
+    }
+    if (valid) atomicAdd(&sg[MDAS_MLP_OFF_B3], dpred);
+#pragma unroll
+    for (int kb = 0; kb < kH / 8; ++kb) st_row8(c.sm + SM_D, t, kb, 8, dz + 8 * kb);
+    // dH1 = dZ2 . W2 on the tensor cores (B = W2 transposed, K-major)
+    run_mma(c, SM_D, SM_W2T, 8, kH / 16);
+    float dh[kH];
+    tmem_row(c, dh);
+#pragma unroll
+    for (int kb = 0; kb < kH / 8; ++kb) {
+        float h[8];
+        ld_row8(c.sm + SM_H, t, kb, 8, h);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int i = 8 * kb + q;
+            const float d1 = h[q] > 0.0f ? dh[i] : 0.0f;
+            z1f[t * 65 + i] = d1;
+            if (valid) atomicAdd(&sg[MDAS_MLP_OFF_B1 + i], d1);
+        }
+    }
+    __syncthreads();
+    // dW2[j][i] = sum_r dZ2[r][j] H1[r][i]: thread t owns j = t / 2, i in [32 (t % 2), +32)
+    {
+        const int j = t >> 1, i0 = (t & 1) * 32;
+        float acc[32];
+#pragma unroll
+        for (int q = 0; q < 32; ++q) acc[q] = 0.0f;
+        for (int row = 0; row < kRows; ++row) {
+            const float d = z2f[row * 65 + j];
+#pragma unroll
+            for (int kb = 0; kb < 4; ++kb) {
+                float h[8];
+                ld_row8(c.sm + SM_H, row, i0 / 8 + kb, 8, h);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) acc[8 * kb + q] += d * h[q];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 32; ++q) sg[MDAS_MLP_OFF_W2 + j * kH + i0 + q] += acc[q];
+    }
+    // dW1[i][k] = sum_r dZ1[r][i] X[r][k]: thread t owns i = t / 2, k in [8 (t % 2), +8)
+    {
+        const int i = t >> 1, kb = t & 1;
+        float acc[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc[q] = 0.0f;
+        for (int row = 0; row < kRows; ++row) {
+            const float d = z1f[row * 65 + i];
+            float x[8];
+            ld_row8(c.sm + SM_X, row, kb, 2, x);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) acc[q] += d * x[q];
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) sg[MDAS_MLP_OFF_W1 + i * kIn + 8 * kb + q] += acc[q];
+    }
+    // loss
+    float l = e * e;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+    if ((t & 31) == 0) atomicAdd(lossSum, l);
+    __syncthreads();
+    for (int i = t; i < MDAS_MLP_PARAMS; i += kThreads) {
+        const float v = sg[i];
+        if (v != 0.0f) atomicAdd(&grads[i], v);
+    }
+    ctx_close(c);
+}
+
+__global__ void k_pack(const float* __restrict__ p, Packed* __restrict__ out) {
+    for (int idx = threadIdx.x; idx < kH * kH; idx += blockDim.x) {
+        const int j = idx / kH, i = idx % kH;  // W2[j][i]: output j, input i
+        const uint16_t b = bf16_bits(p[MDAS_MLP_OFF_W2 + idx]);
+        out->w2[core_off(j, i, 8)] = b;
+        out->w2t[core_off(i, j, 8)] = b;
+        if (idx < kH * kIn) out->w1[core_off(idx / kIn, idx % kIn, 2)] = bf16_bits(p[MDAS_MLP_OFF_W1 + idx]);
+        if (idx < kH) {
+            out->b1[idx] = p[MDAS_MLP_OFF_B1 + idx];
+            out->b2[idx] = p[MDAS_MLP_OFF_B2 + idx];
+            out->w3[idx] = p[MDAS_MLP_OFF_W3 + idx];
+        }
+        if (idx < 4) out->b3[idx] = idx == 0 ? p[MDAS_MLP_OFF_B3] : 0.0f;
+    }
+}
+
+__global__ void k_adam(float* __restrict__ p, float* __restrict__ m1, float* __restrict__ m2, float* __restrict__ g,
+                       int step, float lr) {
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < MDAS_MLP_PARAMS; i += gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float a = b1 * m1[i] + (1.0f - b1) * gi;
+        const float b = b2 * m2[i] + (1.0f - b2) * gi * gi;
+        m1[i] = a;
+        m2[i] = b;
+        p[i] -= lr * (a / c1) / (sqrtf(b / c2) + eps);
+        g[i] = 0.0f;
+    }
+}
+
+int sm_count() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+template <class K>
+cudaError_t set_smem(K kernel, int bytes) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+#define MLP_SWITCH_D(D, CALL)                           \
+    switch (D) {                                        \
+        case 3: { constexpr int DD = 3; CALL; } break;  \
+        case 4: { constexpr int DD = 4; CALL; } break;  \
+        case 5: { constexpr int DD = 5; CALL; } break;  \
+        case 6: { constexpr int DD = 6; CALL; } break;  \
+        default: return cudaErrorInvalidValue;          \
+    }
+
+}  // namespace
+
+cudaError_t pack(const float* params, Packed* packed, cudaStream_t s) {
+    k_pack<<<1, 1024, 0, s>>>(params, packed);
+    return cudaGetLastError();
+}
+
+cudaError_t forward(const Packed* w, const float* features, int m, float* pred, unsigned* status, cudaStream_t s) {
+    if (m <= 0) return cudaSuccess;
+    cudaError_t e = set_smem(k_forward_rows, kFwdSmem);
+    if (e != cudaSuccess) return e;
+    const int tiles = (m + kRows - 1) / kRows;
+    const int grid = tiles < sm_count() * 4 ? tiles : sm_count() * 4;
+    k_forward_rows<<<grid, kThreads, kFwdSmem, s>>>(w, features, m, pred, status);
+    return cudaGetLastError();
+}
+
+cudaError_t predict_leaves(const MdasDeviceGrid& g, int L, const Packed* w, float* pred, unsigned* status,
+                           cudaStream_t s) {
+    if (L <= 0) return cudaSuccess;
+    const int tiles = (L + kRows - 1) / kRows;
+    const int grid = tiles < sm_count() * 4 ? tiles : sm_count() * 4;
+    cudaError_t e = cudaSuccess;
+    MLP_SWITCH_D(g.D, (e = set_smem(k_predict_leaves<DD>, kFwdSmem),
+                       e == cudaSuccess ? (k_predict_leaves<DD><<<grid, kThreads, kFwdSmem, s>>>(g, L, w, pred, status),
+                                           0)
+                                        : 0));
+    return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+cudaError_t leaf_features(const MdasDeviceGrid& g, int L, float* features, cudaStream_t s) {
+    if (L <= 0) return cudaSuccess;
+    const int grid = (L + 255) / 256 < 4096 ? (L + 255) / 256 : 4096;
+    MLP_SWITCH_D(g.D, (k_leaf_features<DD><<<grid, 256, 0, s>>>(g, L, features)));
+    return cudaGetLastError();
+}
+
+cudaError_t gradients(const Packed* w, const float* features, const float* targets, const MdasDeviceGrid* g, int L,
+                      int offset, int stride, int m, float* grads, float* lossSum, unsigned* status, cudaStream_t s) {
+    if (m <= 0) return cudaSuccess;
+    if (!features && (!g || L <= 0)) return cudaErrorInvalidValue;
+    const int tiles = (m + kRows - 1) / kRows;
+    MdasDeviceGrid none{};
+    none.D = 4;
+    const MdasDeviceGrid& gg = g ? *g : none;
+    cudaError_t e = cudaSuccess;
+    MLP_SWITCH_D(gg.D, (e = set_smem(k_gradients<DD>, kTrainSmem),
+                        e == cudaSuccess ? (k_gradients<DD><<<tiles, kThreads, kTrainSmem, s>>>(
+                                                w, features, targets, gg, L, offset, stride, m, grads, lossSum, status),
+                                            0)
+                                         : 0));
+    return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+cudaError_t adam(float* params, float* m1, float* m2, float* grads, int step, float lr, Packed* packed,
+                 cudaStream_t s) {
+    k_adam<<<(MDAS_MLP_PARAMS + 255) / 256, 256, 0, s>>>(params, m1, m2, grads, step, lr);
+    k_pack<<<1, 1024, 0, s>>>(params, packed);
+    return cudaGetLastError();
+}
+
+}  // namespace mdas_mlp

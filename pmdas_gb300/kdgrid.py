@@ -249,6 +249,68 @@ class KDGrid:
         N.check(self._lib.mdas_locate(self._h, _ptr(pts), int(pts.shape[0]), _ptr(out)), "locate")
         return out[:pts.shape[0]]
 
+    # ---- learned acceptance (no reference counterpart)
+    def LearnedEnable(self, on: bool = True, **cfg):
+        """Learned mode on (fresh weights; keys: trainSteps, batch, learningRate, fallback, seed) or off."""
+        if not on:
+            N.check(self._lib.mdas_learned_enable(self._h, None), "learned_enable")
+            return
+        c = N.LearnedConfig()
+        N.check(self._lib.mdas_learned_defaults(C.byref(c)), "learned_defaults")
+        for k, v in cfg.items():
+            setattr(c, k, v)
+        N.check(self._lib.mdas_learned_enable(self._h, C.byref(c)), "learned_enable")
+
+    def LearnedUpdate(self) -> float:
+        loss = C.c_float()
+        N.check(self._lib.mdas_learned_update(self._h, C.byref(loss)), "learned_update")
+        return loss.value
+
+    def LearnedParams(self) -> np.ndarray:
+        p = np.empty(N.MLP_PARAMS, np.float32)
+        N.check(self._lib.mdas_learned_get_params(self._h, _ptr(p)), "learned_get_params")
+        return p
+
+    def SetLearnedParams(self, p: np.ndarray):
+        q = np.ascontiguousarray(p, np.float32)
+        assert q.size == N.MLP_PARAMS
+        N.check(self._lib.mdas_learned_set_params(self._h, _ptr(q)), "learned_set_params")
+
+    def LearnedPredictions(self):
+        import torch
+        n = self.GetNumberOfNodes()
+        out = torch.empty(max(n, 1), dtype=torch.float32, device="cuda")
+        N.check(self._lib.mdas_learned_predictions(self._h, _ptr(out)), "learned_predictions")
+        return out[:n]
+
+    def LeafFeatures(self):
+        import torch
+        n = self.GetNumberOfNodes()
+        out = torch.empty((max(n, 1), 16), dtype=torch.float32, device="cuda")
+        N.check(self._lib.mdas_leaf_features(self._h, _ptr(out)), "leaf_features")
+        return out[:n]
+
+
+def mlp_forward(params, features):
+    """pred [m] of the MLP (params: torch CUDA float32 [MDAS_MLP_PARAMS], features [m, 16])."""
+    import torch
+    p, f = params.contiguous(), features.contiguous()
+    m = f.shape[0]
+    out = torch.empty(max(m, 1), dtype=torch.float32, device="cuda")
+    N.check(N.load().mdas_mlp_forward(_ptr(p), _ptr(f), m, _ptr(out), None), "mlp_forward")
+    return out[:m]
+
+
+def mlp_gradients(params, features, targets):
+    """(grads [MDAS_MLP_PARAMS], loss) of mean((pred - targets)^2)."""
+    import torch
+    p, f, t = params.contiguous(), features.contiguous(), targets.contiguous()
+    g = torch.empty(N.MLP_PARAMS, dtype=torch.float32, device="cuda")
+    loss = C.c_float()
+    N.check(N.load().mdas_mlp_gradients(_ptr(p), _ptr(f), _ptr(t), f.shape[0], _ptr(g), C.byref(loss), None),
+            "mlp_gradients")
+    return g, loss.value
+
 
 def morton_key_bits(dim: int, bitsPerDim: int, extraImgBits: int, fineBits: int) -> int:
     return N.load().mdas_morton_key_bits(dim, bitsPerDim, extraImgBits, fineBits)
