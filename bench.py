@@ -51,6 +51,7 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-quality", action="store_true")
     ap.add_argument("--no-order", action="store_true", help="skip the leaf-order / hierarchy / locate timings")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-acceptance render")
     return ap.parse_args()
 
 
@@ -108,20 +109,21 @@ class ClockSampler:
 def stage_bytes(D: int, W: int, H: int, L0: int, passes: list, N_final: int, L_final: int) -> dict:
     """Algorithmic (compulsory) DRAM bytes of each stage over one render.
 
-    init     : per initial leaf 4 samples * D floats + node 16 + box 8D + error 4 + seed 4 = 24D + 24
+    init     : per initial leaf 4 samples * D floats + node 16 + box 8D + error 4 + seed 4 + sample count 1
+               = 24D + 25
     errors   : first pass (every leaf): error read 4 per leaf; later passes visit only the split
                children: dirty-list entry 4 per split + error read 4 per child; per recomputed
                leaf error write 4 + node 16 + box 8D + its sample values (12 B each; 4 per leaf
                on the first pass, 5 per split pair after)
-    adaptive : error + seed read and seed write, 12 per leaf; per accepted leaf: its node 16
-               (decide), its entry in the accepted list written and read 16, node + box
-               16 + 8D, new coordinate 4D, 4D per sample coordinate it holds (its private
-               copy); per append: node 16 + the new coordinate in the private copy 4D;
-               per split: left node 16 + left mx 4 + left copy 8D + right node + box
-               16 + 8D + right copy 12D + two errors 8 + right seed 4 + dirty entry 4
+    adaptive : error + seed read, seed write, sample count read: 13 per leaf; per accepted leaf:
+               its entry in the accepted list written and read 16, node + box 16 + 8D, new
+               coordinate 4D, 4D per sample coordinate it holds (its private copy); per append:
+               node 16 + the new coordinate in the private copy 4D + count 1; per split: left
+               node 16 + left mx 4 + left copy 8D + right node + box 16 + 8D + right copy 12D +
+               two errors 8 + right seed 4 + dirty entry 4 + two counts 2
     integrate: per leaf node 16 + box 8D, 12 per sample value, pixels cleared and written 32 per pixel
     """
-    init = L0 * (24 * D + 24)
+    init = L0 * (24 * D + 25)
     err = adap = 0
     for k, p in enumerate(passes):
         L, R = p["L"], p["recomputed"]
@@ -129,7 +131,7 @@ def stage_bytes(D: int, W: int, H: int, L0: int, passes: list, N_final: int, L_f
         scan = 4 * L if k == 0 else 4 * R + 2 * R
         err += scan + R * (4 + 16 + 8 * D) + 12 * V
         S, P, G = p["selected"], p["splits"], p["gathered"]
-        adap += 12 * L + S * (48 + 12 * D) + 4 * D * G + (S - P) * (16 + 4 * D) + P * (52 + 28 * D)
+        adap += 13 * L + S * (32 + 12 * D) + 4 * D * G + (S - P) * (17 + 4 * D) + P * (54 + 28 * D)
     integ = L_final * (16 + 8 * D) + 12 * N_final + 32 * W * H
     return {"init": init, "errors": err, "adaptive": adap, "integrate": integ}
 
@@ -260,6 +262,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     # quality: rel-MSE (parse_logs.py:48-50) of the last render against a 4096-spp
     # reference image of the same integrand accumulated in FP64
     quality = None
+    ref = None
     if not args.no_quality:
         img = pixels[..., :3].double()
         t0 = time.perf_counter()
@@ -301,6 +304,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
                "ms_per_step": round(e2e_s * 1e3, 3), "includes": "integrand, host syncs per pass, copies"}
 
     order = None if args.no_order else order_block(grid, wl, peak)
+    learned = None if args.no_learned or world > 1 else learned_block(wl, scene, ref, peaks)
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -325,6 +329,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         "e2e": e2e,
         "quality": quality,
         "leaf_order": order,
+        "learned": learned,
         "gpu_launches": int(launches),
         "clocks": clk,
     }
@@ -377,6 +382,79 @@ def order_block(grid, wl, peak: float, reps: int = 5) -> dict:
                               "passes": passes, "note": "whole sort (histogram + passes) incl. launch gaps"},
             "locate_points": int(pts.shape[0]), "locate_ms": round(loc_ms, 4),
             "locate_mpoints_per_s": round(pts.shape[0] / (loc_ms / 1e3) / 1e6, 1)}
+
+
+def learned_block(wl, scene, ref, peaks: dict, reps: int = 5) -> dict:
+    """The same render in learned mode (MLP acceptance, trained every pass) next
+    to the plain host loop: time, quality, loss, and the tensor-core predict
+    kernel's throughput against both rooflines."""
+    import torch
+
+    import pmdas_gb300 as P
+
+    W, H = wl.width, wl.height
+
+    def host_loop(learned: bool):
+        g = P.KDGrid(wl.dim, wl.maxSamples, wl.candidatesNum, wl.bitsPerDim, wl.extraImgBits, wl.alpha, wl.scaleX,
+                     wl.scaleY)
+        if learned:
+            g.LearnedEnable()
+        px = torch.zeros(H, W, 4, device="cuda")
+        losses = []
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        g.InitialSampling()
+        scene.evaluate(g, 0, g.GetNumberOfSamples())
+        while True:
+            n, _, l, _ = g._counts()
+            if n >= wl.budget or n + l > wl.maxSamples:
+                break
+            g.ComputeErrors()
+            if learned:
+                losses.append(g.LearnedUpdate())
+            g.AdaptiveSampling()
+            n2, nn, _, _ = g._counts()
+            scene.evaluate(g, n2 - nn, nn)
+        g.Integrate(px, W, H)
+        b.record()
+        torch.cuda.synchronize()
+        img = px[..., :3].double()
+        rel = float(torch.nan_to_num((ref - img) ** 2 / (ref ** 2 + 1e-2), nan=0.0).mean().item()) if ref is not None \
+            else None
+        return g, a.elapsed_time(b), rel, losses
+
+    host_loop(True)  # warm
+    g, learned_ms, learned_rel, losses = host_loop(True)
+    _, plain_ms, plain_rel, _ = host_loop(False)
+    L = g.GetNumberOfNodes()
+    ts = []
+    for _ in range(reps + 1):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        g.LearnedPredict()
+        b.record()
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    pred_ms = statistics.median(ts[1:])
+    flops = L * 2.0 * (16 * 64 + 64 * 64)  # tensor-core MACs x 2 (the 64-wide head runs on the CUDA cores)
+    nbf = (4 + 2 * wl.dim + 3) // 4 * 4
+    bytes_ = L * (nbf * 4 + 4 * 12 + 4)  # node + box record, 4 sample values, prediction
+    tf = flops / (pred_ms / 1e3) / 1e12
+    gbs = bytes_ / (pred_ms / 1e3) / 1e9
+    pk_tf = float(peaks.get("bf16_tflops", 1900.0))
+    pk_bw = float(peaks.get("hbm_gbs", 6800.0))
+    return {"config": "defaults: 4 Adam steps x 16384 leaves per pass, lr 2e-3, 5% plain-error fallback",
+            "render_ms": round(learned_ms, 3), "plain_host_loop_render_ms": round(plain_ms, 3),
+            "samples": g.GetNumberOfSamples(), "passes": len(losses),
+            "rel_mse": learned_rel, "plain_rel_mse": plain_rel,
+            "loss_first_last": [round(losses[0], 6), round(losses[-1], 6)] if losses else None,
+            "predict": {"leaves": L, "ms": round(pred_ms, 4), "gleaves_per_s": round(L / (pred_ms / 1e3) / 1e9, 3),
+                        "tensor": {"achieved": round(tf, 2), "peak": pk_tf, "unit": "TFLOP/s",
+                                   "frac": round(tf / pk_tf, 4)},
+                        "hbm": {"achieved": round(gbs, 1), "peak": pk_bw, "unit": "GB/s", "frac": round(gbs / pk_bw, 4)},
+                        "bound": "hbm (features: node + box + 4 gathered values per leaf)"}}
 
 
 def run_batch(args, rank: int, world: int, local_rank: int) -> dict:

@@ -356,6 +356,9 @@ int mdas_learned_enable(mdas_grid* g, const mdas_learned_config* cfg);
  * and predicts every leaf; *loss (host, optional) = the last step's mean
  * squared error.  mdas_sampling_pass calls it between its two halves. */
 int mdas_learned_update(mdas_grid* g, float* loss);
+/* Predicts every leaf with the current weights, without training (frozen or
+ * loaded weights: the next adaptive pass uses these predictions). */
+int mdas_learned_predict(mdas_grid* g);
 /* Host copies of the FP32 parameters (MDAS_MLP_PARAMS floats). */
 int mdas_learned_get_params(mdas_grid* g, float* params);
 int mdas_learned_set_params(mdas_grid* g, const float* params);

@@ -119,6 +119,7 @@ SIGNATURES = {
     "mdas_learned_defaults": (_I, [C.POINTER(LearnedConfig)]),
     "mdas_learned_enable": (_I, [_P, C.POINTER(LearnedConfig)]),
     "mdas_learned_update": (_I, [_P, C.POINTER(_F)]),
+    "mdas_learned_predict": (_I, [_P]),
     "mdas_learned_get_params": (_I, [_P, _P]),
     "mdas_learned_set_params": (_I, [_P, _P]),
     "mdas_learned_predictions": (_I, [_P, _P]),

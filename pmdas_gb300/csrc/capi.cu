@@ -210,6 +210,7 @@ void free_grid(mdas_grid* g) {
     cudaFree(g->dg.nb);
     cudaFree(g->dg.lsc);
     cudaFree(g->dg.errors);
+    cudaFree(g->dg.leafCounts);
     cudaFree(g->dg.seeds);
     cudaFree(g->dg.counts);
     cudaFree(g->dg.ctl);
@@ -308,6 +309,7 @@ int mdas_create_ex(mdas_grid** out, int dim, int maxSamples, int candidatesNum, 
               cudaMalloc(&d.nb, sizeof(float) * (size_t)d.nbFloats * (size_t)d.maxNodes) == cudaSuccess &&
               cudaMalloc(&d.lsc, sizeof(float) * 4 * dim * (size_t)d.maxNodes) == cudaSuccess &&
               cudaMalloc(&d.errors, sizeof(float) * (size_t)d.maxNodes) == cudaSuccess &&
+              cudaMalloc(&d.leafCounts, (size_t)d.maxNodes + 16) == cudaSuccess &&
               cudaMalloc(&d.seeds, sizeof(unsigned) * (size_t)d.maxNodes) == cudaSuccess &&
               cudaMalloc(&d.counts, sizeof(MdasCounts)) == cudaSuccess &&
               cudaMalloc(&d.ctl, sizeof(MdasCtl)) == cudaSuccess &&
@@ -1539,6 +1541,22 @@ int mdas_learned_update(mdas_grid* g, float* loss) {
     memcpy(&st, &h[1], sizeof(st));
     if (st) return MDAS_ERR_TIMEOUT;
     if (loss) *loss = g->lcfg.trainSteps > 0 ? h[0] / (float)m : 0.0f;
+    g->lPredVersion = g->version;
+    return MDAS_OK;
+}
+
+int mdas_learned_predict(mdas_grid* g) {
+    if (!g || !g->learned) return MDAS_ERR_INVALID;
+    if (!g->initialized) return MDAS_ERR_STATE;
+    unsigned* status = reinterpret_cast<unsigned*>(g->lState + 4 * (size_t)MDAS_MLP_PARAMS + 1);
+    cudaError_t e = cudaMemsetAsync(status, 0, sizeof(unsigned), g->stream);
+    if (e == cudaSuccess) e = mdas_mlp::predict_leaves(g->dg, g->L, g->lPacked, g->lPred, status, g->stream);
+    g->launches += 1;
+    unsigned st = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, status, sizeof(st), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    if (st) return MDAS_ERR_TIMEOUT;
     g->lPredVersion = g->version;
     return MDAS_OK;
 }

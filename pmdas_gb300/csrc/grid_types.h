@@ -46,6 +46,7 @@ struct MdasDeviceGrid {
     int nbFloats;         // floats per node + box record
     float* lsc;           // [maxNodes * 4D], per leaf: coordinates of its samples in node-slot order
     float* errors;        // [maxNodes], < 0 = needs recomputation
+    unsigned char* leafCounts;  // [maxNodes + 16], samples per leaf (the node's non-empty slots)
     unsigned* seeds;      // [maxNodes], 0 = not drawn yet
     MdasCounts* counts;   // device counters
     MdasCtl* ctl;         // per-pass scratch

@@ -235,6 +235,7 @@ __device__ __forceinline__ void init_chunk(const MdasDeviceGrid& g, int L, int b
         }
         g.seeds[nodeIndex] = seed;
         g.errors[nodeIndex] = -1.0f;
+        g.leafCounts[nodeIndex] = 4;
         const int s0 = 4 * nodeIndex;
         float mx[D];
 #pragma unroll
@@ -429,9 +430,12 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
     const int warp = threadIdx.x >> 5;
     const int i0 = tile * TILE + threadIdx.x * K;
     const bool full = i0 + K <= L;
+    static_assert(K == 8, "the sample counts of a thread's leaves are one 8-byte load");
     float err[K];
     unsigned sd[K];
+    int lc[K];
     if (full) {
+        const uint2 c8 = *reinterpret_cast<const uint2*>(g.leafCounts + i0);
 #pragma unroll
         for (int q = 0; q < K; q += 4) {
             const float4 e4 = *reinterpret_cast<const float4*>(g.errors + i0 + q);
@@ -439,12 +443,18 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
             err[q] = e4.x; err[q + 1] = e4.y; err[q + 2] = e4.z; err[q + 3] = e4.w;
             sd[q] = s4.x; sd[q + 1] = s4.y; sd[q + 2] = s4.z; sd[q + 3] = s4.w;
         }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            lc[j] = (int)((c8.x >> (8 * j)) & 0xffu);
+            lc[4 + j] = (int)((c8.y >> (8 * j)) & 0xffu);
+        }
     } else {
 #pragma unroll
         for (int j = 0; j < K; ++j) {
             const bool v = i0 + j < L;
             err[j] = v ? g.errors[i0 + j] : 0.0f;
             sd[j] = v ? g.seeds[i0 + j] : 0u;
+            lc[j] = v ? (int)g.leafCounts[i0 + j] : 0;
         }
     }
     unsigned accMask = 0;
@@ -465,7 +475,7 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
     }
     int cnt[K];
 #pragma unroll
-    for (int j = 0; j < K; ++j) cnt[j] = ((accMask >> j) & 1u) ? node_count(nb_node(g.nb + (size_t)(i0 + j) * NB)) : 0;
+    for (int j = 0; j < K; ++j) cnt[j] = ((accMask >> j) & 1u) ? lc[j] : 0;
     unsigned splitMask = 0;
 #pragma unroll
     for (int j = 0; j < K; ++j) {
@@ -680,6 +690,7 @@ __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, i
         else node.w = sampleIndex;
         nb_set_node(nb, node);
         store_point<D>(sc + sampleCount * D, best);
+        g.leafCounts[nodeIndex] = (unsigned char)(sampleCount + 1);
     } else {
         // split dimension: AABB::LargestAxis, ties to the highest index (aabb.h:34-45)
         int axis = -1;
@@ -751,6 +762,8 @@ __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, i
         }
         g.errors[nodeIndex] = -1.0f;
         g.errors[nodeOffset] = -1.0f;
+        g.leafCounts[nodeIndex] = 2;
+        g.leafCounts[nodeOffset] = 3;
         // a new slot starts without a seed: the reference's seed buffer is zeroed
         // once at InitialSampling (kdgrid.cu:637) and right-child slots are never
         // written before; writing the 0 here makes that memset unnecessary
@@ -935,11 +948,13 @@ __global__ void k_unpack_records(const float* __restrict__ nb, int L, int4* __re
 }
 
 template <int D>
-__global__ void k_pack_records(float* __restrict__ nb, float* __restrict__ lsc, int L, const int4* __restrict__ nodes,
-                               const float* __restrict__ boxes, const float* __restrict__ coords) {
+__global__ void k_pack_records(float* __restrict__ nb, float* __restrict__ lsc, unsigned char* __restrict__ counts,
+                               int L, const int4* __restrict__ nodes, const float* __restrict__ boxes,
+                               const float* __restrict__ coords) {
     constexpr int NB = NbLayout<D>::FLOATS;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
         const int4 n = nodes[i];
+        counts[i] = (unsigned char)node_count(n);
         float mn[D], mx[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) {
@@ -1067,8 +1082,8 @@ cudaError_t unpack_records(const MdasDeviceGrid& g, int L, int* nodes, float* bo
 cudaError_t pack_records(const MdasDeviceGrid& g, int L, const int* nodes, const float* boxes, cudaStream_t s) {
     if (L == 0) return cudaSuccess;
     const int grid = (L + 255) / 256 < 4096 ? (L + 255) / 256 : 4096;
-    MDAS_SWITCH_D(g.D, (k_pack_records<DD><<<grid, 256, 0, s>>>(g.nb, g.lsc, L, reinterpret_cast<const int4*>(nodes),
-                                                               boxes, g.coords)));
+    MDAS_SWITCH_D(g.D, (k_pack_records<DD><<<grid, 256, 0, s>>>(g.nb, g.lsc, g.leafCounts, L,
+                                                               reinterpret_cast<const int4*>(nodes), boxes, g.coords)));
     return cudaGetLastError();
 }
 

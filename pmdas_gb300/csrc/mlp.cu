@@ -46,7 +46,8 @@ constexpr int SM_Z2F = 39936;                    // dZ2, FP32 [128][65]
 constexpr int SM_D = SM_Z2F + kRows * 65 * 4;    // dZ2, BF16 core matrices (A of dH1)
 constexpr int SM_Z1F = SM_D + kRows * kH * 2;    // dZ1, FP32 [128][65]
 constexpr int SM_G = SM_Z1F + kRows * 65 * 4;    // per-CTA gradient, FP32 [MDAS_MLP_PARAMS]
-constexpr int SM_TRAIN = SM_G + ((MDAS_MLP_PARAMS * 4 + 127) / 128) * 128;
+constexpr int SM_RED = SM_G + ((MDAS_MLP_PARAMS * 4 + 127) / 128) * 128;  // [3][4 warps][64] partial sums
+constexpr int SM_TRAIN = SM_RED + 3 * 4 * kH * 4;
 constexpr int kFwdSmem = 40960 + 1024;           // also bounds residency: <= 5 CTAs x 64 TMEM columns per SM
 constexpr int kTrainSmem = SM_TRAIN + 1024;
 
@@ -149,6 +150,24 @@ __device__ __forceinline__ void ld_row8(const uint8_t* tile, int r, int kb, int 
         v[2 * i] = bf16_val((uint16_t)(w[i] & 0xffffu));
         v[2 * i + 1] = bf16_val((uint16_t)(w[i] >> 16));
     }
+}
+
+// Sum of v[64] over the warp's lanes, stored to out[64]: a reduce-scatter by
+// halving (62 shuffles); lane l ends with the sums of elements 2l and 2l + 1.
+__device__ __forceinline__ void warp_sum64(float (&v)[kH], float* out) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int off = 16, n = 32; off >= 1; off >>= 1, n >>= 1) {
+        const bool upper = (lane & off) != 0;
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+            const float send = upper ? v[i] : v[i + n];
+            const float keep = upper ? v[i + n] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        }
+    }
+    out[2 * lane] = v[0];
+    out[2 * lane + 1] = v[1];
 }
 
 // ---- per-CTA setup / teardown -------------------------------------------------------
@@ -413,20 +432,28 @@ __global__ void __launch_bounds__(kThreads) k_gradients(const Packed* __restrict
     float z2[kH];
     tile_forward(c, z2);
     const float e = valid ? head(c, z2) - y : 0.0f;
-    const float dpred = 2.0f * e / (float)m;
-    __syncthreads();  // sg zeroed
+    const float dpred = 2.0f * e / (float)m;  // 0 on rows past m
+    float* red = reinterpret_cast<float*>(c.sm + SM_RED);
+    const int warp = t >> 5;
     float dz[kH];
+    {
+        float v[kH];
 #pragma unroll
-    for (int j = 0; j < kH; ++j) {
-        const float h2 = fmaxf(z2[j], 0.0f);
-        dz[j] = z2[j] > 0.0f ? dpred * w3[j] : 0.0f;
-        if (valid) {
-            atomicAdd(&sg[MDAS_MLP_OFF_W3 + j], dpred * h2);
-            atomicAdd(&sg[MDAS_MLP_OFF_B2 + j], dz[j]);
+        for (int j = 0; j < kH; ++j) {
+            v[j] = dpred * fmaxf(z2[j], 0.0f);
+            dz[j] = z2[j] > 0.0f ? dpred * w3[j] : 0.0f;
+            z2f[t * 65 + j] = dz[j];
         }
-        z2f[t * 65 + j] = dz[j];
+        warp_sum64(v, red + (0 * 4 + warp) * kH);  // dw3
+#pragma unroll
+        for (int j = 0; j < kH; ++j) v[j] = dz[j];
+        warp_sum64(v, red + (1 * 4 + warp) * kH);  // db2
+        float d3 = dpred;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) d3 += __shfl_xor_sync(0xffffffffu, d3, o);
+        __syncthreads();  // sg zeroed
+        if ((t & 31) == 0) atomicAdd(&sg[MDAS_MLP_OFF_B3], d3);
     }
-    if (valid) atomicAdd(&sg[MDAS_MLP_OFF_B3], dpred);
 #pragma unroll
     for (int kb = 0; kb < kH / 8; ++kb) st_row8(c.sm + SM_D, t, kb, 8, dz + 8 * kb);
     // dH1 = dZ2 . W2 on the tensor cores (B = W2 transposed, K-major)
@@ -440,12 +467,24 @@ __global__ void __launch_bounds__(kThreads) k_gradients(const Packed* __restrict
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int i = 8 * kb + q;
-            const float d1 = h[q] > 0.0f ? dh[i] : 0.0f;
-            z1f[t * 65 + i] = d1;
-            if (valid) atomicAdd(&sg[MDAS_MLP_OFF_B1 + i], d1);
+            dh[i] = h[q] > 0.0f ? dh[i] : 0.0f;  // dZ1 (0 on rows past m: their dZ2 is 0)
+            z1f[t * 65 + i] = dh[i];
         }
     }
+    warp_sum64(dh, red + (2 * 4 + warp) * kH);  // db1
     __syncthreads();
+    if (t < kH) {
+        float a = 0.0f, b = 0.0f, d = 0.0f;
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            a += red[(0 * 4 + w) * kH + t];
+            b += red[(1 * 4 + w) * kH + t];
+            d += red[(2 * 4 + w) * kH + t];
+        }
+        sg[MDAS_MLP_OFF_W3 + t] = a;
+        sg[MDAS_MLP_OFF_B2 + t] = b;
+        sg[MDAS_MLP_OFF_B1 + t] = d;
+    }
     // dW2[j][i] = sum_r dZ2[r][j] H1[r][i]: thread t owns j = t / 2, i in [32 (t % 2), +32)
     {
         const int j = t >> 1, i0 = (t & 1) * 32;

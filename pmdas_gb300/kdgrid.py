@@ -266,6 +266,9 @@ class KDGrid:
         N.check(self._lib.mdas_learned_update(self._h, C.byref(loss)), "learned_update")
         return loss.value
 
+    def LearnedPredict(self):
+        N.check(self._lib.mdas_learned_predict(self._h), "learned_predict")
+
     def LearnedParams(self) -> np.ndarray:
         p = np.empty(N.MLP_PARAMS, np.float32)
         N.check(self._lib.mdas_learned_get_params(self._h, _ptr(p)), "learned_get_params")
