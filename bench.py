@@ -304,7 +304,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
                "ms_per_step": round(e2e_s * 1e3, 3), "includes": "integrand, host syncs per pass, copies"}
 
     order = None if args.no_order else order_block(grid, wl, peak)
-    learned = None if args.no_learned or world > 1 else learned_block(wl, scene, ref, peaks)
+    learned = None if args.no_learned or world > 1 else learned_block(peaks)
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -384,77 +384,78 @@ def order_block(grid, wl, peak: float, reps: int = 5) -> dict:
             "locate_mpoints_per_s": round(pts.shape[0] / (loc_ms / 1e3) / 1e6, 1)}
 
 
-def learned_block(wl, scene, ref, peaks: dict, reps: int = 5) -> dict:
-    """The same render in learned mode (MLP acceptance, trained every pass) next
-    to the plain host loop: time, quality, loss, and the tensor-core predict
-    kernel's throughput against both rooflines."""
+def time_to_target(points, target):
+    """Wall time at which rel-MSE reaches `target`, interpolated log-log between the
+    two ladder points around it; None if the ladder never reaches it."""
+    import math
+    for (t0, e0), (t1, e1) in zip(points, points[1:]):
+        if e1 <= target < e0 or e0 <= target:
+            if e0 <= target:
+                return t0
+            f = (math.log(target) - math.log(e0)) / (math.log(e1) - math.log(e0))
+            return math.exp(math.log(t0) + f * (math.log(t1) - math.log(t0)))
+    if points and points[-1][1] <= target:
+        return points[-1][0]
+    return None
+
+
+def learned_block(peaks: dict, ladder=(16, 32, 64, 128, 256, 512), target: float = 1e-3) -> dict:
+    """Time to rel-MSE 1e-3, learned vs plain, on the learned workload (5-D motion
+    blur + depth of field, 1920x1080, evaluation scene seed 100): both render a
+    ladder of budgets through the device-side loop (integrand included) until the
+    image's rel-MSE against the FP64 4096-spp reference reaches the target."""
+    import numpy as np
     import torch
 
     import pmdas_gb300 as P
+    from pmdas_gb300.workloads import WORKLOADS
 
+    wl = WORKLOADS["mbdof1080"]
+    wpath = os.path.join(ROOT, "pmdas_gb300", "weights", "priority_mbdof1080.f32")
+    if not os.path.exists(wpath):
+        return {"unavailable": "no trained weights (python -m pmdas_gb300.train_priority)"}
+    params = np.fromfile(wpath, dtype="<f4")
     W, H = wl.width, wl.height
-
-    def host_loop(learned: bool):
-        g = P.KDGrid(wl.dim, wl.maxSamples, wl.candidatesNum, wl.bitsPerDim, wl.extraImgBits, wl.alpha, wl.scaleX,
-                     wl.scaleY)
-        if learned:
-            g.LearnedEnable()
-        px = torch.zeros(H, W, 4, device="cuda")
-        losses = []
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        a.record()
-        g.InitialSampling()
-        scene.evaluate(g, 0, g.GetNumberOfSamples())
-        while True:
-            n, _, l, _ = g._counts()
-            if n >= wl.budget or n + l > wl.maxSamples:
+    scene = P.Scene(wl.scene_kind, wl.scene_seed, wl.scene_count, wl.scaleX, wl.scaleY, W, H)
+    ref = scene.reference_image(W, H, spp=4096)
+    out = {"workload": f"{wl.name}: 5-D 1920x1080, scene seed {wl.scene_seed}, alpha {wl.alpha}",
+           "weights": os.path.relpath(wpath, ROOT), "target_rel_mse": target,
+           "timing": "device-side render loop (one CUDA graph), integrand included, CUDA events"}
+    pixels = torch.zeros(H, W, 4, device="cuda")
+    for mode in ("plain", "learned"):
+        pts, rows = [], []
+        for spp in ladder:
+            budget = int(spp * W * H)
+            ms_cap = min(max(budget * 3 // 2, 4 * wl.initial_leaves + 1), (1 << 30) - 1)
+            g = P.KDGrid(wl.dim, ms_cap, wl.candidatesNum, wl.bitsPerDim, wl.extraImgBits, wl.alpha, wl.scaleX,
+                         wl.scaleY)
+            if mode == "learned":
+                g.LearnedEnable(params=params)
+            P.render_graph(g, scene, budget, pixels, W, H)  # build + warm
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            st = P.render_graph(g, scene, budget, pixels, W, H)
+            b.record()
+            torch.cuda.synchronize()
+            ms = a.elapsed_time(b)
+            img = pixels[..., :3].double()
+            rel = float(torch.nan_to_num((ref - img) ** 2 / (ref ** 2 + 1e-2), nan=0.0).mean().item())
+            row = {"spp": spp, "samples": st.numberOfSamples, "passes": st.passes, "ms": round(ms, 3),
+                   "rel_mse": rel}
+            if mode == "learned":
+                ls = g.LearnedStats()
+                row["passes_judged_plain"] = ls["plain"]
+            rows.append(row)
+            pts.append((ms, rel))
+            g.close()
+            if rel <= target:
                 break
-            g.ComputeErrors()
-            if learned:
-                losses.append(g.LearnedUpdate())
-            g.AdaptiveSampling()
-            n2, nn, _, _ = g._counts()
-            scene.evaluate(g, n2 - nn, nn)
-        g.Integrate(px, W, H)
-        b.record()
-        torch.cuda.synchronize()
-        img = px[..., :3].double()
-        rel = float(torch.nan_to_num((ref - img) ** 2 / (ref ** 2 + 1e-2), nan=0.0).mean().item()) if ref is not None \
-            else None
-        return g, a.elapsed_time(b), rel, losses
-
-    host_loop(True)  # warm
-    g, learned_ms, learned_rel, losses = host_loop(True)
-    _, plain_ms, plain_rel, _ = host_loop(False)
-    L = g.GetNumberOfNodes()
-    ts = []
-    for _ in range(reps + 1):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        a.record()
-        g.LearnedPredict()
-        b.record()
-        torch.cuda.synchronize()
-        ts.append(a.elapsed_time(b))
-    pred_ms = statistics.median(ts[1:])
-    flops = L * 2.0 * (16 * 64 + 64 * 64)  # tensor-core MACs x 2 (the 64-wide head runs on the CUDA cores)
-    nbf = (4 + 2 * wl.dim + 3) // 4 * 4
-    bytes_ = L * (nbf * 4 + 4 * 12 + 4)  # node + box record, 4 sample values, prediction
-    tf = flops / (pred_ms / 1e3) / 1e12
-    gbs = bytes_ / (pred_ms / 1e3) / 1e9
-    pk_tf = float(peaks.get("bf16_tflops", 1900.0))
-    pk_bw = float(peaks.get("hbm_gbs", 6800.0))
-    return {"config": "defaults: 4 Adam steps x 16384 leaves per pass, lr 2e-3, 5% plain-error fallback",
-            "render_ms": round(learned_ms, 3), "plain_host_loop_render_ms": round(plain_ms, 3),
-            "samples": g.GetNumberOfSamples(), "passes": len(losses),
-            "rel_mse": learned_rel, "plain_rel_mse": plain_rel,
-            "loss_first_last": [round(losses[0], 6), round(losses[-1], 6)] if losses else None,
-            "predict": {"leaves": L, "ms": round(pred_ms, 4), "gleaves_per_s": round(L / (pred_ms / 1e3) / 1e9, 3),
-                        "tensor": {"achieved": round(tf, 2), "peak": pk_tf, "unit": "TFLOP/s",
-                                   "frac": round(tf / pk_tf, 4)},
-                        "hbm": {"achieved": round(gbs, 1), "peak": pk_bw, "unit": "GB/s", "frac": round(gbs / pk_bw, 4)},
-                        "bound": "hbm (features: node + box + 4 gathered values per leaf)"}}
+        t = time_to_target(pts, target)
+        out[mode] = {"ladder": rows, "ms_to_target": round(t, 3) if t else None}
+    tp, tl = out["plain"]["ms_to_target"], out["learned"]["ms_to_target"]
+    out["learned_over_plain_time"] = round(tl / tp, 4) if tp and tl else None
+    scene.close()
+    return out
 
 
 def run_batch(args, rank: int, world: int, local_rank: int) -> dict:

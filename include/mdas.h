@@ -329,36 +329,43 @@ int mdas_locate(mdas_grid* g, const float* points, int n, int* leaves);
 /* ---- Learned acceptance: a leaf-priority MLP on the tensor cores.
  *
  * No reference counterpart.  The reference accepts a leaf with probability
- * powf(error / g_error, alpha) (kdgrid.cu:326).  In learned mode the ratio is
- * 2^prediction / g_error (at most 1), where the prediction is a
- * 16 -> 64 -> 64 -> 1 ReLU MLP (BF16 tcgen05 GEMMs, FP32 accumulation) of
- * per-leaf features: log2 box extents (image axes relative to the image), their
- * mean, the sample count, log2(1 + mean value) and log2(1 + mean absolute
- * deviation) per colour channel.  The plain error is the judge: every pass the
- * model takes `trainSteps` Adam steps on `batch` leaves against
- * log2(error) / 32, and a fixed hashed `fallback` fraction of the leaves keeps
- * the plain ratio.  Learned mode runs in mdas_sampling_pass / mdas_render
- * (not in mdas_render_graph, which returns MDAS_ERR_STATE while it is on). */
+ * powf(error / g_error, alpha) (kdgrid.cu:326).  In learned mode the error is
+ * replaced by an estimate of the leaf's true reconstruction error: the plain
+ * error times 2^(32 c), c the output of a 16 -> 64 -> 64 -> 1 ReLU MLP (BF16
+ * tcgen05 GEMMs, FP32 accumulation) of per-leaf features: log2 box extents of
+ * the first five dimensions (image axes relative to the image), the sample
+ * count, log2(1 + x) of the samples' luminance mean, deviation, minimum and
+ * maximum, the plain error, the depth below the initial cell, and the plain
+ * errors of the four neighbouring leaf slots; the ratio is the estimate over
+ * the largest one.  The model is trained offline (mdas_leaf_features,
+ * mdas_leaf_true_errors, mdas_mlp_gradients, mdas_mlp_adam) on
+ * log2(true error / plain error) / 32.  The plain error still judges every
+ * pass: both schedules' acceptance is drawn from the same random number, and a
+ * pass in which the learned schedule leaves more than (1 + tolerance) x the
+ * plain schedule's plain error unrefined takes the plain acceptance.
+ * Predictions are refreshed for the leaves whose error a pass recomputes.
+ * Learned mode runs in mdas_sampling_pass, mdas_render and mdas_render_graph. */
 #define MDAS_MLP_PARAMS 5313 /* W1[64][16], b1[64], W2[64][64], b2[64], w3[64], b3 */
 
 typedef struct mdas_learned_config {
-    int trainSteps;     /* Adam steps per pass (default 4) */
-    int batch;          /* leaves per step (default 16384) */
-    float learningRate; /* default 2e-3 */
-    float fallback;     /* fraction of leaves that keep the plain ratio (default 0.05) */
-    uint64_t seed;      /* weight initialisation (default 1) */
+    float tolerance;      /* default 0.05 */
+    uint64_t seed;        /* initial weights when params is NULL (default 1) */
+    const float* params;  /* host, MDAS_MLP_PARAMS trained weights (NULL: seeded initial weights) */
 } mdas_learned_config;
 
 int mdas_learned_defaults(mdas_learned_config* cfg);
-/* Turns learned mode on with freshly initialised weights (cfg == NULL: off). */
+/* Turns learned mode on (cfg == NULL: off). */
 int mdas_learned_enable(mdas_grid* g, const mdas_learned_config* cfg);
-/* Trains on the current leaves (needs their errors: after mdas_compute_errors)
- * and predicts every leaf; *loss (host, optional) = the last step's mean
- * squared error.  mdas_sampling_pass calls it between its two halves. */
-int mdas_learned_update(mdas_grid* g, float* loss);
-/* Predicts every leaf with the current weights, without training (frozen or
- * loaded weights: the next adaptive pass uses these predictions). */
+/* Predicts every leaf and judges the pass (needs the leaves' errors: after
+ * mdas_compute_errors); mdas_sampling_pass calls it between its halves. */
+int mdas_learned_update(mdas_grid* g);
+/* Predicts every leaf, without judging (tests, inspection). */
 int mdas_learned_predict(mdas_grid* g);
+/* Passes judged, passes sent back to the plain acceptance, the last pass's
+ * verdict (1 = plain) and its unrefined plain error of each schedule (each
+ * pointer optional). */
+int mdas_learned_stats(mdas_grid* g, int* judgedPasses, int* plainPasses, int* lastPlain, double* unrefinedLearned,
+                       double* unrefinedPlain);
 /* Host copies of the FP32 parameters (MDAS_MLP_PARAMS floats). */
 int mdas_learned_get_params(mdas_grid* g, float* params);
 int mdas_learned_set_params(mdas_grid* g, const float* params);
@@ -366,13 +373,22 @@ int mdas_learned_set_params(mdas_grid* g, const float* params);
 int mdas_learned_predictions(mdas_grid* g, float* pred);
 /* Device copy of the leaves' features (numberOfNodes x 16 floats). */
 int mdas_leaf_features(mdas_grid* g, float* features);
+/* Training targets: the true reconstruction error of leaves against the
+ * integrand's mean over each box from samplesPerLeaf uniform points (FP64
+ * accumulation): volume * sum_c |mean_c - ref_c| / sqrt(ref_c^2 + 1e-2).  For
+ * the `count` leaf slots in `leaves` (device), or every leaf if leaves is
+ * NULL; device output, one float per row. */
+int mdas_leaf_true_errors(mdas_grid* g, mdas_scene* s, int samplesPerLeaf, uint64_t seed, const int* leaves,
+                          int count, float* errors);
 
 /* The MLP on its own (device pointers): pred[m] of features[m x 16];
  * gradients of mean((pred - target)^2) into grads[MDAS_MLP_PARAMS] and the
- * loss into *loss (host). */
+ * loss into *loss (host); one bias-corrected Adam step (step >= 1) that also
+ * zeroes grads. */
 int mdas_mlp_forward(const float* params, const float* features, int m, float* pred, void* stream);
 int mdas_mlp_gradients(const float* params, const float* features, const float* targets, int m, float* grads,
                        float* loss, void* stream);
+int mdas_mlp_adam(float* params, float* m1, float* m2, float* grads, int step, float learningRate, void* stream);
 
 /* ---- env configuration (SDK/sutil/Environment.{h,cpp}; the options the MDAS
  *      apps register, optixMotionBlur.cpp:104-137) ---- */

@@ -166,6 +166,17 @@ class OracleGrid:
         self.N, self.L = n, l
 
 
+def evaluate_points(scene, points) -> np.ndarray:
+    """The integrand at arbitrary points (rows of `dim` floats) -> [n, 3] values."""
+    pts = np.ascontiguousarray(points, np.float32)
+    n, dim = pts.shape
+    vals = np.zeros((max(n, 1), 3), np.float32)
+    desc = C.create_string_buffer(scene.desc_bytes, len(scene.desc_bytes))
+    prims = np.ascontiguousarray(scene.prims, np.float32)
+    load().orc_evaluate(desc, prims.ctypes.data if prims.size else None, dim, _p(pts), _p(vals), 0, n)
+    return vals[:n]
+
+
 def convert_to_bytes(pixels: np.ndarray) -> np.ndarray:
     px = np.ascontiguousarray(pixels, np.float32)
     out = np.zeros(px.shape[:-1] + (4,), np.uint8)

@@ -40,8 +40,7 @@ MLP_PARAMS = 5313
 
 
 class LearnedConfig(C.Structure):
-    _fields_ = [("trainSteps", C.c_int), ("batch", C.c_int), ("learningRate", C.c_float), ("fallback", C.c_float),
-                ("seed", C.c_uint64)]
+    _fields_ = [("tolerance", C.c_float), ("seed", C.c_uint64), ("params", C.c_void_p)]
 
 
 class RenderStats(C.Structure):
@@ -118,8 +117,12 @@ SIGNATURES = {
     "mdas_locate": (_I, [_P, _P, _I, _P]),
     "mdas_learned_defaults": (_I, [C.POINTER(LearnedConfig)]),
     "mdas_learned_enable": (_I, [_P, C.POINTER(LearnedConfig)]),
-    "mdas_learned_update": (_I, [_P, C.POINTER(_F)]),
+    "mdas_learned_update": (_I, [_P]),
     "mdas_learned_predict": (_I, [_P]),
+    "mdas_learned_stats": (_I, [_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_double),
+                                C.POINTER(C.c_double)]),
+    "mdas_leaf_true_errors": (_I, [_P, _P, _I, C.c_uint64, _P, _I, _P]),
+    "mdas_mlp_adam": (_I, [_P, _P, _P, _P, _I, _F, _P]),
     "mdas_learned_get_params": (_I, [_P, _P]),
     "mdas_learned_set_params": (_I, [_P, _P]),
     "mdas_learned_predictions": (_I, [_P, _P]),

@@ -170,6 +170,7 @@ __global__ void __launch_bounds__(256) k_batch_errors(const MdasBatchImage* __re
 // ---- adaptive pass: decide
 template <int D>
 __global__ void __launch_bounds__(256) k_batch_decide(const MdasBatchImage* __restrict__ imgs, int n) {
+    pdl_launch_dependents();
     __shared__ int s_pre[MDAS_MAX_BATCH + 1];
     __shared__ unsigned s_warp[8];
     const int total = batch_prefix(n, s_pre, s_warp, [&](int i) {
@@ -195,6 +196,8 @@ __global__ void __launch_bounds__(256) k_batch_decide(const MdasBatchImage* __re
 
 // ---- adaptive pass: scan (one CTA of 1024 threads per image)
 __global__ void __launch_bounds__(1024) k_batch_scan(const MdasBatchImage* __restrict__ imgs, int n) {
+    pdl_wait();
+    pdl_launch_dependents();
     __shared__ unsigned s_sel[32], s_split[32];
     if ((int)blockIdx.x >= n) return;
     const MdasDeviceGrid& g = imgs[blockIdx.x].g;
@@ -205,6 +208,7 @@ __global__ void __launch_bounds__(1024) k_batch_scan(const MdasBatchImage* __res
 // ---- adaptive pass: place (one thread per accepted leaf)
 template <int D>
 __global__ void __launch_bounds__(256, 4) k_batch_place(const MdasBatchImage* __restrict__ imgs, int n) {
+    pdl_wait();
     __shared__ int s_pre[MDAS_MAX_BATCH + 1];
     __shared__ unsigned s_warp[8];
     const int total = batch_prefix(n, s_pre, s_warp, [&](int i) {
@@ -301,12 +305,15 @@ cudaError_t batch_decide(const MdasBatchImage* imgs, int n, int D, int grid, cud
 }
 
 cudaError_t batch_scan(const MdasBatchImage* imgs, int n, cudaStream_t s) {
-    k_batch_scan<<<n, 1024, 0, s>>>(imgs, n);
+    cudaError_t e = launch_pdl(k_batch_scan, n, 1024, s, imgs, n);
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
 cudaError_t batch_place(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s) {
-    MDAS_BATCH_SWITCH_D(D, (k_batch_place<DD><<<grid, 256, 0, s>>>(imgs, n)));
+    cudaError_t e = cudaSuccess;
+    MDAS_BATCH_SWITCH_D(D, (e = launch_pdl(k_batch_place<DD>, grid, 256, s, imgs, n)));
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
+#include <stddef.h>
 #include <math.h>
 #include <fstream>
 #include <string>
@@ -94,12 +95,12 @@ struct mdas_grid {
     size_t sortTempBytes = 0;
     // learned acceptance (mdas_learned_enable)
     bool learned = false;
-    mdas_learned_config lcfg{};
-    float* lState = nullptr;            // params, Adam m1, m2, grads (MDAS_MLP_PARAMS each), loss sum, status
+    float* lState = nullptr;            // FP32 params (MDAS_MLP_PARAMS), then a status word
     mdas_mlp::Packed* lPacked = nullptr;
     float* lPred = nullptr;             // [maxNodes] predicted log2(error) / MDAS_MLP_TARGET_SCALE
-    uint64_t lPredVersion = ~0ull;      // grid version the predictions belong to
-    int lStep = 0;
+    MdasLearnedStats* lStats = nullptr;
+    uint64_t lPredVersion = ~0ull;      // grid version the predictions (and the verdict) belong to
+    bool lastErrorsDirty = false;       // the last errors pass visited only the split children
 };
 
 namespace {
@@ -230,6 +231,7 @@ void free_grid(mdas_grid* g) {
     cudaFree(g->lState);
     cudaFree(g->lPacked);
     cudaFree(g->lPred);
+    cudaFree(g->lStats);
     if (g->scratch) cudaFree(g->scratch);
     if (g->hcounts) cudaFreeHost(g->hcounts);
     delete g->log;
@@ -402,6 +404,7 @@ int mdas_compute_errors(mdas_grid* g) {
     g->launches += 1;
     if (rc) return rc;
     g->errorsClean = true;
+    g->lastErrorsDirty = dirty;
     if (g->log) *g->log << "COMPUTE ERRORS TIME\n" << last_stage_ms(g, 1) << std::endl;
     return MDAS_OK;
 }
@@ -436,7 +439,7 @@ int mdas_sampling_pass(mdas_grid* g) {
     int rc = mdas_compute_errors(g);
     if (rc) return rc;
     if (g->learned) {
-        rc = mdas_learned_update(g, nullptr);
+        rc = mdas_learned_update(g);
         if (rc) return rc;
     }
     return mdas_adaptive_sampling(g);
@@ -818,6 +821,8 @@ cudaError_t launch_adaptive_on(mdas_grid* g, int gridDecide, int gridPlace, cuda
 // conditional while node around {errors, adaptive pass, integrand for the new
 // samples, loop condition}, integrate.  Every kernel has a fixed persistent
 // grid and reads the leaf and sample counts from device memory.
+cudaError_t learned_queue(mdas_grid* g, int L, cudaStream_t s);
+
 int build_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, int width, int height) {
     if (g->graph.exec) {
         cudaGraphExecDestroy(g->graph.exec);
@@ -880,7 +885,12 @@ int build_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, i
     e = cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
     if (e != cudaSuccess) return fail(e);
     cudaError_t eb = launch_errors_auto(g, gErr, bs);
+    if (eb == cudaSuccess && g->learned) {
+        eb = learned_queue(g, -1, bs);  // predictions and the judge's verdict for this pass
+        g->dg.priority = g->lPred;
+    }
     if (eb == cudaSuccess) eb = launch_adaptive_on(g, gDecide, gPlace, bs);
+    g->dg.priority = nullptr;
     if (eb == cudaSuccess)
         eb = mdas_launch_evaluate(s->desc, s->d_prims, d.coords, d.values, d.D, d.counts, 0, 0, gEval, bs);
     if (eb == cudaSuccess)
@@ -914,7 +924,6 @@ int build_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, i
 int mdas_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, int width, int height,
                       mdas_render_stats* stats) {
     if (!g || !s || !pixels || width <= 0 || height <= 0 || s->desc.dim > g->dg.D) return MDAS_ERR_INVALID;
-    if (g->learned) return MDAS_ERR_STATE;  // learned mode trains between passes: mdas_render runs it
     int rc = scene_upload(s, g->stream);
     if (rc) return rc;
     flush_timing(g);
@@ -1424,11 +1433,9 @@ int mdas_locate(mdas_grid* g, const float* points, int n, int* leaves) {
 
 int mdas_learned_defaults(mdas_learned_config* cfg) {
     if (!cfg) return MDAS_ERR_INVALID;
-    cfg->trainSteps = 4;
-    cfg->batch = 16384;
-    cfg->learningRate = 2e-3f;
-    cfg->fallback = 0.05f;
+    cfg->tolerance = 0.05f;
     cfg->seed = 1;
+    cfg->params = nullptr;
     return MDAS_OK;
 }
 
@@ -1462,18 +1469,38 @@ void mlp_init(std::vector<float>& p, uint64_t seed) {
     fill(MDAS_MLP_OFF_B3, 1, MDAS_MLP_HIDDEN);
 }
 
-constexpr size_t kStateFloats = 4 * (size_t)MDAS_MLP_PARAMS + 4;  // params, m1, m2, grads, loss sum, status
+unsigned* learned_status(mdas_grid* g) { return reinterpret_cast<unsigned*>(g->lState + MDAS_MLP_PARAMS); }
 
 int learned_upload(mdas_grid* g, const float* hostParams) {
-    const size_t P = MDAS_MLP_PARAMS;
-    cudaError_t e = cudaMemsetAsync(g->lState, 0, sizeof(float) * kStateFloats, g->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(g->lState, hostParams, sizeof(float) * P, cudaMemcpyHostToDevice, g->stream);
+    cudaError_t e = cudaMemcpyAsync(g->lState, hostParams, sizeof(float) * MDAS_MLP_PARAMS, cudaMemcpyHostToDevice,
+                                    g->stream);
     if (e == cudaSuccess) e = mdas_mlp::pack(g->lState, g->lPacked, g->stream);
     g->launches += 1;
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
-    g->lStep = 0;
     g->lPredVersion = ~0ull;
     return status_of(e);
+}
+
+// Queues the per-pass learned work on stream s: clear the pass's statistics,
+// predict every leaf (L < 0: the device leaf count), judge both schedules.
+cudaError_t learned_queue(mdas_grid* g, int L, cudaStream_t s) {
+    MdasLearnedStats* st = g->lStats;
+    cudaError_t e = cudaMemsetAsync(st, 0, offsetof(MdasLearnedStats, plainPasses), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(&st->unrefinedLearned, 0, 2 * sizeof(double), s);
+    // refresh the leaves whose error was recomputed (every leaf when the last
+    // errors pass was a full one or the predictions are not from the previous
+    // pass), then the exact maximum
+    const int mode = L < 0 ? 2 : (g->lastErrorsDirty && g->lPredVersion + 1 == g->version ? 1 : 0);
+    if (e == cudaSuccess)
+        e = mdas_mlp::predict_leaves(g->dg, L, mode, g->lPacked, g->lPred, &st->predMax, learned_status(g), s);
+    MdasDeviceGrid dg = g->dg;
+    dg.priority = g->lPred;
+    const int grid = g->numSMs * 4;
+    if (e == cudaSuccess)
+        e = g->arith == MDAS_ARITH_IEEE ? mdas_ieee::learned_judge(dg, L, grid, s)
+                                        : mdas_fast::learned_judge(dg, L, grid, s);
+    g->launches += 3;
+    return e;
 }
 
 }  // namespace
@@ -1482,65 +1509,48 @@ extern "C" {
 
 int mdas_learned_enable(mdas_grid* g, const mdas_learned_config* cfg) {
     if (!g) return MDAS_ERR_INVALID;
+    if (g->graph.exec) cudaGraphExecDestroy(g->graph.exec);  // a cached device-side render was built for the other mode
+    g->graph = RenderGraph{};
     if (!cfg) {
         g->learned = false;
         g->lPredVersion = ~0ull;
+        g->dg.priority = nullptr;
+        g->dg.learned = nullptr;
         return MDAS_OK;
     }
-    if (cfg->trainSteps < 0 || cfg->batch < 1 || !(cfg->learningRate >= 0.0f) || !(cfg->fallback >= 0.0f) ||
-        cfg->fallback > 1.0f)
-        return MDAS_ERR_INVALID;
+    if (!(cfg->tolerance >= 0.0f)) return MDAS_ERR_INVALID;
     if (!g->lState) {
-        const bool ok = cudaMalloc(&g->lState, sizeof(float) * kStateFloats) == cudaSuccess &&
+        const bool ok = cudaMalloc(&g->lState, sizeof(float) * (MDAS_MLP_PARAMS + 1)) == cudaSuccess &&
                         cudaMalloc(&g->lPacked, sizeof(mdas_mlp::Packed)) == cudaSuccess &&
-                        cudaMalloc(&g->lPred, sizeof(float) * (size_t)g->dg.maxNodes) == cudaSuccess;
+                        cudaMalloc(&g->lPred, sizeof(float) * (size_t)g->dg.maxNodes) == cudaSuccess &&
+                        cudaMalloc(&g->lStats, sizeof(MdasLearnedStats)) == cudaSuccess;
         if (!ok) return MDAS_ERR_ALLOC;
     }
-    g->lcfg = *cfg;
+    MdasLearnedStats h{};
+    h.tolerance = cfg->tolerance;
+    cudaError_t e = cudaMemcpyAsync(g->lStats, &h, sizeof(h), cudaMemcpyHostToDevice, g->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(learned_status(g), 0, sizeof(unsigned), g->stream);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
     std::vector<float> p;
-    mlp_init(p, cfg->seed);
+    if (cfg->params) p.assign(cfg->params, cfg->params + MDAS_MLP_PARAMS);
+    else mlp_init(p, cfg->seed);
     const int rc = learned_upload(g, p.data());
     if (rc) return rc;
     g->dg.priorityScale = MDAS_MLP_TARGET_SCALE;
-    g->dg.fallback1024 = (int)lrintf(cfg->fallback * 1024.0f);
+    g->dg.learned = g->lStats;
     g->learned = true;
     return MDAS_OK;
 }
 
-int mdas_learned_update(mdas_grid* g, float* loss) {
+int mdas_learned_update(mdas_grid* g) {
     if (!g || !g->learned) return MDAS_ERR_INVALID;
     if (!g->initialized || !g->errorsClean) return MDAS_ERR_STATE;  // needs current leaf errors
-    const size_t P = MDAS_MLP_PARAMS;
-    float* params = g->lState;
-    float* m1 = params + P;
-    float* m2 = m1 + P;
-    float* grads = m2 + P;
-    float* lossSum = grads + P;
-    unsigned* status = reinterpret_cast<unsigned*>(lossSum + 1);
-    const int L = g->L;
-    const int m = g->lcfg.batch < L ? g->lcfg.batch : L;
-    const int stride = L / m > 0 ? L / m : 1;
-    cudaError_t e = cudaMemsetAsync(lossSum, 0, sizeof(float) * 2, g->stream);
-    for (int k = 0; k < g->lcfg.trainSteps && e == cudaSuccess; ++k) {
-        const int step = ++g->lStep;
-        const int offset = (int)(((uint64_t)step * 2654435761ull) % (uint64_t)stride);
-        e = cudaMemsetAsync(lossSum, 0, sizeof(float), g->stream);
-        if (e == cudaSuccess)
-            e = mdas_mlp::gradients(g->lPacked, nullptr, nullptr, &g->dg, L, offset, stride, m, grads, lossSum, status,
-                                    g->stream);
-        if (e == cudaSuccess) e = mdas_mlp::adam(params, m1, m2, grads, step, g->lcfg.learningRate, g->lPacked, g->stream);
-        g->launches += 3;
-    }
-    if (e == cudaSuccess) e = mdas_mlp::predict_leaves(g->dg, L, g->lPacked, g->lPred, status, g->stream);
-    g->launches += 1;
-    float h[2] = {0.0f, 0.0f};
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h, lossSum, sizeof(h), cudaMemcpyDeviceToHost, g->stream);
+    cudaError_t e = learned_queue(g, g->L, g->stream);
+    unsigned st = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, learned_status(g), sizeof(st), cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     if (e != cudaSuccess) return MDAS_ERR_CUDA;
-    unsigned st;
-    memcpy(&st, &h[1], sizeof(st));
     if (st) return MDAS_ERR_TIMEOUT;
-    if (loss) *loss = g->lcfg.trainSteps > 0 ? h[0] / (float)m : 0.0f;
     g->lPredVersion = g->version;
     return MDAS_OK;
 }
@@ -1548,16 +1558,28 @@ int mdas_learned_update(mdas_grid* g, float* loss) {
 int mdas_learned_predict(mdas_grid* g) {
     if (!g || !g->learned) return MDAS_ERR_INVALID;
     if (!g->initialized) return MDAS_ERR_STATE;
-    unsigned* status = reinterpret_cast<unsigned*>(g->lState + 4 * (size_t)MDAS_MLP_PARAMS + 1);
-    cudaError_t e = cudaMemsetAsync(status, 0, sizeof(unsigned), g->stream);
-    if (e == cudaSuccess) e = mdas_mlp::predict_leaves(g->dg, g->L, g->lPacked, g->lPred, status, g->stream);
-    g->launches += 1;
+    cudaError_t e = mdas_mlp::predict_leaves(g->dg, g->L, 0, g->lPacked, g->lPred, &g->lStats->predMax,
+                                             learned_status(g), g->stream);
+    g->launches += 2;
     unsigned st = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, status, sizeof(st), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, learned_status(g), sizeof(st), cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     if (e != cudaSuccess) return MDAS_ERR_CUDA;
-    if (st) return MDAS_ERR_TIMEOUT;
-    g->lPredVersion = g->version;
+    return st ? MDAS_ERR_TIMEOUT : MDAS_OK;
+}
+
+int mdas_learned_stats(mdas_grid* g, int* judgedPasses, int* plainPasses, int* lastPlain, double* unrefinedLearned,
+                       double* unrefinedPlain) {
+    if (!g || !g->lStats) return MDAS_ERR_INVALID;
+    MdasLearnedStats h;
+    cudaError_t e = cudaMemcpyAsync(&h, g->lStats, sizeof(h), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    if (judgedPasses) *judgedPasses = h.judgedPasses;
+    if (plainPasses) *plainPasses = h.plainPasses;
+    if (lastPlain) *lastPlain = h.usePlain;
+    if (unrefinedLearned) *unrefinedLearned = h.unrefinedLearned;
+    if (unrefinedPlain) *unrefinedPlain = h.unrefinedPlain;
     return MDAS_OK;
 }
 
@@ -1575,8 +1597,21 @@ int mdas_learned_set_params(mdas_grid* g, const float* params) {
 
 int mdas_learned_predictions(mdas_grid* g, float* pred) {
     if (!g || !pred) return MDAS_ERR_INVALID;
-    if (!g->learned || g->lPredVersion != g->version) return MDAS_ERR_STATE;
+    if (!g->learned) return MDAS_ERR_STATE;
     cudaError_t e = cudaMemcpyAsync(pred, g->lPred, sizeof(float) * (size_t)g->L, cudaMemcpyDeviceToDevice, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    return status_of(e);
+}
+
+int mdas_leaf_true_errors(mdas_grid* g, mdas_scene* s, int samplesPerLeaf, uint64_t seed, const int* leaves,
+                          int count, float* errors) {
+    if (!g || !s || !errors || samplesPerLeaf < 1 || s->desc.dim > g->dg.D || (leaves && count < 0)) return MDAS_ERR_INVALID;
+    if (!g->initialized) return MDAS_ERR_STATE;
+    int rc = scene_upload(s, g->stream);
+    if (rc) return rc;
+    cudaError_t e = mdas_launch_leaf_true_errors(s->desc, s->d_prims, g->dg, leaves, leaves ? count : g->L,
+                                                 samplesPerLeaf, seed, errors, g->stream);
+    g->launches += 1;
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     return status_of(e);
 }
@@ -1628,6 +1663,16 @@ int mdas_mlp_forward(const float* params, const float* features, int m, float* p
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return MDAS_ERR_CUDA;
     return st ? MDAS_ERR_TIMEOUT : MDAS_OK;
+}
+
+int mdas_mlp_adam(float* params, float* m1, float* m2, float* grads, int step, float learningRate, void* stream) {
+    if (!params || !m1 || !m2 || !grads || step < 1 || !(learningRate >= 0.0f)) return MDAS_ERR_INVALID;
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    MlpScratch sc;
+    if (!sc.open()) return MDAS_ERR_ALLOC;
+    cudaError_t e = mdas_mlp::adam(params, m1, m2, grads, step, learningRate, sc.packed, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return status_of(e);
 }
 
 int mdas_mlp_gradients(const float* params, const float* features, const float* targets, int m, float* grads,

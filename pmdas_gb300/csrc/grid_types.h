@@ -22,6 +22,32 @@ struct MdasCounts {
     int active;         // batched rendering: 1 while this image still takes passes
 };
 
+// Learned acceptance, one pass: the largest prediction, and the judge's sums of
+// the plain errors that each schedule leaves unrefined (leaves it does not
+// accept) and its verdict.
+struct MdasLearnedStats {
+    unsigned predMax;            // order-preserving bits of the largest prediction
+    unsigned blocksDone;         // judge blocks finished (the last one decides)
+    int usePlain;                // 1: this pass takes the plain acceptance
+    int plainPasses;             // passes the judge sent back to the plain acceptance
+    double unrefinedLearned;     // sum of plain errors of the leaves the learned schedule does not accept
+    double unrefinedPlain;       // the same for the plain schedule
+    float tolerance;             // revert when unrefinedLearned > (1 + tolerance) * unrefinedPlain
+    int judgedPasses;
+};
+
+// Order-preserving unsigned image of a float (for atomicMax over floats of any sign).
+__host__ __device__ inline unsigned mdas_float_order(float f) {
+    union { float f; unsigned u; } c;
+    c.f = f;
+    return (c.u & 0x80000000u) ? ~c.u : (c.u | 0x80000000u);
+}
+__host__ __device__ inline float mdas_float_unorder(unsigned u) {
+    union { float f; unsigned u; } c;
+    c.u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    return c.f;
+}
+
 // Scratch of one adaptive pass: the counts before it, for the place kernel.
 struct MdasCtl {
     int N0;
@@ -57,11 +83,10 @@ struct MdasDeviceGrid {
     int maxTiles;
     int* dirty;           // [maxNodes/2 + 1], slots of the left children of the last pass's splits
     // learned acceptance (nullptr: the reference's plain error ratio): predicted
-    // log2(error) / priorityScale per leaf; leaves whose hash falls below
-    // fallback1024 / 1024 keep the plain ratio
+    // log2(error) / priorityScale per leaf, and the pass's statistics and verdict
     const float* priority;
     float priorityScale;
-    int fallback1024;
+    MdasLearnedStats* learned;
 };
 
 // One image of a batched render (device-side descriptor).
@@ -116,6 +141,7 @@ struct MdasBatchImage {
     cudaError_t loop_condition(const MdasDeviceGrid& g, cudaGraphConditionalHandle h, int budget,           \
                                int maxPasses, cudaStream_t s);                                              \
     int max_blocks_per_sm(int D, int which);                                                                \
+    cudaError_t learned_judge(const MdasDeviceGrid& g, int L, int grid, cudaStream_t s);                     \
     }
 
 MDAS_DECLARE_LAUNCHERS(mdas_fast)

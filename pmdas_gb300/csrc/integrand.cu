@@ -148,6 +148,63 @@ __global__ void __launch_bounds__(256) k_reference_image(MdasScene sc, const flo
     }
 }
 
+// True reconstruction error of each leaf (the training target of the learned
+// leaf priority): the leaf's mean sample value against the integrand's mean
+// over the leaf's box, estimated from `samples` uniform points with FP64
+// accumulation; err = volume * sum_c |mean_c - ref_c| / sqrt(ref_c^2 + 1e-2),
+// in the units of the plain error (a relative deviation times the volume,
+// image axes in pixels).
+template <int D>
+__global__ void __launch_bounds__(256) k_leaf_true_errors(MdasScene sc, const float* __restrict__ prims,
+                                                           MdasDeviceGrid g, const int* __restrict__ leaves, int L,
+                                                           int samples, unsigned long long seed,
+                                                           float* __restrict__ out) {
+    extern __shared__ float s_prims[];
+    const int nfl = sc.count * MDAS_PRIM_STRIDE;
+    for (int k = threadIdx.x; k < nfl; k += blockDim.x) s_prims[k] = prims[k];
+    __syncthreads();
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < L; row += gridDim.x * blockDim.x) {
+        const int i = leaves ? leaves[row] : row;
+        const float* nb = g.nb + (size_t)i * g.nbFloats;
+        const int idx[4] = {reinterpret_cast<const int*>(nb)[0], reinterpret_cast<const int*>(nb)[1],
+                            reinterpret_cast<const int*>(nb)[2], reinterpret_cast<const int*>(nb)[3]};
+        float mn[D], mx[D];
+        float volume = 1.0f;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            mn[d] = nb[4 + d];
+            mx[d] = nb[4 + D + d];
+            volume *= mx[d] - mn[d];
+        }
+        float mean[3] = {0.0f, 0.0f, 0.0f};
+        int n = 0;
+        for (int k = 0; k < 4; ++k) {
+            if (idx[k] < 0) continue;
+            for (int c = 0; c < 3; ++c) mean[c] += g.values[3 * (size_t)idx[k] + c];
+            ++n;
+        }
+        for (int c = 0; c < 3; ++c) mean[c] = n ? mean[c] / (float)n : 0.0f;
+        Lcg64 rng{seed ^ (0x9E3779B97F4A7C15ull * (unsigned long long)(i + 1))};
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (int s = 0; s < samples; ++s) {
+            float c[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) c[d] = mn[d] + rng.next() * (mx[d] - mn[d]);
+            float v[3];
+            mdas_shade(&sc, s_prims, c, v);
+            acc[0] += (double)v[0];
+            acc[1] += (double)v[1];
+            acc[2] += (double)v[2];
+        }
+        double e = 0.0;
+        for (int c = 0; c < 3; ++c) {
+            const double ref = acc[c] / (double)samples;
+            e += fabs((double)mean[c] - ref) / sqrt(ref * ref + 1e-2);
+        }
+        out[row] = (float)(e * (double)volume);
+    }
+}
+
 // splitmix64 (Steele, Lea & Flood, "Fast splittable pseudorandom number
 // generators", OOPSLA 2014): the documented stream every scene is drawn from.
 struct SplitMix64 {
@@ -164,6 +221,22 @@ struct SplitMix64 {
 };
 
 }  // namespace
+
+cudaError_t mdas_launch_leaf_true_errors(const MdasScene& sc, const float* d_prims, const MdasDeviceGrid& g,
+                                         const int* leaves, int L, int samples, unsigned long long seed, float* out,
+                                         cudaStream_t s) {
+    if (L <= 0) return cudaSuccess;
+    const size_t smem = sizeof(float) * MDAS_PRIM_STRIDE * (size_t)sc.count;
+    const int grid = (L + 255) / 256 < 65535 ? (L + 255) / 256 : 65535;
+    switch (g.D) {
+        case 3: k_leaf_true_errors<3><<<grid, 256, smem, s>>>(sc, d_prims, g, leaves, L, samples, seed, out); break;
+        case 4: k_leaf_true_errors<4><<<grid, 256, smem, s>>>(sc, d_prims, g, leaves, L, samples, seed, out); break;
+        case 5: k_leaf_true_errors<5><<<grid, 256, smem, s>>>(sc, d_prims, g, leaves, L, samples, seed, out); break;
+        case 6: k_leaf_true_errors<6><<<grid, 256, smem, s>>>(sc, d_prims, g, leaves, L, samples, seed, out); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
 
 cudaError_t mdas_launch_evaluate(const MdasScene& sc, const float* d_prims, const float* coords, float* values,
                                  int dim, const MdasCounts* counts, int offset, int count, int grid, cudaStream_t s) {

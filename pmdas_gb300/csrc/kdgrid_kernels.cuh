@@ -69,6 +69,14 @@ __device__ __forceinline__ unsigned lcg(unsigned& prev) {
 
 __device__ __forceinline__ float rnd(unsigned& prev) { return (float)lcg(prev) / (float)0x01000000; }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialisation may start before its predecessor ends; it waits here (in
+// hardware) until the predecessor has completed and its writes are visible.
+// Without that launch attribute the wait returns at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Lets the next kernel (if launched programmatically) be scheduled now.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+
 // ---- vector loads and stores of NF floats from a 16-byte aligned address ---------
 template <int NF>
 __device__ __forceinline__ void ld_floats(const float* __restrict__ p, float (&out)[NF]) {
@@ -406,13 +414,10 @@ __device__ __forceinline__ unsigned acc_pack(unsigned local, unsigned splitRank,
     return local | (splitRank << 11) | (split << 22) | (cnt << 23);
 }
 
-// Learned acceptance ratio (no reference counterpart): 2^(predicted log2 error)
-// / g_error, at most 1; a fixed hashed fraction of the leaves keeps the plain
-// error ratio of kdgrid.cu:326.
-__device__ __forceinline__ float learned_ratio(const MdasDeviceGrid& g, int leaf, float err, float gError) {
-    const unsigned h = ((unsigned)leaf * 2654435761u) >> 22;  // 10-bit multiplicative hash
-    if ((int)h < g.fallback1024) return err / gError;
-    return fminf(exp2f(g.priority[leaf] * g.priorityScale - log2f(gError)), 1.0f);
+// Learned acceptance ratio (no reference counterpart): the predicted error over
+// the largest predicted error, as kdgrid.cu:326 divides the error by g_error.
+__device__ __forceinline__ float learned_ratio(const MdasDeviceGrid& g, int leaf, float predMax) {
+    return exp2f((g.priority[leaf] - predMax) * g.priorityScale);
 }
 
 // decide, one tile: acceptance of the tile's leaves, final seeds, the tile's
@@ -457,6 +462,9 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
             lc[j] = v ? (int)g.leafCounts[i0 + j] : 0;
         }
     }
+    // learned acceptance unless the judge sent this pass back to the plain one
+    const bool learned = g.priority != nullptr && !g.learned->usePlain;
+    const float predMax = learned ? mdas_float_unorder(g.learned->predMax) : 0.0f;
     unsigned accMask = 0;
     unsigned seedAcc[K];
 #pragma unroll
@@ -466,8 +474,8 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
         if (seed == 0) seed = tea4((unsigned)leaf, 0);
         bool a = false;
         if (leaf < L) {
-            if (!g.priority) a = mdas_pow(err[j] / gError, g.alpha) >= rnd(seed);
-            else a = mdas_pow(learned_ratio(g, leaf, err[j], gError), g.alpha) >= rnd(seed);
+            if (!learned) a = mdas_pow(err[j] / gError, g.alpha) >= rnd(seed);
+            else a = mdas_pow(learned_ratio(g, leaf, predMax), g.alpha) >= rnd(seed);
         }
         seedAcc[j] = seed;
         sd[j] = a ? jumpA * seed + jumpC : seed;  // the seed after the candidate draws
@@ -534,6 +542,7 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
 
 template <int D>
 __global__ void __launch_bounds__(256) k_adaptive_decide(MdasDeviceGrid g, unsigned jumpA, unsigned jumpC) {
+    pdl_launch_dependents();
     __shared__ unsigned s_warp[8];
     const int L = g.counts->L;
     const float gError = __uint_as_float(g.counts->gerr);
@@ -620,6 +629,8 @@ __device__ __forceinline__ void scan_image(const MdasDeviceGrid& g, unsigned* s_
 }
 
 __global__ void __launch_bounds__(1024) k_adaptive_scan(MdasDeviceGrid g) {
+    pdl_wait();
+    pdl_launch_dependents();
     __shared__ unsigned s_sel[32], s_split[32];
     scan_image(g, s_sel, s_split);
 }
@@ -791,6 +802,7 @@ __device__ __forceinline__ void place_rank(const MdasDeviceGrid& g, int k, int N
 // One thread per accepted leaf, in accepted-rank order.
 template <int D>
 __global__ void __launch_bounds__(256, 4) k_adaptive_place(MdasDeviceGrid g) {
+    pdl_wait();
     const int N = g.ctl->N0;
     const int L = g.ctl->L0;
     const int accepted = g.counts->newN;
@@ -973,7 +985,78 @@ __global__ void k_pack_records(float* __restrict__ nb, float* __restrict__ lsc, 
     }
 }
 
+// Learned mode, per pass: both schedules' acceptance of every leaf (the same
+// first draw of its seed as decide's), the plain errors each leaves unrefined,
+// and the verdict, set by the last block to finish (no block waits for another).
+__global__ void __launch_bounds__(256) k_learned_judge(MdasDeviceGrid g, int Lhost) {
+    __shared__ double s_l[8], s_p[8];
+    __shared__ bool s_last;
+    const int L = Lhost >= 0 ? Lhost : g.counts->L;  // < 0: the device leaf count (inside a graph)
+    const float gError = __uint_as_float(g.counts->gerr);
+    const float predMax = mdas_float_unorder(g.learned->predMax);
+    double ul = 0.0, up = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
+        const float e = g.errors[i];
+        unsigned seed = g.seeds[i];
+        if (seed == 0) seed = tea4((unsigned)i, 0);
+        const float r = rnd(seed);
+        const bool plain = mdas_pow(e / gError, g.alpha) >= r;
+        const bool learned = mdas_pow(learned_ratio(g, i, predMax), g.alpha) >= r;
+        if (!plain) up += (double)e;
+        if (!learned) ul += (double)e;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ul += __shfl_xor_sync(0xffffffffu, ul, o);
+        up += __shfl_xor_sync(0xffffffffu, up, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s_l[threadIdx.x >> 5] = ul;
+        s_p[threadIdx.x >> 5] = up;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            a += s_l[w];
+            b += s_p[w];
+        }
+        atomicAdd(&g.learned->unrefinedLearned, a);
+        atomicAdd(&g.learned->unrefinedPlain, b);
+        __threadfence();
+        s_last = atomicAdd(&g.learned->blocksDone, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+        __threadfence();
+        MdasLearnedStats* st = g.learned;
+        const double a = atomicAdd(&st->unrefinedLearned, 0.0), b = atomicAdd(&st->unrefinedPlain, 0.0);
+        const int revert = a > (1.0 + (double)st->tolerance) * b ? 1 : 0;
+        st->usePlain = revert;
+        st->plainPasses += revert;
+        st->judgedPasses += 1;
+        st->blocksDone = 0;
+    }
+}
+
 // ---- host launchers -------------------------------------------------------------
+// A launch that may overlap the tail of the previous kernel on the stream (the
+// kernel calls pdl_wait() before it reads what that kernel wrote).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 #define MDAS_SWITCH_D(D, EXPR)                 \
     switch (D) {                               \
         case 3: { constexpr int DD = 3; EXPR; } break; \
@@ -1043,8 +1126,16 @@ cudaError_t adaptive_sampling(const MdasDeviceGrid& g, int gridDecide, int gridP
     unsigned A, C;
     lcg_jump((unsigned)(g.candidatesNum * g.D), &A, &C);
     MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD><<<gridDecide, 256, 0, s>>>(g, A, C)));
-    k_adaptive_scan<<<1, 1024, 0, s>>>(g);
-    MDAS_SWITCH_D(g.D, (k_adaptive_place<DD><<<gridPlace, 256, 0, s>>>(g)));
+    e = launch_pdl(k_adaptive_scan, 1, 1024, s, g);
+    if (e != cudaSuccess) return e;
+    MDAS_SWITCH_D(g.D, (e = launch_pdl(k_adaptive_place<DD>, gridPlace, 256, s, g)));
+    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+cudaError_t learned_judge(const MdasDeviceGrid& g, int L, int grid, cudaStream_t s) {
+    if (L == 0 || !g.learned || !g.priority) return cudaErrorInvalidValue;
+    k_learned_judge<<<grid, 256, 0, s>>>(g, L);
     return cudaGetLastError();
 }
 

@@ -20,6 +20,7 @@
 #include "mlp.h"
 
 #include <cuda_bf16.h>
+#include <float.h>
 
 namespace mdas_mlp {
 
@@ -282,62 +283,62 @@ __device__ __forceinline__ void put_features(const Ctx& c, const float (&f)[kIn]
 }
 
 // ---- features --------------------------------------------------------------------
-// Per leaf: log2 extents (image axes relative to the image), their mean, the
-// sample count, and log2(1 + x) of the mean and of the mean absolute deviation
-// of the sample values per channel.
+// Per leaf (16): log2 box extents of the first five dimensions (image axes
+// relative to the image; 0 past D) / 16; the sample count / 4; log2(1 + x) of
+// the samples' luminance mean, standard deviation, minimum and maximum; the
+// plain error log2(error) / 32; the depth (splits below the initial cell,
+// sum over dimensions of log2(initial extent / extent)) / 32; and the plain
+// errors of the four neighbouring leaf slots (slot +-1, +-2: initial cells in
+// Morton order, split children next to the children of neighbouring parents),
+// log2(error) / 32.
+__device__ __forceinline__ float log2_err(float e) { return log2f(fmaxf(e, 1e-30f)) * (1.0f / MDAS_MLP_TARGET_SCALE); }
+
 template <int D>
-__device__ void leaf_feats(const MdasDeviceGrid& g, int leaf, float (&f)[kIn], float* err) {
+__device__ void leaf_feats(const MdasDeviceGrid& g, int leaf, int L, float (&f)[kIn], float* err) {
     const float* nb = g.nb + (size_t)leaf * g.nbFloats;
     const int4 node = *reinterpret_cast<const int4*>(nb);
     float depth = 0.0f;
 #pragma unroll
-    for (int j = 0; j < 6; ++j) {
-        float l = 0.0f;
-        if (j < D) {
-            float e = nb[4 + D + j] - nb[4 + j];
-            if (j == 0) e /= g.scaleX;
-            if (j == 1) e /= g.scaleY;
-            l = log2f(fmaxf(e, 1e-30f));
-            depth += l;
-        }
-        f[j] = l * (1.0f / 16.0f);
+    for (int j = 0; j < D; ++j) {
+        float e = nb[4 + D + j] - nb[4 + j];
+        if (j == 0) e /= g.scaleX;
+        if (j == 1) e /= g.scaleY;
+        const float l = log2f(fmaxf(e, 1e-30f));
+        if (j < 5) f[j] = l * (1.0f / 16.0f);
+        depth += -(float)(g.bitsPerDim + (j < 2 ? g.extraImgBits : 0)) - l;
     }
-    f[6] = depth * (1.0f / (16.0f * D));
+#pragma unroll
+    for (int j = D; j < 5; ++j) f[j] = 0.0f;
     const int idx[4] = {node.x, node.y, node.z, node.w};
-    float v[4][3];
-    float mean[3] = {0.0f, 0.0f, 0.0f};
+    float lsum = 0.0f, lsq = 0.0f, lmin = FLT_MAX, lmax = -FLT_MAX;
     int n = 0;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         if (idx[i] >= 0) {
             const float* p = g.values + 3 * (size_t)idx[i];
-            v[i][0] = __ldg(p);
-            v[i][1] = __ldg(p + 1);
-            v[i][2] = __ldg(p + 2);
-            mean[0] += v[i][0];
-            mean[1] += v[i][1];
-            mean[2] += v[i][2];
+            const float lum = 0.2126f * __ldg(p) + 0.7152f * __ldg(p + 1) + 0.0722f * __ldg(p + 2);
+            lsum += lum;
+            lsq += lum * lum;
+            lmin = fminf(lmin, lum);
+            lmax = fmaxf(lmax, lum);
             ++n;
         }
     }
     const float inv = n ? 1.0f / (float)n : 0.0f;
-    float dev[3] = {0.0f, 0.0f, 0.0f};
+    const float mean = lsum * inv;
+    const float var = fmaxf(lsq * inv - mean * mean, 0.0f);
+    f[5] = (float)n * 0.25f;
+    f[6] = log2f(1.0f + fabsf(mean));
+    f[7] = log2f(1.0f + sqrtf(var));
+    f[8] = n ? log2f(1.0f + fabsf(lmin)) : 0.0f;
+    f[9] = n ? log2f(1.0f + fabsf(lmax)) : 0.0f;
+    const float e0 = g.errors[leaf];
+    f[10] = log2_err(e0);
+    f[11] = depth * (1.0f / 32.0f);
+    const int nbr[4] = {leaf - 2, leaf - 1, leaf + 1, leaf + 2};
 #pragma unroll
-    for (int c = 0; c < 3; ++c) mean[c] *= inv;
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-        if (idx[i] >= 0)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) dev[c] += fabsf(v[i][c] - mean[c]);
-    f[7] = (float)n * 0.25f;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        f[8 + c] = log2f(1.0f + fabsf(mean[c]));
-        f[11 + c] = log2f(1.0f + dev[c] * inv);
-    }
-    f[14] = 0.0f;
-    f[15] = 0.0f;
-    if (err) *err = g.errors[leaf];
+    for (int q = 0; q < 4; ++q) f[12 + q] = nbr[q] >= 0 && nbr[q] < L ? log2_err(g.errors[nbr[q]]) : f[10];
+    if (err) *err = e0;
 }
 
 __device__ __forceinline__ float target_of(float err) {
@@ -364,16 +365,27 @@ __global__ void __launch_bounds__(kThreads) k_forward_rows(const Packed* __restr
     ctx_close(c);
 }
 
+// Priority of leaves: the plain log2 error (feature 10) plus the network's
+// correction.  MODE 0: every leaf; 1: the leaves whose error the last errors
+// pass recomputed (the split children of the last adaptive pass: its split
+// list and the appended right children); 2: as 1, or every leaf before the
+// first adaptive pass.  Lhost < 0: the leaf count in the device counters.
 template <int D>
-__global__ void __launch_bounds__(kThreads) k_predict_leaves(MdasDeviceGrid g, int L, const Packed* __restrict__ w,
-                                                             float* __restrict__ pred, unsigned* status) {
+__global__ void __launch_bounds__(kThreads) k_predict_leaves(MdasDeviceGrid g, int Lhost, int mode,
+                                                             const Packed* __restrict__ w, float* __restrict__ pred,
+                                                             unsigned* status) {
     Ctx c;
     ctx_open(c, w, status);
-    const int tiles = (L + kRows - 1) / kRows;
+    const int L = Lhost >= 0 ? Lhost : g.counts->L;
+    const bool dirty = mode == 1 || (mode == 2 && g.counts->passes > 0);
+    const int newL = g.counts->newL;
+    const int rows = dirty ? 2 * newL : L;
+    const int tiles = (rows + kRows - 1) / kRows;
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const int r = tile * kRows + threadIdx.x;
+        const int leaf = !dirty ? r : (r < newL ? g.dirty[r] : (L - newL) + (r - newL));
         float f[kIn];
-        if (r < L) leaf_feats<D>(g, r, f, nullptr);
+        if (r < rows) leaf_feats<D>(g, leaf, L, f, nullptr);
         else
 #pragma unroll
             for (int i = 0; i < kIn; ++i) f[i] = 0.0f;
@@ -381,16 +393,27 @@ __global__ void __launch_bounds__(kThreads) k_predict_leaves(MdasDeviceGrid g, i
         float z2[kH];
         tile_forward(c, z2);
         const float p = head(c, z2);
-        if (r < L) pred[r] = p;
+        if (r < rows) pred[leaf] = f[10] + p;
     }
     ctx_close(c);
+}
+
+// The largest priority over all leaves (order-preserving bits into *out).
+__global__ void __launch_bounds__(256) k_priority_max(const MdasDeviceGrid g, int Lhost, const float* __restrict__ pred,
+                                                      unsigned* out) {
+    const int L = Lhost >= 0 ? Lhost : g.counts->L;
+    unsigned best = 0u;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x)
+        best = max(best, mdas_float_order(pred[i]));
+    best = __reduce_max_sync(0xffffffffu, best);
+    if ((threadIdx.x & 31) == 0 && best) atomicMax(out, best);
 }
 
 template <int D>
 __global__ void k_leaf_features(MdasDeviceGrid g, int L, float* __restrict__ out) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < L; r += gridDim.x * blockDim.x) {
         float f[kIn];
-        leaf_feats<D>(g, r, f, nullptr);
+        leaf_feats<D>(g, r, L, f, nullptr);
 #pragma unroll
         for (int i = 0; i < kIn; ++i) out[(size_t)r * kIn + i] = f[i];
     }
@@ -425,7 +448,7 @@ __global__ void __launch_bounds__(kThreads) k_gradients(const Packed* __restrict
     } else {
         const int leaf = (int)(((long long)offset + (long long)r * stride) % L);
         float err;
-        leaf_feats<D>(g, leaf, f, &err);
+        leaf_feats<D>(g, leaf, L, f, &err);
         y = target_of(err);
     }
     put_features(c, f);
@@ -602,17 +625,24 @@ cudaError_t forward(const Packed* w, const float* features, int m, float* pred, 
     return cudaGetLastError();
 }
 
-cudaError_t predict_leaves(const MdasDeviceGrid& g, int L, const Packed* w, float* pred, unsigned* status,
-                           cudaStream_t s) {
-    if (L <= 0) return cudaSuccess;
-    const int tiles = (L + kRows - 1) / kRows;
+cudaError_t predict_leaves(const MdasDeviceGrid& g, int L, int mode, const Packed* w, float* pred, unsigned* predMax,
+                           unsigned* status, cudaStream_t s) {
+    if (L == 0) return cudaSuccess;
+    const int tiles = L > 0 && mode == 0 ? (L + kRows - 1) / kRows : sm_count() * 4;
     const int grid = tiles < sm_count() * 4 ? tiles : sm_count() * 4;
     cudaError_t e = cudaSuccess;
     MLP_SWITCH_D(g.D, (e = set_smem(k_predict_leaves<DD>, kFwdSmem),
-                       e == cudaSuccess ? (k_predict_leaves<DD><<<grid, kThreads, kFwdSmem, s>>>(g, L, w, pred, status),
+                       e == cudaSuccess ? (k_predict_leaves<DD><<<grid, kThreads, kFwdSmem, s>>>(g, L, mode, w, pred,
+                                                                                               status),
                                            0)
                                         : 0));
-    return e != cudaSuccess ? e : cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (predMax) {
+        e = cudaMemsetAsync(predMax, 0, sizeof(unsigned), s);
+        if (e != cudaSuccess) return e;
+        k_priority_max<<<sm_count() * 4, 256, 0, s>>>(g, L, pred, predMax);
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t leaf_features(const MdasDeviceGrid& g, int L, float* features, cudaStream_t s) {

@@ -4,9 +4,13 @@
 //
 // No counterpart in the reference: the reference accepts a leaf with
 // probability powf(error / g_error, alpha) (kdgrid.cu:326).  In learned mode
-// the ratio comes from the MLP's predicted error instead, except on a fixed
-// hashed fraction of the leaves, which keep the plain error; the plain error is
-// also the training target, so it judges the model every pass.
+// the error is replaced by an estimate of the leaf's true reconstruction error:
+// the plain error times 2^(32 x the MLP's output), the network being trained
+// offline on log2(true error / plain error) / 32 against high-sample integrals
+// of the leaves; the ratio is that estimate over the largest one.  Every pass
+// a judge compares the plain errors each schedule would leave unrefined and
+// sends the pass back to the plain acceptance when the learned one leaves more
+// than (1 + tolerance) times the plain one's.
 #pragma once
 
 #include <stdint.h>
@@ -23,7 +27,7 @@
 #define MDAS_MLP_OFF_W3 (MDAS_MLP_OFF_B2 + MDAS_MLP_HIDDEN)
 #define MDAS_MLP_OFF_B3 (MDAS_MLP_OFF_W3 + MDAS_MLP_HIDDEN)
 #define MDAS_MLP_PARAMS (MDAS_MLP_OFF_B3 + 1)  // 5313
-// the target and the prediction are log2(error) / MDAS_MLP_TARGET_SCALE
+// priorities, network outputs and training targets are log2 quantities / MDAS_MLP_TARGET_SCALE
 #define MDAS_MLP_TARGET_SCALE 32.0f
 
 namespace mdas_mlp {
@@ -45,15 +49,19 @@ struct Packed {
 cudaError_t pack(const float* params, Packed* packed, cudaStream_t s);
 // pred[i] = MLP(features[i]) for m rows of 16 features (FP32, converted to BF16).
 cudaError_t forward(const Packed* w, const float* features, int m, float* pred, unsigned* status, cudaStream_t s);
-// Predictions for the grid's leaves [0, L) from their own features.
-cudaError_t predict_leaves(const MdasDeviceGrid& g, int L, const Packed* w, float* pred, unsigned* status,
-                           cudaStream_t s);
-// Features of the grid's leaves (for tests and callers that train elsewhere).
+// Priorities of the grid's leaves: log2(plain error) / 32 plus the network's
+// correction, for every leaf (mode 0), the leaves whose error the last errors
+// pass recomputed (1), or as 1 unless no adaptive pass ran yet (2); L < 0: the
+// leaf count in the device counters.  Then the largest priority over all
+// leaves into *predMax (order-preserving bits; skipped if null).
+cudaError_t predict_leaves(const MdasDeviceGrid& g, int L, int mode, const Packed* w, float* pred, unsigned* predMax,
+                           unsigned* status, cudaStream_t s);
+// Features of the grid's leaves (training data, tests).
 cudaError_t leaf_features(const MdasDeviceGrid& g, int L, float* features, cudaStream_t s);
 // Adds the gradients of the mean squared error over m rows to grads (FP32,
 // MDAS_MLP_PARAMS) and the sum of squared errors to *lossSum.  Rows come from
 // features/targets if given, else from the grid's leaves (row r = leaf
-// (offset + r * stride) % L, target = log2(error) / MDAS_MLP_TARGET_SCALE).
+// (offset + r * stride) % L, target = its plain log2(error) / MDAS_MLP_TARGET_SCALE).
 cudaError_t gradients(const Packed* w, const float* features, const float* targets, const MdasDeviceGrid* g, int L,
                       int offset, int stride, int m, float* grads, float* lossSum, unsigned* status, cudaStream_t s);
 // One Adam step (bias-corrected, step >= 1) on params with grads (zeroed

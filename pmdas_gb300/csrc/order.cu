@@ -290,21 +290,34 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(SweepArgs a) {
     st_relaxed(mine, (tile == 0 ? kFlagInclusive : kFlagAggregate) | count);
     unsigned exclusive = 0;
     if (tile > 0) {
+        // walk back over the predecessors' words, four per round trip: add
+        // aggregates until an inclusive prefix; re-poll from a word not yet published
         int t = tile - 1;
         int spins = 0;
-        while (t >= 0) {
-            const unsigned w = ld_relaxed(a.lookback + (size_t)t * kBins + b);
-            if ((w & ~kCountMask) == 0u) {
+        bool done = false;
+        while (!done && t >= 0) {
+            unsigned w[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                w[q] = t - q >= 0 ? ld_relaxed(a.lookback + (size_t)(t - q) * kBins + b) : kFlagInclusive;
+            int q = 0;
+            for (; q < 4; ++q) {
+                if ((w[q] & ~kCountMask) == 0u) break;
+                exclusive += w[q] & kCountMask;
+                if (w[q] & kFlagInclusive) {
+                    done = true;
+                    break;
+                }
+            }
+            if (done) break;
+            t -= q;
+            if (q < 4) {  // tile t has not published yet
                 if (++spins > kSpinLimit || ld_relaxed(a.status) != 0u) {
                     atomicOr(a.status, 1u);
                     break;
                 }
                 __nanosleep(20);
-                continue;
             }
-            exclusive += w & kCountMask;
-            if (w & kFlagInclusive) break;
-            --t;
         }
         st_relaxed(mine, kFlagInclusive | ((exclusive + count) & kCountMask));
     }

@@ -15,6 +15,10 @@
 cudaError_t mdas_launch_evaluate(const MdasScene& sc, const float* d_prims, const float* coords, float* values,
                                  int dim, const MdasCounts* counts, int offset, int count, int grid, cudaStream_t s);
 
+cudaError_t mdas_launch_leaf_true_errors(const MdasScene& sc, const float* d_prims, const MdasDeviceGrid& g,
+                                         const int* leaves, int L, int samples, unsigned long long seed, float* out,
+                                         cudaStream_t s);
+
 cudaError_t mdas_launch_reference_image(const MdasScene& sc, const float* d_prims, int width, int height, int strata,
                                         unsigned long long seed, double* out, int grid, cudaStream_t s);
 

@@ -250,21 +250,43 @@ class KDGrid:
         return out[:pts.shape[0]]
 
     # ---- learned acceptance (no reference counterpart)
-    def LearnedEnable(self, on: bool = True, **cfg):
-        """Learned mode on (fresh weights; keys: trainSteps, batch, learningRate, fallback, seed) or off."""
+    def LearnedEnable(self, on: bool = True, params=None, tolerance: float = 0.05, seed: int = 1):
+        """Learned mode on (trained `params`, MDAS_MLP_PARAMS floats, or seeded initial weights) or off."""
         if not on:
             N.check(self._lib.mdas_learned_enable(self._h, None), "learned_enable")
             return
         c = N.LearnedConfig()
         N.check(self._lib.mdas_learned_defaults(C.byref(c)), "learned_defaults")
-        for k, v in cfg.items():
-            setattr(c, k, v)
+        c.tolerance = tolerance
+        c.seed = seed
+        keep = None
+        if params is not None:
+            keep = np.ascontiguousarray(params, np.float32)
+            assert keep.size == N.MLP_PARAMS
+            c.params = keep.ctypes.data
         N.check(self._lib.mdas_learned_enable(self._h, C.byref(c)), "learned_enable")
 
-    def LearnedUpdate(self) -> float:
-        loss = C.c_float()
-        N.check(self._lib.mdas_learned_update(self._h, C.byref(loss)), "learned_update")
-        return loss.value
+    def LearnedUpdate(self):
+        """Predict every leaf and judge the pass (after ComputeErrors)."""
+        N.check(self._lib.mdas_learned_update(self._h), "learned_update")
+
+    def LearnedStats(self) -> dict:
+        j, p, lp, ul, up = C.c_int(), C.c_int(), C.c_int(), C.c_double(), C.c_double()
+        N.check(self._lib.mdas_learned_stats(self._h, C.byref(j), C.byref(p), C.byref(lp), C.byref(ul), C.byref(up)),
+                "stats")
+        return dict(judged=j.value, plain=p.value, last_plain=lp.value, unrefined_learned=ul.value,
+                    unrefined_plain=up.value)
+
+    def LeafTrueErrors(self, scene, samples: int = 64, seed: int = 1, leaves=None):
+        """Training targets: the true reconstruction error of every leaf, or of the
+        leaf slots in `leaves` (torch CUDA int32) -> torch CUDA float32."""
+        import torch
+        n = self.GetNumberOfNodes() if leaves is None else int(leaves.shape[0])
+        out = torch.empty(max(n, 1), dtype=torch.float32, device="cuda")
+        idx = None if leaves is None else leaves.contiguous()
+        N.check(self._lib.mdas_leaf_true_errors(self._h, scene.handle, samples, seed, _ptr(idx), n, _ptr(out)),
+                "leaf_true_errors")
+        return out[:n]
 
     def LearnedPredict(self):
         N.check(self._lib.mdas_learned_predict(self._h), "learned_predict")
@@ -302,6 +324,12 @@ def mlp_forward(params, features):
     out = torch.empty(max(m, 1), dtype=torch.float32, device="cuda")
     N.check(N.load().mdas_mlp_forward(_ptr(p), _ptr(f), m, _ptr(out), None), "mlp_forward")
     return out[:m]
+
+
+def mlp_adam(params, m1, m2, grads, step: int, lr: float):
+    """One Adam step on torch CUDA float32 [MDAS_MLP_PARAMS] tensors, in place (grads zeroed)."""
+    N.check(N.load().mdas_mlp_adam(_ptr(params), _ptr(m1), _ptr(m2), _ptr(grads), int(step), float(lr), None),
+            "mlp_adam")
 
 
 def mlp_gradients(params, features, targets):
