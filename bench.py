@@ -385,18 +385,28 @@ def order_block(grid, wl, peak: float, reps: int = 5) -> dict:
 
 
 def time_to_target(points, target):
-    """Wall time at which rel-MSE reaches `target`, interpolated log-log between the
-    two ladder points around it; None if the ladder never reaches it."""
+    """Wall time at which rel-MSE reaches `target`: interpolated log-log between the
+    two ladder points around it, or extrapolated from the last two points when the
+    ladder ends above it.  Returns (ms, how) or (None, None)."""
     import math
-    for (t0, e0), (t1, e1) in zip(points, points[1:]):
-        if e1 <= target < e0 or e0 <= target:
-            if e0 <= target:
-                return t0
-            f = (math.log(target) - math.log(e0)) / (math.log(e1) - math.log(e0))
-            return math.exp(math.log(t0) + f * (math.log(t1) - math.log(t0)))
-    if points and points[-1][1] <= target:
-        return points[-1][0]
-    return None
+
+    def loglog(p0, p1):
+        (t0, e0), (t1, e1) = p0, p1
+        if e1 == e0:
+            return None
+        f = (math.log(target) - math.log(e0)) / (math.log(e1) - math.log(e0))
+        return math.exp(math.log(t0) + f * (math.log(t1) - math.log(t0)))
+
+    if not points:
+        return None, None
+    if points[0][1] <= target:
+        return points[0][0], "measured"
+    for p0, p1 in zip(points, points[1:]):
+        if p1[1] <= target:
+            return loglog(p0, p1), "interpolated"
+    if len(points) >= 2 and points[-1][1] < points[-2][1]:
+        return loglog(points[-2], points[-1]), "extrapolated"
+    return None, None
 
 
 def learned_block(peaks: dict, ladder=(16, 32, 64, 128, 256, 512), target: float = 1e-3) -> dict:
@@ -450,8 +460,8 @@ def learned_block(peaks: dict, ladder=(16, 32, 64, 128, 256, 512), target: float
             g.close()
             if rel <= target:
                 break
-        t = time_to_target(pts, target)
-        out[mode] = {"ladder": rows, "ms_to_target": round(t, 3) if t else None}
+        t, how = time_to_target(pts, target)
+        out[mode] = {"ladder": rows, "ms_to_target": round(t, 3) if t else None, "to_target": how}
     tp, tl = out["plain"]["ms_to_target"], out["learned"]["ms_to_target"]
     out["learned_over_plain_time"] = round(tl / tp, 4) if tp and tl else None
     scene.close()

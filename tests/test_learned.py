@@ -226,19 +226,25 @@ def test_true_errors_match_oracle_integrand(cuda):
     assert np.allclose(got, want, rtol=1e-4, atol=1e-12)
 
 
-def test_constant_model_accepts_every_leaf(cuda):
+def test_constant_correction_is_the_plain_ranking(cuda):
+    """A network that outputs a constant leaves the plain ranking: the learned
+    ratio is error / max error up to rounding, so the pass accepts the same
+    leaves but for a few at the threshold, and the judge keeps it."""
     torch = cuda
-    g, sc = _grid(torch)
+    a, sa = _grid(torch)
+    b, sb = _grid(torch)
     p = np.zeros(N.MLP_PARAMS, np.float32)
-    p[OFF_B3] = -0.5  # every prediction equal: ratio 1 for every leaf
-    g.LearnedEnable(params=p)
-    g.InitialSampling()
-    sc.evaluate(g, 0, g.GetNumberOfSamples())
-    L = g.GetNumberOfNodes()
-    g.SamplingPass()
-    assert g.GetNewSamples() == L
-    s = g.LearnedStats()
-    assert s["judged"] == 1 and s["plain"] == 0 and s["unrefined_learned"] == 0.0 and s["unrefined_plain"] > 0
+    p[OFF_B3] = 0.1
+    a.LearnedEnable(params=p)
+    for g, sc in ((a, sa), (b, sb)):
+        g.InitialSampling()
+        sc.evaluate(g, 0, g.GetNumberOfSamples())
+        g.SamplingPass()
+    L = a.GetNumberOfNodes() - a.GetNewNodes()
+    assert abs(a.GetNewSamples() - b.GetNewSamples()) <= max(2, L // 200)
+    s = a.LearnedStats()
+    assert s["judged"] == 1 and s["last_plain"] == 0
+    assert abs(s["unrefined_learned"] - s["unrefined_plain"]) <= 0.01 * s["unrefined_plain"]
 
 
 def test_judge_matches_numpy(cuda):
