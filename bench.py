@@ -304,7 +304,10 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
                "ms_per_step": round(e2e_s * 1e3, 3), "includes": "integrand, host syncs per pass, copies"}
 
     order = None if args.no_order else order_block(grid, wl, peak)
-    learned = None if args.no_learned or world > 1 else learned_block(peaks)
+    learned = None
+    if not args.no_learned and world == 1:
+        learned = {"config2_single": learned_block(peaks, "mbdof1080"),
+                   "config4_batched": learned_block(peaks, "dl4k", batched=True, ladder=(16, 32, 64, 128))}
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -409,28 +412,31 @@ def time_to_target(points, target):
     return None, None
 
 
-def learned_block(peaks: dict, ladder=(16, 32, 64, 128, 256, 512), target: float = 1e-3) -> dict:
-    """Time to rel-MSE 1e-3, learned vs plain, on the learned workload (5-D motion
-    blur + depth of field, 1920x1080, evaluation scene seed 100): both render a
-    ladder of budgets through the device-side loop (integrand included) until the
-    image's rel-MSE against the FP64 4096-spp reference reaches the target."""
+def learned_block(peaks: dict, name: str = "mbdof1080", batched: bool = False,
+                  ladder=(16, 32, 64, 128, 256, 512), target: float = 1e-3) -> dict:
+    """Time to rel-MSE `target`, learned vs plain, on one workload (its scene seed
+    is the evaluation scene; the weights were trained on seeds 1-32): both render
+    a ladder of budgets until the image's rel-MSE against the FP64 4096-spp
+    reference reaches the target.  Plain renders use the device-side loop of one
+    image; learned renders use it too, or (batched) the batch API's graph."""
     import numpy as np
     import torch
 
     import pmdas_gb300 as P
     from pmdas_gb300.workloads import WORKLOADS
 
-    wl = WORKLOADS["mbdof1080"]
-    wpath = os.path.join(ROOT, "pmdas_gb300", "weights", "priority_mbdof1080.f32")
+    wl = WORKLOADS[name]
+    wpath = os.path.join(ROOT, "pmdas_gb300", "weights", f"priority_{name}.f32")
     if not os.path.exists(wpath):
-        return {"unavailable": "no trained weights (python -m pmdas_gb300.train_priority)"}
+        return {"unavailable": f"no trained weights for {name} (python -m pmdas_gb300.train_priority)"}
     params = np.fromfile(wpath, dtype="<f4")
     W, H = wl.width, wl.height
     scene = P.Scene(wl.scene_kind, wl.scene_seed, wl.scene_count, wl.scaleX, wl.scaleY, W, H)
     ref = scene.reference_image(W, H, spp=4096)
-    out = {"workload": f"{wl.name}: 5-D 1920x1080, scene seed {wl.scene_seed}, alpha {wl.alpha}",
+    out = {"workload": f"{wl.name}: {wl.dim}-D {W}x{H}, scene seed {wl.scene_seed}, alpha {wl.alpha}",
            "weights": os.path.relpath(wpath, ROOT), "target_rel_mse": target,
-           "timing": "device-side render loop (one CUDA graph), integrand included, CUDA events"}
+           "timing": "whole render on the device (one CUDA graph), integrand included, CUDA events",
+           "learned_path": "batch API (one image per batch)" if batched else "device-side loop of one grid"}
     pixels = torch.zeros(H, W, 4, device="cuda")
     for mode in ("plain", "learned"):
         pts, rows = [], []
@@ -439,12 +445,21 @@ def learned_block(peaks: dict, ladder=(16, 32, 64, 128, 256, 512), target: float
             ms_cap = min(max(budget * 3 // 2, 4 * wl.initial_leaves + 1), (1 << 30) - 1)
             g = P.KDGrid(wl.dim, ms_cap, wl.candidatesNum, wl.bitsPerDim, wl.extraImgBits, wl.alpha, wl.scaleX,
                          wl.scaleY)
+            batch = None
             if mode == "learned":
                 g.LearnedEnable(params=params)
-            P.render_graph(g, scene, budget, pixels, W, H)  # build + warm
+                if batched:
+                    batch = P.Batch([g], [scene], [budget], [pixels], [W], [H])
+
+            def render():
+                if batch is not None:
+                    return batch.render()[0]
+                return P.render_graph(g, scene, budget, pixels, W, H)
+
+            render()  # build + warm
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record()
-            st = P.render_graph(g, scene, budget, pixels, W, H)
+            st = render()
             b.record()
             torch.cuda.synchronize()
             ms = a.elapsed_time(b)
@@ -454,9 +469,11 @@ def learned_block(peaks: dict, ladder=(16, 32, 64, 128, 256, 512), target: float
                    "rel_mse": rel}
             if mode == "learned":
                 ls = g.LearnedStats()
-                row["passes_judged_plain"] = ls["plain"]
+                row["passes_judged_plain"] = ls["plain"] // 2  # two renders
             rows.append(row)
             pts.append((ms, rel))
+            if batch is not None:
+                batch.close()
             g.close()
             if rel <= target:
                 break

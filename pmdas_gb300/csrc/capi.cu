@@ -971,6 +971,8 @@ struct mdas_batch {
     cudaGraphExec_t exec = nullptr;
     int tune[4] = {4, 4, 4, 8};  // persistent CTAs per SM: errors, decide, place, integrate/integrand
     uint64_t launches = 0;
+    bool anyLearned = false;     // some image takes the learned acceptance
+    unsigned* status = nullptr;  // bounded waits of the batched learned kernels
 };
 
 namespace {
@@ -1032,6 +1034,13 @@ int build_batch_graph(mdas_batch* b) {
     cudaError_t eb = MDAS_ARITH_CALL(b, batch_reset, b->d_imgs, b->n, 0, bs);
     for (const auto& gr : b->groups)
         if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_errors, b->d_imgs + gr.offset, gr.count, gr.D, gErr, bs);
+    if (eb == cudaSuccess && b->anyLearned) {
+        // learned images: priorities of the leaves whose error was recomputed, then the judge
+        eb = MDAS_ARITH_CALL(b, batch_reset, b->d_imgs, b->n, 2, bs);
+        for (const auto& gr : b->groups)
+            if (eb == cudaSuccess) eb = mdas_mlp::batch_predict(b->d_imgs + gr.offset, gr.count, gr.D, b->status, bs);
+        if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_learned_judge, b->d_imgs, b->n, b->numSMs * 4, bs);
+    }
     if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_reset, b->d_imgs, b->n, 1, bs);
     for (const auto& gr : b->groups)
         if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_decide, b->d_imgs + gr.offset, gr.count, gr.D, gDec, bs);
@@ -1066,6 +1075,7 @@ void free_batch(mdas_batch* b) {
     if (b->bodyStream) cudaStreamDestroy(b->bodyStream);
     cudaFree(b->d_imgs);
     cudaFree(b->d_scenes);
+    cudaFree(b->status);
     delete b;
 }
 
@@ -1107,7 +1117,10 @@ int mdas_batch_create(mdas_batch** out, int n, mdas_grid* const* grids, mdas_sce
         }
         MdasBatchImage im{};
         im.g = g->dg;
-        im.g.priority = nullptr;  // batched renders use the plain acceptance
+        im.g.priority = g->learned ? g->lPred : nullptr;  // learned images keep their weights and statistics
+        im.g.learned = g->learned ? g->lStats : nullptr;
+        im.mlp = g->learned ? g->lPacked : nullptr;
+        if (g->learned) b->anyLearned = true;
         im.pixels = reinterpret_cast<float4*>(pixels[i]);
         im.width = widths[i];
         im.height = heights[i];
@@ -1138,6 +1151,8 @@ int mdas_batch_create(mdas_batch** out, int n, mdas_grid* const* grids, mdas_sce
                   cudaSuccess &&
               cudaMemcpy(b->d_scenes, b->hscenes.data(), sizeof(MdasBatchScene) * n, cudaMemcpyHostToDevice) ==
                   cudaSuccess &&
+              cudaMalloc(&b->status, sizeof(unsigned)) == cudaSuccess &&
+              cudaMemset(b->status, 0, sizeof(unsigned)) == cudaSuccess &&
               cudaStreamCreateWithFlags(&b->captureStream, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&b->bodyStream, cudaStreamNonBlocking) == cudaSuccess;
     if (!ok) {
@@ -1168,6 +1183,11 @@ int mdas_batch_render(mdas_batch* b, mdas_render_stats* stats) {
     if (e != cudaSuccess) return MDAS_ERR_CUDA;
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return MDAS_ERR_CUDA;
     int status = MDAS_OK;
+    if (b->anyLearned) {
+        unsigned st = 0;
+        if (cudaMemcpy(&st, b->status, sizeof(st), cudaMemcpyDeviceToHost) != cudaSuccess) return MDAS_ERR_CUDA;
+        if (st) status = MDAS_ERR_TIMEOUT;
+    }
     for (int i = 0; i < b->n; ++i) {
         mdas_grid* g = b->grids[i];
         const int rc = read_counts(g);

@@ -97,7 +97,7 @@ struct MdasBatchImage {
     int budget;
     int initialLeaves;
     unsigned jumpA, jumpC;  // LCG jump-ahead over the candidate draws of one accepted leaf
-    int pad[2];
+    const void* mlp;        // packed weights of a learned image (g.priority set), nullptr: plain acceptance
 };
 
 // Leaves per thread and per tile of the adaptive pass.
@@ -142,6 +142,7 @@ struct MdasBatchImage {
                                int maxPasses, cudaStream_t s);                                              \
     int max_blocks_per_sm(int D, int which);                                                                \
     cudaError_t learned_judge(const MdasDeviceGrid& g, int L, int grid, cudaStream_t s);                     \
+    cudaError_t batch_learned_judge(const MdasBatchImage* imgs, int n, int grid, cudaStream_t s);            \
     }
 
 MDAS_DECLARE_LAUNCHERS(mdas_fast)

@@ -183,19 +183,23 @@ __device__ __forceinline__ uint8_t* aligned_smem() {
     return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dyn) + 1023) & ~(uintptr_t)1023);
 }
 
+// weights: W1, W2, W2^T tiles and the vectors (Packed keeps them contiguous)
+__device__ __forceinline__ void copy_weights(uint8_t* sm, const Packed* w) {
+    const uint4* src = reinterpret_cast<const uint4*>(w);
+    uint4* dst = reinterpret_cast<uint4*>(sm + SM_W1);
+    constexpr int n16 = (int)(sizeof(Packed) / 16);
+    static_assert(sizeof(Packed) % 16 == 0, "Packed is copied in 16-byte pieces");
+    static_assert(SM_W1 + (int)sizeof(Packed) <= SM_BAR, "Packed fits before the barrier");
+    for (int i = threadIdx.x; i < n16; i += kThreads) dst[i] = src[i];
+}
+
 __device__ void ctx_open(Ctx& c, const Packed* w, unsigned* status) {
     c.sm = aligned_smem();
     c.base = smem_u32(c.sm);
     c.bar = c.base + SM_BAR;
     c.phase = 0;
     c.status = status;
-    // weights: W1, W2, W2^T tiles and the vectors (Packed keeps them contiguous)
-    const uint4* src = reinterpret_cast<const uint4*>(w);
-    uint4* dst = reinterpret_cast<uint4*>(c.sm + SM_W1);
-    constexpr int n16 = (int)(sizeof(Packed) / 16);
-    static_assert(sizeof(Packed) % 16 == 0, "Packed is copied in 16-byte pieces");
-    static_assert(SM_W1 + (int)sizeof(Packed) <= SM_BAR, "Packed fits before the barrier");
-    for (int i = threadIdx.x; i < n16; i += kThreads) dst[i] = src[i];
+    if (w) copy_weights(c.sm, w);
     if (threadIdx.x == 0) {
         mbar_init(c.bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -394,6 +398,64 @@ __global__ void __launch_bounds__(kThreads) k_predict_leaves(MdasDeviceGrid g, i
         tile_forward(c, z2);
         const float p = head(c, z2);
         if (r < rows) pred[leaf] = f[10] + p;
+    }
+    ctx_close(c);
+}
+
+// Batched: the learned images' priorities in one launch (one dimension).
+// Tiles of 128 rows are enumerated across the images (each image's rows as in
+// mode 2 above); a CTA reloads the weights when its tile belongs to an image
+// with other weights.
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_batch_predict(const MdasBatchImage* __restrict__ imgs, int n,
+                                                            unsigned* status) {
+    __shared__ int s_pre[257];
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int i = 0; i < n; ++i) {
+            s_pre[i] = acc;
+            const MdasCounts* cn = imgs[i].g.counts;
+            if (imgs[i].mlp && cn->active) acc += ((cn->passes > 0 ? 2 * cn->newL : cn->L) + kRows - 1) / kRows;
+        }
+        s_pre[n] = acc;
+    }
+    __syncthreads();
+    const int total = s_pre[n];
+    const Packed* loaded = nullptr;
+    Ctx c;
+    ctx_open(c, nullptr, status);
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        int lo = 0, hi = n - 1;  // the image whose tile range holds t
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_pre[mid] <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        const MdasBatchImage& im = imgs[lo];
+        const Packed* w = reinterpret_cast<const Packed*>(im.mlp);
+        if (w != loaded) {  // no MMA is in flight between tiles
+            __syncthreads();
+            copy_weights(c.sm, w);
+            __syncthreads();
+            loaded = w;
+        }
+        const MdasDeviceGrid& g = im.g;
+        const int L = g.counts->L;
+        const bool dirty = g.counts->passes > 0;
+        const int newL = g.counts->newL;
+        const int rows = dirty ? 2 * newL : L;
+        const int r = (t - s_pre[lo]) * kRows + threadIdx.x;
+        const int leaf = !dirty ? r : (r < newL ? g.dirty[r] : (L - newL) + (r - newL));
+        float f[kIn];
+        if (r < rows) leaf_feats<D>(g, leaf, L, f, nullptr);
+        else
+#pragma unroll
+            for (int i = 0; i < kIn; ++i) f[i] = 0.0f;
+        put_features(c, f);
+        float z2[kH];
+        tile_forward(c, z2);
+        const float p = head(c, z2);
+        if (r < rows) const_cast<float*>(g.priority)[leaf] = f[10] + p;
     }
     ctx_close(c);
 }
@@ -643,6 +705,15 @@ cudaError_t predict_leaves(const MdasDeviceGrid& g, int L, int mode, const Packe
         k_priority_max<<<sm_count() * 4, 256, 0, s>>>(g, L, pred, predMax);
     }
     return cudaGetLastError();
+}
+
+cudaError_t batch_predict(const MdasBatchImage* imgs, int n, int D, unsigned* status, cudaStream_t s) {
+    const int grid = sm_count() * 4;
+    cudaError_t e = cudaSuccess;
+    MLP_SWITCH_D(D, (e = set_smem(k_batch_predict<DD>, kFwdSmem),
+                     e == cudaSuccess ? (k_batch_predict<DD><<<grid, kThreads, kFwdSmem, s>>>(imgs, n, status), 0)
+                                      : 0));
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t leaf_features(const MdasDeviceGrid& g, int L, float* features, cudaStream_t s) {

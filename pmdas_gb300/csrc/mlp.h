@@ -56,6 +56,9 @@ cudaError_t forward(const Packed* w, const float* features, int m, float* pred, 
 // leaves into *predMax (order-preserving bits; skipped if null).
 cudaError_t predict_leaves(const MdasDeviceGrid& g, int L, int mode, const Packed* w, float* pred, unsigned* predMax,
                            unsigned* status, cudaStream_t s);
+// Batched: the priorities of the active learned images of a batch (all of one
+// dimension D), each image's rows as predict_leaves mode 2.
+cudaError_t batch_predict(const MdasBatchImage* imgs, int n, int D, unsigned* status, cudaStream_t s);
 // Features of the grid's leaves (training data, tests).
 cudaError_t leaf_features(const MdasDeviceGrid& g, int L, float* features, cudaStream_t s);
 // Adds the gradients of the mean squared error over m rows to grads (FP32,

@@ -298,3 +298,50 @@ def test_learned_graph_render_equals_host_loop(cuda, arith):
         assert np.array_equal(x[k].view(np.uint8), y[k].view(np.uint8)), k
     assert a.Validate() and b.Validate()
     assert a.LearnedStats()["judged"] == b.LearnedStats()["judged"] > 0
+
+
+@pytest.mark.parametrize("arith", [P.ARITH_REFERENCE, P.ARITH_IEEE])
+def test_learned_batch_equals_single_renders(cuda, arith):
+    """Learned and plain images of different dimension in one batch: every image
+    ends exactly as its own device-side render (learned ones with their own
+    predictions and judge), over two renders of the batch."""
+    torch = cuda
+    from tests.parity import assert_states_equal, rel_close
+    specs = [  # (kind, D, W, H, spp, learned weights seed or None)
+        (P.SCENE_DISCS_MB, 3, 64, 48, 8, 5),
+        (P.SCENE_DISCS_DOF, 4, 96, 64, 16, 6),
+        (P.SCENE_DISCS_MBDOF, 5, 48, 40, 12, 7),
+        (P.SCENE_DISCS_DOF, 4, 80, 56, 8, None),
+    ]
+    grids, scenes, pix, budgets, singles = [], [], [], [], []
+    for kind, D, W, H_, spp, wseed in specs:
+        budget = spp * W * H_
+        eib = 3 if D < 5 else 2
+        ms = 2 * budget + 8 * ((1 << D) << (2 * eib))
+        sc = P.Scene(kind, 20 + D, 32, W, H_, W, H_)
+        made = []
+        for _ in range(2):
+            g = P.KDGrid(D, ms, 4, 1, eib, 0.25, W, H_, arith=arith)
+            if wseed is not None:
+                g.LearnedEnable(seed=wseed)
+            made.append(g)
+        rpx = torch.zeros(H_, W, 4, device="cuda")
+        st = P.render_graph(made[0], sc, budget, rpx, W, H_)
+        singles.append((made[0].dump_state(), rpx.cpu().numpy(), st.passes,
+                        made[0].LearnedStats()["judged"] if wseed is not None else 0))
+        grids.append(made[1])
+        scenes.append(sc)
+        pix.append(torch.zeros(H_, W, 4, device="cuda"))
+        budgets.append(budget)
+    batch = P.Batch(grids, scenes, budgets, pix, [sp[2] for sp in specs], [sp[3] for sp in specs])
+    for rnd in range(2):
+        stats = batch.render()
+        for i, (want, img, passes, judged) in enumerate(singles):
+            assert stats[i].passes == passes, (rnd, i)
+            assert_states_equal(grids[i].dump_state(), want,
+                                keys=("coords", "values", "nodes", "boxes", "errors", "seeds"), what=f"image {i}")
+            ok, worst = rel_close(pix[i].cpu().numpy(), img)
+            assert ok, (i, worst)
+            if specs[i][5] is not None:
+                assert grids[i].LearnedStats()["judged"] == (rnd + 1) * judged
+    batch.close()
