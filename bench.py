@@ -307,7 +307,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     learned = None
     if not args.no_learned and world == 1:
         learned = {"config2_single": learned_block(peaks, "mbdof1080"),
-                   "config4_batched": learned_block(peaks, "dl4k", batched=True, ladder=(16, 32, 64, 128))}
+                   "config4_batched": learned_block(peaks, "dl4k", batched=True, ladder=(1, 2, 4, 8, 16, 32, 64),
+                                                    target=1e-4)}
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -121,72 +121,74 @@ __global__ void k_batch_reset(const MdasBatchImage* __restrict__ imgs, int n, in
     }
 }
 
-// ---- learned images: the largest priority and the judge, chunks of 256 leaves
-// across the active learned images; the last chunk of an image sets its verdict.
-__global__ void __launch_bounds__(256) k_batch_learned_judge(const MdasBatchImage* __restrict__ imgs, int n,
-                                                             int phase) {
-    __shared__ int s_pre[MDAS_MAX_BATCH + 1];
-    __shared__ unsigned s_warp[8];
-    __shared__ double s_l[8], s_p[8];
-    __shared__ bool s_last;
-    const int total = batch_prefix(n, s_pre, s_warp, [&](int i) {
-        return imgs[i].mlp && imgs[i].g.counts->active ? ceil_div(imgs[i].g.counts->L, 256) : 0;
-    });
-    for (int ch = blockIdx.x; ch < total; ch += gridDim.x) {
-        const int img = batch_image_of(s_pre, n, ch);
-        const MdasDeviceGrid& g = imgs[img].g;
-        const int L = g.counts->L;
-        const int i = (ch - s_pre[img]) * 256 + threadIdx.x;
-        MdasLearnedStats* st = g.learned;
-        if (phase == 0) {  // the largest priority
-            unsigned best = i < L ? mdas_float_order(g.priority[i]) : 0u;
-            best = __reduce_max_sync(0xffffffffu, best);
-            if ((threadIdx.x & 31) == 0 && best) atomicMax(&st->predMax, best);
-            continue;
-        }
-        double ul = 0.0, up = 0.0;
-        if (i < L) {
-            const float gError = __uint_as_float(g.counts->gerr);
-            const float predMax = mdas_float_unorder(st->predMax);
-            const float e = g.errors[i];
-            unsigned seed = g.seeds[i];
-            if (seed == 0) seed = tea4((unsigned)i, 0);
-            const float r = rnd(seed);
-            if (!(mdas_pow(e / gError, g.alpha) >= r)) up = (double)e;
-            if (!(mdas_pow(learned_ratio(g, i, predMax), g.alpha) >= r)) ul = (double)e;
-        }
+// ---- learned images: the largest priority (phase 0), then the plain errors
+// each schedule leaves unrefined (phase 1), over chunks of 256 leaves across the
+// active learned images.  A block keeps its partial results while its chunks
+// stay in one image and adds them to that image's statistics when it moves on
+// (a few atomics per block and image); the verdicts follow in k_batch_verdict.
+__device__ __forceinline__ void flush_learned(MdasLearnedStats* st, int phase, unsigned best, double ul, double up) {
+    if (phase == 0) {
+        best = __reduce_max_sync(0xffffffffu, best);
+        if ((threadIdx.x & 31) == 0 && best) atomicMax(&st->predMax, best);
+    } else {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             ul += __shfl_xor_sync(0xffffffffu, ul, o);
             up += __shfl_xor_sync(0xffffffffu, up, o);
         }
         if ((threadIdx.x & 31) == 0) {
-            s_l[threadIdx.x >> 5] = ul;
-            s_p[threadIdx.x >> 5] = up;
+            if (ul != 0.0) atomicAdd(&st->unrefinedLearned, ul);
+            if (up != 0.0) atomicAdd(&st->unrefinedPlain, up);
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double a = 0.0, b = 0.0;
-            for (int w = 0; w < 8; ++w) {
-                a += s_l[w];
-                b += s_p[w];
-            }
-            atomicAdd(&st->unrefinedLearned, a);
-            atomicAdd(&st->unrefinedPlain, b);
-            __threadfence();
-            s_last = atomicAdd(&st->blocksDone, 1u) == (unsigned)(s_pre[img + 1] - s_pre[img]) - 1u;
-            if (s_last) {
-                __threadfence();
-                const double A = atomicAdd(&st->unrefinedLearned, 0.0), B = atomicAdd(&st->unrefinedPlain, 0.0);
-                const int revert = A > (1.0 + (double)st->tolerance) * B ? 1 : 0;
-                st->usePlain = revert;
-                st->plainPasses += revert;
-                st->judgedPasses += 1;
-                st->blocksDone = 0;
-            }
-        }
-        __syncthreads();
     }
+}
+
+__global__ void __launch_bounds__(256) k_batch_learned_reduce(const MdasBatchImage* __restrict__ imgs, int n,
+                                                              int phase) {
+    __shared__ int s_pre[MDAS_MAX_BATCH + 1];
+    __shared__ unsigned s_warp[8];
+    const int total = batch_prefix(n, s_pre, s_warp, [&](int i) {
+        return imgs[i].mlp && imgs[i].g.counts->active ? ceil_div(imgs[i].g.counts->L, 256) : 0;
+    });
+    int cur = -1;  // the image the block's partial results belong to (uniform across the block)
+    unsigned best = 0u;
+    double ul = 0.0, up = 0.0;
+    for (int ch = blockIdx.x; ch < total; ch += gridDim.x) {
+        const int img = batch_image_of(s_pre, n, ch);
+        if (img != cur) {
+            if (cur >= 0) flush_learned(imgs[cur].g.learned, phase, best, ul, up);
+            cur = img;
+            best = 0u;
+            ul = up = 0.0;
+        }
+        const MdasDeviceGrid& g = imgs[img].g;
+        const int i = (ch - s_pre[img]) * 256 + threadIdx.x;
+        if (i >= g.counts->L) continue;
+        if (phase == 0) {
+            best = max(best, mdas_float_order(g.priority[i]));
+            continue;
+        }
+        const float gError = __uint_as_float(g.counts->gerr);
+        const float predMax = mdas_float_unorder(g.learned->predMax);
+        const float e = g.errors[i];
+        unsigned seed = g.seeds[i];
+        if (seed == 0) seed = tea4((unsigned)i, 0);
+        const float r = rnd(seed);
+        if (!(mdas_pow(e / gError, g.alpha) >= r)) up += (double)e;
+        if (!(mdas_pow(learned_ratio(g, i, predMax), g.alpha) >= r)) ul += (double)e;
+    }
+    if (cur >= 0) flush_learned(imgs[cur].g.learned, phase, best, ul, up);
+}
+
+// One thread per image: the verdict of a learned image's pass.
+__global__ void k_batch_verdict(const MdasBatchImage* __restrict__ imgs, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !imgs[i].mlp || !imgs[i].g.counts->active) return;
+    MdasLearnedStats* st = imgs[i].g.learned;
+    const int revert = st->unrefinedLearned > (1.0 + (double)st->tolerance) * st->unrefinedPlain ? 1 : 0;
+    st->usePlain = revert;
+    st->plainPasses += revert;
+    st->judgedPasses += 1;
 }
 
 // ---- errors: full on an image's first pass, its split children after
@@ -376,8 +378,9 @@ cudaError_t batch_reset(const MdasBatchImage* imgs, int n, int which, cudaStream
 }
 
 cudaError_t batch_learned_judge(const MdasBatchImage* imgs, int n, int grid, cudaStream_t s) {
-    k_batch_learned_judge<<<grid, 256, 0, s>>>(imgs, n, 0);  // the largest priority of every image first
-    k_batch_learned_judge<<<grid, 256, 0, s>>>(imgs, n, 1);
+    k_batch_learned_reduce<<<grid, 256, 0, s>>>(imgs, n, 0);  // the largest priority of every image first
+    k_batch_learned_reduce<<<grid, 256, 0, s>>>(imgs, n, 1);
+    k_batch_verdict<<<(n + 255) / 256, 256, 0, s>>>(imgs, n);
     return cudaGetLastError();
 }
 
