@@ -51,7 +51,9 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-quality", action="store_true")
     ap.add_argument("--no-order", action="store_true", help="skip the leaf-order / hierarchy / locate timings")
-    ap.add_argument("--no-learned", action="store_true", help="skip the learned-acceptance render")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain comparison")
+    ap.add_argument("--learned-host", action="store_true",
+                    help="render the learned-vs-plain ladders through the host loop (mdas_render) instead of graphs")
     return ap.parse_args()
 
 
@@ -306,9 +308,10 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     order = None if args.no_order else order_block(grid, wl, peak)
     learned = None
     if not args.no_learned and world == 1:
-        learned = {"config2_single": learned_block(peaks, "mbdof1080"),
-                   "config4_batched": learned_block(peaks, "dl4k", batched=True, ladder=(1, 2, 4, 8, 16, 32, 64),
-                                                    target=1e-4)}
+        learned = {"config2_single": learned_block(peaks, "mbdof1080", host=args.learned_host),
+                   "config4_batched": learned_block(peaks, "dl4k", batched=not args.learned_host,
+                                                    ladder=(1, 2, 4, 8, 16, 32, 64), target=1e-4,
+                                                    host=args.learned_host)}
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -414,7 +417,7 @@ def time_to_target(points, target):
 
 
 def learned_block(peaks: dict, name: str = "mbdof1080", batched: bool = False,
-                  ladder=(16, 32, 64, 128, 256, 512), target: float = 1e-3) -> dict:
+                  ladder=(16, 32, 64, 128, 256, 512), target: float = 1e-3, host: bool = False) -> dict:
     """Time to rel-MSE `target`, learned vs plain, on one workload (its scene seed
     is the evaluation scene; the weights were trained on seeds 1-32): both render
     a ladder of budgets until the image's rel-MSE against the FP64 4096-spp
@@ -436,8 +439,10 @@ def learned_block(peaks: dict, name: str = "mbdof1080", batched: bool = False,
     ref = scene.reference_image(W, H, spp=4096)
     out = {"workload": f"{wl.name}: {wl.dim}-D {W}x{H}, scene seed {wl.scene_seed}, alpha {wl.alpha}",
            "weights": os.path.relpath(wpath, ROOT), "target_rel_mse": target,
-           "timing": "whole render on the device (one CUDA graph), integrand included, CUDA events",
-           "learned_path": "batch API (one image per batch)" if batched else "device-side loop of one grid"}
+           "timing": ("host loop (mdas_render)" if host else "whole render on the device (one CUDA graph)") +
+                     ", integrand included, CUDA events",
+           "learned_path": "batch API (one image per batch)" if batched else
+                           ("host loop of one grid" if host else "device-side loop of one grid")}
     pixels = torch.zeros(H, W, 4, device="cuda")
     for mode in ("plain", "learned"):
         pts, rows = [], []
@@ -455,6 +460,8 @@ def learned_block(peaks: dict, name: str = "mbdof1080", batched: bool = False,
             def render():
                 if batch is not None:
                     return batch.render()[0]
+                if host:
+                    return P.render(g, scene, budget, pixels, W, H)
                 return P.render_graph(g, scene, budget, pixels, W, H)
 
             render()  # build + warm

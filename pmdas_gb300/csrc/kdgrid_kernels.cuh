@@ -500,6 +500,38 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
         for (int j = 0; j < K; ++j)
             if (i0 + j < L) g.seeds[i0 + j] = sd[j];
     }
+    // The accepted leaves' new sample counts (an append adds one, a split leaves
+    // 2 in the left child) and the split leaves' error (-1: recompute), written
+    // here as whole vectors instead of by place at scattered slots.
+    if (accMask) {
+        unsigned c8[2] = {0u, 0u};
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            const unsigned nc = ((splitMask >> j) & 1u) ? 2u : (unsigned)(lc[j] + (int)((accMask >> j) & 1u));
+            c8[j >> 2] |= nc << (8 * (j & 3));
+        }
+        if (full) {
+            *reinterpret_cast<uint2*>(g.leafCounts + i0) = make_uint2(c8[0], c8[1]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < K; ++j)
+                if (i0 + j < L) g.leafCounts[i0 + j] = (unsigned char)((c8[j >> 2] >> (8 * (j & 3))) & 0xffu);
+        }
+    }
+    if (splitMask) {
+#pragma unroll
+        for (int j = 0; j < K; ++j)
+            if ((splitMask >> j) & 1u) err[j] = -1.0f;
+        if (full) {
+#pragma unroll
+            for (int q = 0; q < K; q += 4)
+                *reinterpret_cast<float4*>(g.errors + i0 + q) = make_float4(err[q], err[q + 1], err[q + 2], err[q + 3]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < K; ++j)
+                if (i0 + j < L && ((splitMask >> j) & 1u)) g.errors[i0 + j] = -1.0f;
+        }
+    }
 
     // block scan of (accepted, split) counts, packed lo16 | hi16
     const unsigned flag = (unsigned)__popc(accMask) | ((unsigned)__popc(splitMask) << 16);
@@ -700,8 +732,7 @@ __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, i
         else if (sampleCount == 2) node.z = sampleIndex;
         else node.w = sampleIndex;
         nb_set_node(nb, node);
-        store_point<D>(sc + sampleCount * D, best);
-        g.leafCounts[nodeIndex] = (unsigned char)(sampleCount + 1);
+        store_point<D>(sc + sampleCount * D, best);  // (decide wrote the new count)
     } else {
         // split dimension: AABB::LargestAxis, ties to the highest index (aabb.h:34-45)
         int axis = -1;
@@ -771,9 +802,8 @@ __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, i
             if (k < 4) store_point<D>(dst, samples[k < 4 ? k : 0]);
             else store_point<D>(dst, best);
         }
-        g.errors[nodeIndex] = -1.0f;
+        // (decide wrote the left child's error -1 and count 2)
         g.errors[nodeOffset] = -1.0f;
-        g.leafCounts[nodeIndex] = 2;
         g.leafCounts[nodeOffset] = 3;
         // a new slot starts without a seed: the reference's seed buffer is zeroed
         // once at InitialSampling (kdgrid.cu:637) and right-child slots are never
