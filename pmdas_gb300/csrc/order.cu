@@ -165,6 +165,10 @@ constexpr unsigned kFlagInclusive = 2u << 30;
 constexpr unsigned kCountMask = (1u << 30) - 1u;
 constexpr int kSpinLimit = 1 << 18;  // polls of one look-back word before giving up
 constexpr int kMaxPasses = 8;
+#ifndef MDAS_SORT_WINDOW
+#define MDAS_SORT_WINDOW 4
+#endif
+constexpr int kWindow = MDAS_SORT_WINDOW;  // predecessor words read per look-back round trip
 
 __device__ __forceinline__ unsigned ld_relaxed(const unsigned* p) {
     unsigned v;
@@ -296,12 +300,12 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(SweepArgs a) {
         int spins = 0;
         bool done = false;
         while (!done && t >= 0) {
-            unsigned w[4];
+            unsigned w[kWindow];
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
+            for (int q = 0; q < kWindow; ++q)
                 w[q] = t - q >= 0 ? ld_relaxed(a.lookback + (size_t)(t - q) * kBins + b) : kFlagInclusive;
             int q = 0;
-            for (; q < 4; ++q) {
+            for (; q < kWindow; ++q) {
                 if ((w[q] & ~kCountMask) == 0u) break;
                 exclusive += w[q] & kCountMask;
                 if (w[q] & kFlagInclusive) {
@@ -311,7 +315,7 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(SweepArgs a) {
             }
             if (done) break;
             t -= q;
-            if (q < 4) {  // tile t has not published yet
+            if (q < kWindow) {  // tile t has not published yet
                 if (++spins > kSpinLimit || ld_relaxed(a.status) != 0u) {
                     atomicOr(a.status, 1u);
                     break;
