@@ -108,6 +108,18 @@ class ClockSampler:
 
 
 # ---- traffic accounting -------------------------------------------------------------
+# DRAM traffic of the dominant stage per pass, from the committed ncu capture of
+# every launch (dram__bytes_read.sum + dram__bytes_write.sum, mean per pass of
+# decide + scan + place): profiles/kernels_dram_dof1024.md
+MEASURED_TRAFFIC = {"dof1024": (207.0e6, "profiles/kernels_dram_dof1024.md (ncu: decide 27.7 + scan 0.0 + place "
+                                         "179.3 MB, mean per pass)")}
+
+
+def workload_label(wl) -> str:
+    return (f"{wl.name}: {wl.dim}-D {wl.width}x{wl.height}, {wl.spp:g} spp, bitsPerDim {wl.bitsPerDim}, "
+            f"extraImgBits {wl.extraImgBits}, alpha {wl.alpha}, {wl.candidatesNum} candidates, {wl.scene_count} discs")
+
+
 def stage_bytes(D: int, W: int, H: int, L0: int, passes: list, N_final: int, L_final: int) -> dict:
     """Algorithmic (compulsory) DRAM bytes of each stage over one render.
 
@@ -317,9 +329,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(mdas_ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded analytic integrand)",
-        "config": {"workload": f"{wl.name}: {D}-D {W}x{H}, {wl.spp:g} spp, bitsPerDim {wl.bitsPerDim}, "
-                               f"extraImgBits {wl.extraImgBits}, alpha {wl.alpha}, {wl.candidatesNum} candidates, "
-                               f"{wl.scene_count} discs",
+        "config": {"workload": workload_label(wl),
                    "final_samples": n_final, "final_leaves": l_final, "initial_leaves": L0,
                    "passes": len(passes), "maxSamples": wl.maxSamples, "arith": "reference (fast-math)",
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
@@ -328,7 +338,10 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         "wall_ms_per_step": round(wall_ms / args.steps, 3),
         "graph_render_ms": round(graph_ms, 3) if graph_ms else None,
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": MEASURED_TRAFFIC[wl.name][0] if dom == 2 and wl.name in MEASURED_TRAFFIC else None,
+                     "traffic_source": MEASURED_TRAFFIC[wl.name][1] if dom == 2 and wl.name in MEASURED_TRAFFIC
+                     else None,
                      "algorithmic_bytes_per_launch": int(per_launch_bytes), "launches_per_step": launches_of,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s",
                      "all_stages_gbs": round(overall_gbs, 1)},
@@ -569,6 +582,7 @@ def cpu_baseline(wl, threads: int, budget_s: float = 30.0) -> dict:
                                         threads=threads)
     mdas_s = sum(t[:4]) / 1e3
     return {"value": round(n / mdas_s / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "mdas_ms": round(mdas_s * 1e3, 1),
             "sample": f"one full {wl.name} render ({n} samples, {passes} passes); integrand "
                       f"{t[4] / 1e3:.2f} s excluded", "wall_s": round(wall, 2)}
 
@@ -632,9 +646,11 @@ def run_reference_arm(args):
     value = statistics.median(v["value"] for v in vals)
     n = vals[0]
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": statistics.median(v["mdas_ms"] for v in vals),
+            "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded analytic integrand)", "impl": "reference",
-            "config": {"workload": wl.name},
+            "config": {"workload": workload_label(wl), "maxSamples": wl.maxSamples,
+                       "arith": "strict IEEE binary32 CPU restatement (oracle)", "parallelism": f"{threads} host threads"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": n["sample"]},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
