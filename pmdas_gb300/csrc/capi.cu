@@ -248,6 +248,14 @@ int scene_upload(mdas_scene* s, cudaStream_t stream) {
     if (!s->prims.empty() && cudaMemcpyAsync(s->d_prims, s->prims.data(), sizeof(float) * s->prims.size(),
                                              cudaMemcpyHostToDevice, stream) != cudaSuccess)
         return MDAS_ERR_CUDA;
+    const size_t cullWords = mdas_cull_words(s->desc);
+    if (cullWords) {
+        if (cudaMalloc(&s->d_cull, sizeof(unsigned) * cullWords) != cudaSuccess) {
+            s->d_cull = nullptr;
+            return MDAS_ERR_ALLOC;
+        }
+        if (mdas_launch_build_cull(s->desc, s->d_prims, s->d_cull, stream) != cudaSuccess) return MDAS_ERR_CUDA;
+    }
     return cudaStreamSynchronize(stream) == cudaSuccess ? MDAS_OK : MDAS_ERR_CUDA;
 }
 
@@ -704,6 +712,7 @@ int mdas_scene_create(mdas_scene** out, int kind, uint64_t seed, int count, floa
 int mdas_scene_destroy(mdas_scene* s) {
     if (!s) return MDAS_ERR_INVALID;
     if (s->d_prims) cudaFree(s->d_prims);
+    if (s->d_cull) cudaFree(s->d_cull);
     delete s;
     return MDAS_OK;
 }
@@ -734,7 +743,7 @@ int mdas_evaluate(mdas_grid* g, mdas_scene* s, int offset, int count) {
     int rc = scene_upload(s, g->stream);
     if (rc) return rc;
     rc = timed(g, 4, [&]() {
-        return mdas_launch_evaluate(s->desc, s->d_prims, g->dg.coords, g->dg.values, g->dg.D,
+        return mdas_launch_evaluate(s->desc, s->d_prims, s->d_cull, g->dg.coords, g->dg.values, g->dg.D,
                                     count < 0 ? g->dg.counts : nullptr, offset, count, grid, g->stream);
     });
     g->launches += 1;
@@ -753,8 +762,8 @@ int mdas_scene_evaluate(mdas_scene* s, const float* coords, float* values, int d
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int64_t want = ((int64_t)count + 255) / 256;
     const int grid = (int)(want < (int64_t)nsm * 8 ? want : (int64_t)nsm * 8);
-    return status_of(mdas_launch_evaluate(s->desc, s->d_prims, coords, values, dim, nullptr, offset, count, grid,
-                                          (cudaStream_t)stream));
+    return status_of(mdas_launch_evaluate(s->desc, s->d_prims, s->d_cull, coords, values, dim, nullptr, offset, count,
+                                          grid, (cudaStream_t)stream));
 }
 
 int mdas_scene_reference_image(mdas_scene* s, int width, int height, int spp, uint64_t seed, double* out,
@@ -858,7 +867,7 @@ int build_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, i
                                     : mdas_fast::initial_sampling(d, (int)L0, cs);
     if (e != cudaSuccess) return fail(e);
     k_set_counts<<<1, 1, 0, cs>>>(d.counts, (int)N0, (int)L0);
-    e = mdas_launch_evaluate(s->desc, s->d_prims, d.coords, d.values, d.D, nullptr, 0, (int)N0, gEval, cs);
+    e = mdas_launch_evaluate(s->desc, s->d_prims, s->d_cull, d.coords, d.values, d.D, nullptr, 0, (int)N0, gEval, cs);
     if (e != cudaSuccess) return fail(e);
     // the conditional while node
     cudaStreamCaptureStatus status;
@@ -892,7 +901,7 @@ int build_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, i
     if (eb == cudaSuccess) eb = launch_adaptive_on(g, gDecide, gPlace, bs);
     g->dg.priority = nullptr;
     if (eb == cudaSuccess)
-        eb = mdas_launch_evaluate(s->desc, s->d_prims, d.coords, d.values, d.D, d.counts, 0, 0, gEval, bs);
+        eb = mdas_launch_evaluate(s->desc, s->d_prims, s->d_cull, d.coords, d.values, d.D, d.counts, 0, 0, gEval, bs);
     if (eb == cudaSuccess)
         eb = g->arith == MDAS_ARITH_IEEE ? mdas_ieee::loop_condition(d, handle, budget, kMaxGraphPasses, bs)
                                          : mdas_fast::loop_condition(d, handle, budget, kMaxGraphPasses, bs);
@@ -1138,6 +1147,7 @@ int mdas_batch_create(mdas_batch** out, int n, mdas_grid* const* grids, mdas_sce
         MdasBatchScene bs{};
         bs.sc = scenes[i]->desc;
         bs.prims = scenes[i]->d_prims;
+        bs.cull = scenes[i]->d_cull;
         bs.counts = g->dg.counts;
         bs.coords = g->dg.coords;
         bs.values = g->dg.values;
@@ -1257,8 +1267,9 @@ int mdas_render_host(mdas_grid* g, mdas_scene* s, const float* hostPrims, int bu
     rc = scene_upload(s, g->stream);
     if (rc) return rc;
     if (hostPrims && s->desc.count > 0) {
-        const cudaError_t e = cudaMemcpyAsync(s->d_prims, hostPrims, sizeof(float) * MDAS_PRIM_STRIDE * s->desc.count,
-                                              cudaMemcpyHostToDevice, g->stream);
+        cudaError_t e = cudaMemcpyAsync(s->d_prims, hostPrims, sizeof(float) * MDAS_PRIM_STRIDE * s->desc.count,
+                                        cudaMemcpyHostToDevice, g->stream);
+        if (e == cudaSuccess) e = mdas_launch_build_cull(s->desc, s->d_prims, s->d_cull, g->stream);  // new primitives
         if (e != cudaSuccess) return MDAS_ERR_CUDA;
     }
     rc = mdas_render_graph(g, s, budget, g->scratch, width, height, stats);

@@ -16,14 +16,140 @@
 
 namespace {
 
+// ---- disc culling ---------------------------------------------------------------------
+__host__ __device__ inline bool mdas_culled_kind(int kind) {
+    return kind == MDAS_SCENE_DISCS_MB || kind == MDAS_SCENE_DISCS_DOF || kind == MDAS_SCENE_DISCS_MBDOF;
+}
+
+// Can disc p cover a sample whose image point lies in [x0, x1] x [y0, y1] (in
+// [0, 1] image units)?  Motion blur: the disc's centre sweeps the box between
+// its positions at t = 0 and t = 1.  Depth of field: the ray meets the disc's
+// plane at s * focal * (nx * filmHalfW, ny * filmHalfH) + (1 - s) * lens point,
+// s = depth / focal, |lens point| <= lensRadius.  So the disc can be hit only
+// if the distance between those two boxes is within r (+ |1 - s| * lensRadius).
+// NaNs keep the disc (only a certain miss drops it).
+__device__ bool cull_may_cover(const MdasScene& sc, const float* p, float x0, float x1, float y0, float y1) {
+    const bool moving = sc.kind != MDAS_SCENE_DISCS_DOF;
+    const float vx = moving ? p[4] : 0.0f, vy = moving ? p[5] : 0.0f;
+    const float cx0 = p[0] + fminf(0.0f, vx), cx1 = p[0] + fmaxf(0.0f, vx);
+    const float cy0 = p[1] + fminf(0.0f, vy), cy1 = p[1] + fmaxf(0.0f, vy);
+    float bx0 = x0, bx1 = x1, by0 = y0, by1 = y1, reach = sqrtf(fmaxf(p[7], 0.0f));
+    float scale = 1.0f;
+    if (sc.kind != MDAS_SCENE_DISCS_MB) {
+        const float s = p[6];
+        const float ax = s * sc.focalDistance * sc.filmHalfW, ay = s * sc.focalDistance * sc.filmHalfH;
+        const float ux0 = ax * (2.0f * x0 - 1.0f), ux1 = ax * (2.0f * x1 - 1.0f);
+        const float uy0 = ay * (2.0f * y0 - 1.0f), uy1 = ay * (2.0f * y1 - 1.0f);
+        bx0 = fminf(ux0, ux1);
+        bx1 = fmaxf(ux0, ux1);
+        by0 = fminf(uy0, uy1);
+        by1 = fmaxf(uy0, uy1);
+        reach += fabsf(1.0f - s) * fabsf(sc.lensRadius);
+        scale += fabsf(ax) + fabsf(ay) + fabsf(sc.lensRadius);
+    }
+    scale += fabsf(cx0) + fabsf(cx1) + fabsf(cy0) + fabsf(cy1) + reach;
+    const float dx = fmaxf(fmaxf(cx0 - bx1, bx0 - cx1), 0.0f);
+    const float dy = fmaxf(fmaxf(cy0 - by1, by0 - cy1), 0.0f);
+    const float dist = sqrtf(dx * dx + dy * dy);
+    return !(dist > reach + 1.0e-3f * scale);
+}
+
+// One thread per (tile, mask word).
+__global__ void __launch_bounds__(256) k_build_cull(MdasScene sc, const float* __restrict__ prims,
+                                                     unsigned* __restrict__ masks) {
+    constexpr int T = MDAS_CULL_TILES;
+    const int words = (sc.count + 31) / 32;
+    const int total = T * T * words;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int tile = i / words, w = i - tile * words;
+        const int tx = tile % T, ty = tile / T;
+        const float pad = 1.0e-4f;
+        const float x0 = (float)tx / T - pad, x1 = (float)(tx + 1) / T + pad;
+        const float y0 = (float)ty / T - pad, y1 = (float)(ty + 1) / T + pad;
+        unsigned m = 0u;
+        for (int b = 0; b < 32; ++b) {
+            const int k = 32 * w + b;
+            if (k < sc.count && cull_may_cover(sc, prims + MDAS_PRIM_STRIDE * k, x0, x1, y0, y1)) m |= 1u << b;
+        }
+        masks[i] = m;
+    }
+}
+
+__device__ __forceinline__ int cull_tile(float px, float py) {
+    constexpr int T = MDAS_CULL_TILES;
+    const int tx = min(max((int)(px * (float)T), 0), T - 1);
+    const int ty = min(max((int)(py * (float)T), 0), T - 1);
+    return ty * T + tx;
+}
+
+// mdas_shade over the tile's candidate discs: the same tests in the same order
+// as the full scans of integrand.h (the direct-light kind is not culled).
+__device__ void shade_culled(const MdasScene& sc, const float* prims, const unsigned* __restrict__ cull,
+                             const float* c, float* out) {
+    const int words = (sc.count + 31) / 32;
+    float R = sc.background, G = sc.background, B = sc.background;
+    if (sc.kind == MDAS_SCENE_DISCS_MB) {
+        const float px = c[0] / sc.scaleX;
+        const float py = c[1] / sc.scaleY;
+        const float t = c[2];
+        const unsigned* m = cull + (size_t)cull_tile(px, py) * words;
+        // the last listed covering disc wins: from the back
+        for (int w = words - 1; w >= 0; --w) {
+            unsigned bits = m[w];
+            while (bits) {
+                const int b = 31 - __clz(bits);
+                bits &= ~(1u << b);
+                const float* p = prims + MDAS_PRIM_STRIDE * (32 * w + b);
+                if (mdas_disc_mb_covers(p, px, py, t)) {
+                    R = p[8];
+                    G = p[9];
+                    B = p[10];
+                    goto done;
+                }
+            }
+        }
+    } else if (sc.kind == MDAS_SCENE_DISCS_DOF || sc.kind == MDAS_SCENE_DISCS_MBDOF) {
+        const int moving = sc.kind == MDAS_SCENE_DISCS_MBDOF;
+        float t, lx, ly, wx, wy;
+        mdas_dof_ray(&sc, c, moving, &t, &lx, &ly, &wx, &wy);
+        const unsigned* m = cull + (size_t)cull_tile(c[0] / sc.scaleX, c[1] / sc.scaleY) * words;
+        for (int w = 0; w < words; ++w) {
+            unsigned bits = m[w];
+            while (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1u;
+                const float* p = prims + MDAS_PRIM_STRIDE * (32 * w + b);
+                if (mdas_disc_dof_covers(p, lx, ly, wx, wy, t, moving)) {
+                    R = p[8];
+                    G = p[9];
+                    B = p[10];
+                    goto done;
+                }
+            }
+        }
+    } else {
+        mdas_shade(&sc, prims, c, out);
+        return;
+    }
+done:
+    out[0] = R;
+    out[1] = G;
+    out[2] = B;
+}
+
 template <int D>
 __global__ void __launch_bounds__(256) k_evaluate(MdasScene sc, const float* __restrict__ prims,
-                                                   const float* __restrict__ coords, float* __restrict__ values,
-                                                   const MdasCounts* __restrict__ counts, int offset, int count) {
+                                                   const unsigned* __restrict__ cull, const float* __restrict__ coords,
+                                                   float* __restrict__ values, const MdasCounts* __restrict__ counts,
+                                                   int offset, int count) {
+    // a full scan reads every primitive for every sample: staged in shared
+    // memory; a culled scan reads a few, straight from the (L1-resident) table
     extern __shared__ float s_prims[];
-    const int nfl = sc.count * MDAS_PRIM_STRIDE;
-    for (int k = threadIdx.x; k < nfl; k += blockDim.x) s_prims[k] = prims[k];
-    __syncthreads();
+    if (!cull) {
+        const int nfl = sc.count * MDAS_PRIM_STRIDE;
+        for (int k = threadIdx.x; k < nfl; k += blockDim.x) s_prims[k] = prims[k];
+        __syncthreads();
+    }
     if (counts) {  // the samples the last adaptive pass added
         offset = counts->N - counts->newN;
         count = counts->newN;
@@ -34,7 +160,8 @@ __global__ void __launch_bounds__(256) k_evaluate(MdasScene sc, const float* __r
 #pragma unroll
         for (int d = 0; d < D; ++d) c[d] = coords[s * D + d];
         float out[3];
-        mdas_shade(&sc, s_prims, c, out);
+        if (cull) shade_culled(sc, prims, cull, c, out);
+        else mdas_shade(&sc, s_prims, c, out);
         values[3 * s + 0] = out[0];
         values[3 * s + 1] = out[1];
         values[3 * s + 2] = out[2];
@@ -92,7 +219,8 @@ __global__ void __launch_bounds__(256) k_evaluate_batch(const MdasBatchScene* __
 #pragma unroll
             for (int d = 0; d < D; ++d) c[d] = b.coords[s * D + d];
             float out[3];
-            mdas_shade(&b.sc, b.prims, c, out);
+            if (b.cull) shade_culled(b.sc, b.prims, b.cull, c, out);
+            else mdas_shade(&b.sc, b.prims, c, out);
             b.values[3 * s + 0] = out[0];
             b.values[3 * s + 1] = out[1];
             b.values[3 * s + 2] = out[2];
@@ -238,16 +366,31 @@ cudaError_t mdas_launch_leaf_true_errors(const MdasScene& sc, const float* d_pri
     return cudaGetLastError();
 }
 
-cudaError_t mdas_launch_evaluate(const MdasScene& sc, const float* d_prims, const float* coords, float* values,
-                                 int dim, const MdasCounts* counts, int offset, int count, int grid, cudaStream_t s) {
-    const size_t smem = sizeof(float) * MDAS_PRIM_STRIDE * (size_t)sc.count;
+size_t mdas_cull_words(const MdasScene& sc) {
+    if (!mdas_culled_kind(sc.kind) || sc.count <= 0) return 0;
+    return (size_t)MDAS_CULL_TILES * MDAS_CULL_TILES * (size_t)((sc.count + 31) / 32);
+}
+
+cudaError_t mdas_launch_build_cull(const MdasScene& sc, const float* d_prims, unsigned* masks, cudaStream_t s) {
+    const size_t words = mdas_cull_words(sc);
+    if (words == 0) return cudaSuccess;
+    if (!masks) return cudaErrorInvalidValue;
+    k_build_cull<<<(unsigned)((words + 255) / 256), 256, 0, s>>>(sc, d_prims, masks);
+    return cudaGetLastError();
+}
+
+cudaError_t mdas_launch_evaluate(const MdasScene& sc, const float* d_prims, const unsigned* cull, const float* coords,
+                                 float* values, int dim, const MdasCounts* counts, int offset, int count, int grid,
+                                 cudaStream_t s) {
     if (grid <= 0) grid = 1;
     if (dim < sc.dim) return cudaErrorInvalidValue;
+    if (!mdas_culled_kind(sc.kind)) cull = nullptr;
+    const size_t smem = cull ? 0 : sizeof(float) * MDAS_PRIM_STRIDE * (size_t)sc.count;
     switch (dim) {
-        case 3: k_evaluate<3><<<grid, 256, smem, s>>>(sc, d_prims, coords, values, counts, offset, count); break;
-        case 4: k_evaluate<4><<<grid, 256, smem, s>>>(sc, d_prims, coords, values, counts, offset, count); break;
-        case 5: k_evaluate<5><<<grid, 256, smem, s>>>(sc, d_prims, coords, values, counts, offset, count); break;
-        case 6: k_evaluate<6><<<grid, 256, smem, s>>>(sc, d_prims, coords, values, counts, offset, count); break;
+        case 3: k_evaluate<3><<<grid, 256, smem, s>>>(sc, d_prims, cull, coords, values, counts, offset, count); break;
+        case 4: k_evaluate<4><<<grid, 256, smem, s>>>(sc, d_prims, cull, coords, values, counts, offset, count); break;
+        case 5: k_evaluate<5><<<grid, 256, smem, s>>>(sc, d_prims, cull, coords, values, counts, offset, count); break;
+        case 6: k_evaluate<6><<<grid, 256, smem, s>>>(sc, d_prims, cull, coords, values, counts, offset, count); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -83,6 +83,13 @@ MDAS_HD void mdas_concentric(float u, float v, float radius, float* lx, float* l
     }
 }
 
+// Motion-blur disc p covers image point (px, py) at shutter time t.
+MDAS_HD int mdas_disc_mb_covers(const float* p, float px, float py, float t) {
+    const float dx = px - mdas_fma(p[4], t, p[0]);
+    const float dy = py - mdas_fma(p[5], t, p[1]);
+    return mdas_fma(dx, dx, dy * dy) <= p[7];
+}
+
 MDAS_HD void mdas_shade_discs_mb(const MdasScene* sc, const float* prims, const float* c, float* out) {
     const float px = c[0] / sc->scaleX;
     const float py = c[1] / sc->scaleY;
@@ -91,9 +98,7 @@ MDAS_HD void mdas_shade_discs_mb(const MdasScene* sc, const float* prims, const 
     // the last listed covering disc wins: scan from the back, stop at the first cover
     for (int k = sc->count - 1; k >= 0; --k) {
         const float* p = prims + MDAS_PRIM_STRIDE * k;
-        const float dx = px - mdas_fma(p[4], t, p[0]);
-        const float dy = py - mdas_fma(p[5], t, p[1]);
-        if (mdas_fma(dx, dx, dy * dy) <= p[7]) {
+        if (mdas_disc_mb_covers(p, px, py, t)) {
             R = p[8];
             G = p[9];
             B = p[10];
@@ -105,6 +110,35 @@ MDAS_HD void mdas_shade_discs_mb(const MdasScene* sc, const float* prims, const 
     out[2] = B;
 }
 
+// Thin-lens ray of sample c (layout of mdas_shade_discs_dof): shutter time t,
+// lens point (lx, ly) and the offset (wx, wy) from the lens point to the
+// pinhole ray's point on the focal plane.
+MDAS_HD void mdas_dof_ray(const MdasScene* sc, const float* c, int moving, float* t, float* lx, float* ly, float* wx,
+                          float* wy) {
+    const float px = c[0] / sc->scaleX;
+    const float py = c[1] / sc->scaleY;
+    *t = moving ? c[2] : 0.0f;
+    const float u = moving ? c[3] : c[2];
+    const float v = moving ? c[4] : c[3];
+    const float nx = (px + px) - 1.0f;
+    const float ny = (py + py) - 1.0f;
+    mdas_concentric(u, v, sc->lensRadius, lx, ly);
+    *wx = sc->focalDistance * (nx * sc->filmHalfW) - *lx;
+    *wy = sc->focalDistance * (ny * sc->filmHalfH) - *ly;
+}
+
+// Fronto-parallel disc p covers the lens ray at its depth: the ray meets the
+// disc's plane at lens point + (depth / focal) * offset.
+MDAS_HD int mdas_disc_dof_covers(const float* p, float lx, float ly, float wx, float wy, float t, int moving) {
+    const float hx = mdas_fma(p[6], wx, lx);
+    const float hy = mdas_fma(p[6], wy, ly);
+    const float cx = moving ? mdas_fma(p[4], t, p[0]) : p[0];
+    const float cy = moving ? mdas_fma(p[5], t, p[1]) : p[1];
+    const float dx = hx - cx;
+    const float dy = hy - cy;
+    return mdas_fma(dx, dx, dy * dy) <= p[7];
+}
+
 // Thin-lens camera at the origin looking down +z (SDK/cuda/whitted.cu:164-249):
 // the pinhole ray through the film point meets the focal plane at
 // focal * (nx * filmHalfW, ny * filmHalfH, 1); the lens ray starts at the lens
@@ -114,27 +148,12 @@ MDAS_HD void mdas_shade_discs_mb(const MdasScene* sc, const float* prims, const 
 // the first covering disc in list order is that hit.
 MDAS_HD void mdas_shade_discs_dof(const MdasScene* sc, const float* prims, const float* c, int moving,
                                   float* out) {
-    const float px = c[0] / sc->scaleX;
-    const float py = c[1] / sc->scaleY;
-    const float t = moving ? c[2] : 0.0f;
-    const float u = moving ? c[3] : c[2];
-    const float v = moving ? c[4] : c[3];
-    const float nx = (px + px) - 1.0f;
-    const float ny = (py + py) - 1.0f;
-    float lx, ly;
-    mdas_concentric(u, v, sc->lensRadius, &lx, &ly);
-    const float wx = sc->focalDistance * (nx * sc->filmHalfW) - lx;
-    const float wy = sc->focalDistance * (ny * sc->filmHalfH) - ly;
+    float t, lx, ly, wx, wy;
+    mdas_dof_ray(sc, c, moving, &t, &lx, &ly, &wx, &wy);
     float R = sc->background, G = sc->background, B = sc->background;
     for (int k = 0; k < sc->count; ++k) {
         const float* p = prims + MDAS_PRIM_STRIDE * k;
-        const float hx = mdas_fma(p[6], wx, lx);
-        const float hy = mdas_fma(p[6], wy, ly);
-        const float cx = moving ? mdas_fma(p[4], t, p[0]) : p[0];
-        const float cy = moving ? mdas_fma(p[5], t, p[1]) : p[1];
-        const float dx = hx - cx;
-        const float dy = hy - cy;
-        if (mdas_fma(dx, dx, dy * dy) <= p[7]) {
+        if (mdas_disc_dof_covers(p, lx, ly, wx, wy, t, moving)) {
             R = p[8];
             G = p[9];
             B = p[10];
