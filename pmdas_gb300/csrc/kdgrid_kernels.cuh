@@ -351,7 +351,9 @@ __global__ void __launch_bounds__(256) k_compute_errors(MdasDeviceGrid g) {
     unsigned recomputed = 0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < items; k += gridDim.x * blockDim.x) {
         const int nodeIndex = DIRTY ? (k < newL ? g.dirty[k] : firstRight + (k - newL)) : k;
-        float error = g.errors[nodeIndex];
+        // the last pass set the error of both children of each split to -1 (decide
+        // the left one, place the right one), so a dirty item is never read
+        float error = DIRTY ? -1.0f : g.errors[nodeIndex];
         if (error < 0.0f) {
             error = leaf_error<D>(g, nodeIndex);
             g.errors[nodeIndex] = error;

@@ -158,8 +158,17 @@ cudaError_t leaf_keys(const MdasDeviceGrid& g, int L, int F, uint64_t* keys, cud
 constexpr int kBins = 256;
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kItems = 12;
-constexpr int kTile = kThreads * kItems;  // 3072 keys per tile
+#ifndef MDAS_SORT_ITEMS
+#define MDAS_SORT_ITEMS 12
+#endif
+constexpr int kItems = MDAS_SORT_ITEMS;    // keys per thread
+constexpr int kTile = kThreads * kItems;  // keys per tile
+// the tile staged in digit order: static shared memory up to 12 keys per
+// thread, dynamic (keys, then values) above
+#ifndef MDAS_SORT_DYNAMIC_SMEM
+#define MDAS_SORT_DYNAMIC_SMEM (MDAS_SORT_ITEMS > 12)
+#endif
+constexpr size_t kSweepSmem = MDAS_SORT_DYNAMIC_SMEM ? (size_t)kTile * (sizeof(uint64_t) + sizeof(uint32_t)) : 0;
 constexpr unsigned kFlagAggregate = 1u << 30;
 constexpr unsigned kFlagInclusive = 2u << 30;
 constexpr unsigned kCountMask = (1u << 30) - 1u;
@@ -233,12 +242,21 @@ struct SweepArgs {
     unsigned* status;
 };
 
-__global__ void __launch_bounds__(kThreads) k_onesweep(SweepArgs a) {
+#ifndef MDAS_SORT_MIN_CTAS
+#define MDAS_SORT_MIN_CTAS 4  // 64 registers: 4 CTAs per SM (3 at 80 registers: 12 % slower)
+#endif
+__global__ void __launch_bounds__(kThreads, MDAS_SORT_MIN_CTAS) k_onesweep(SweepArgs a) {
     __shared__ unsigned s_warpHist[kWarps][kBins];  // per-warp digit counts, then per-warp offsets
     __shared__ unsigned s_localStart[kBins];         // digit start within the tile
     __shared__ unsigned s_globalBase[kBins];         // output position of the tile's first key of each digit
+#if MDAS_SORT_DYNAMIC_SMEM
+    extern __shared__ __align__(16) unsigned char s_tileBuf[];
+    uint64_t* s_keys = reinterpret_cast<uint64_t*>(s_tileBuf);
+    uint32_t* s_values = reinterpret_cast<uint32_t*>(s_tileBuf + sizeof(uint64_t) * kTile);
+#else
     __shared__ __align__(16) uint64_t s_keys[kTile];
     __shared__ uint32_t s_values[kTile];
+#endif
     __shared__ int s_tile;
 
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(a.tileCounter, 1u);
@@ -437,6 +455,10 @@ cudaError_t radix_sort(void* temp, size_t tempBytes, const uint64_t* keysIn, uin
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (kSweepSmem > 0) {
+        e = cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSweepSmem);
+        if (e != cudaSuccess) return e;
+    }
     const int histBlocks = min(blocks_for(n, kThreads), 2 * (sms > 0 ? sms : 1));
     k_histogram<<<histBlocks, kThreads, 0, s>>>(keysIn, n, beginBit, endBit, passes, hist);
     k_digit_starts<<<passes, kBins, 0, s>>>(hist);
@@ -460,7 +482,7 @@ cudaError_t radix_sort(void* temp, size_t tempBytes, const uint64_t* keysIn, uin
         a.lookback = reinterpret_cast<unsigned*>(base + l.lookback) + (size_t)p * tiles * kBins;
         a.tileCounter = counters + p;
         a.status = status;
-        k_onesweep<<<(unsigned)tiles, kThreads, 0, s>>>(a);
+        k_onesweep<<<(unsigned)tiles, kThreads, kSweepSmem, s>>>(a);
         srcK = a.keysOut;
         srcV = a.valuesOut;
     }
