@@ -126,7 +126,7 @@ def stage_bytes(D: int, W: int, H: int, L0: int, passes: list, N_final: int, L_f
     init     : per initial leaf 4 samples * D floats + node 16 + box 8D + error 4 + seed 4 + sample count 1
                = 24D + 25
     errors   : first pass (every leaf): error read 4 per leaf; later passes visit only the split
-               children: dirty-list entry 4 per split + error read 4 per child; per recomputed
+               children (whose errors the pass set to -1, not read): dirty-list entry 4 per split; per recomputed
                leaf error write 4 + node 16 + box 8D + its sample values (12 B each; 4 per leaf
                on the first pass, 5 per split pair after)
     adaptive : error + seed read, seed write, sample count read: 13 per leaf; per accepted leaf:
@@ -142,7 +142,7 @@ def stage_bytes(D: int, W: int, H: int, L0: int, passes: list, N_final: int, L_f
     for k, p in enumerate(passes):
         L, R = p["L"], p["recomputed"]
         V = 4 * R if k == 0 else (5 * R) // 2
-        scan = 4 * L if k == 0 else 4 * R + 2 * R
+        scan = 4 * L if k == 0 else 2 * R
         err += scan + R * (4 + 16 + 8 * D) + 12 * V
         S, P, G = p["selected"], p["splits"], p["gathered"]
         adap += 13 * L + S * (32 + 12 * D) + 4 * D * G + (S - P) * (17 + 4 * D) + P * (54 + 28 * D)

@@ -418,8 +418,11 @@ __device__ __forceinline__ unsigned acc_pack(unsigned local, unsigned splitRank,
 
 // Learned acceptance ratio (no reference counterpart): the predicted error over
 // the largest predicted error, as kdgrid.cu:326 divides the error by g_error.
+__device__ __forceinline__ float learned_ratio_of(float priority, float predMax, float scale) {
+    return exp2f((priority - predMax) * scale);
+}
 __device__ __forceinline__ float learned_ratio(const MdasDeviceGrid& g, int leaf, float predMax) {
-    return exp2f((g.priority[leaf] - predMax) * g.priorityScale);
+    return learned_ratio_of(g.priority[leaf], predMax, g.priorityScale);
 }
 
 // decide, one tile: acceptance of the tile's leaves, final seeds, the tile's
@@ -1027,16 +1030,28 @@ __global__ void __launch_bounds__(256) k_learned_judge(MdasDeviceGrid g, int Lho
     const float gError = __uint_as_float(g.counts->gerr);
     const float predMax = mdas_float_unorder(g.learned->predMax);
     double ul = 0.0, up = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
-        const float e = g.errors[i];
-        unsigned seed = g.seeds[i];
+    auto judge = [&](int i, float e, unsigned seed, float prio) {
         if (seed == 0) seed = tea4((unsigned)i, 0);
         const float r = rnd(seed);
         const bool plain = mdas_pow(e / gError, g.alpha) >= r;
-        const bool learned = mdas_pow(learned_ratio(g, i, predMax), g.alpha) >= r;
+        const bool learned = mdas_pow(learned_ratio_of(prio, predMax, g.priorityScale), g.alpha) >= r;
         if (!plain) up += (double)e;
         if (!learned) ul += (double)e;
+    };
+    // four leaves per thread and iteration: 16-byte loads of errors, seeds and
+    // priorities (all 256-byte aligned)
+    const int L4 = L >> 2;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < L4; v += gridDim.x * blockDim.x) {
+        const float4 e = reinterpret_cast<const float4*>(g.errors)[v];
+        const uint4 sd = reinterpret_cast<const uint4*>(g.seeds)[v];
+        const float4 p = reinterpret_cast<const float4*>(g.priority)[v];
+        judge(4 * v, e.x, sd.x, p.x);
+        judge(4 * v + 1, e.y, sd.y, p.y);
+        judge(4 * v + 2, e.z, sd.z, p.z);
+        judge(4 * v + 3, e.w, sd.w, p.w);
     }
+    for (int i = 4 * L4 + blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x)
+        judge(i, g.errors[i], g.seeds[i], g.priority[i]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         ul += __shfl_xor_sync(0xffffffffu, ul, o);

@@ -465,7 +465,24 @@ __global__ void __launch_bounds__(256) k_priority_max(const MdasDeviceGrid g, in
                                                       unsigned* out) {
     const int L = Lhost >= 0 ? Lhost : g.counts->L;
     unsigned best = 0u;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x)
+    // 16-byte loads, two in flight per thread (pred is 256-byte aligned)
+    const int L4 = L >> 2;
+    const float4* p4 = reinterpret_cast<const float4*>(pred);
+    const int stride = gridDim.x * blockDim.x;
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    for (; v + stride < L4; v += 2 * stride) {
+        const float4 a = p4[v], b = p4[v + stride];
+        best = max(best, max(max(mdas_float_order(a.x), mdas_float_order(a.y)),
+                             max(mdas_float_order(a.z), mdas_float_order(a.w))));
+        best = max(best, max(max(mdas_float_order(b.x), mdas_float_order(b.y)),
+                             max(mdas_float_order(b.z), mdas_float_order(b.w))));
+    }
+    if (v < L4) {
+        const float4 a = p4[v];
+        best = max(best, max(max(mdas_float_order(a.x), mdas_float_order(a.y)),
+                             max(mdas_float_order(a.z), mdas_float_order(a.w))));
+    }
+    for (int i = 4 * L4 + blockIdx.x * blockDim.x + threadIdx.x; i < L; i += stride)
         best = max(best, mdas_float_order(pred[i]));
     best = __reduce_max_sync(0xffffffffu, best);
     if ((threadIdx.x & 31) == 0 && best) atomicMax(out, best);
