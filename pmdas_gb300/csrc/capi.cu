@@ -93,6 +93,12 @@ struct mdas_grid {
     unsigned* hVisits = nullptr;      // [cap + 1] refit arrival counters, then the locate status word
     void* sortTemp = nullptr;
     size_t sortTempBytes = 0;
+    // point location: coarse keys of the queries (2 cap), their order, sort scratch
+    int qCap = 0;
+    uint64_t* qKeys = nullptr;
+    uint32_t* qPerm = nullptr;
+    void* qTemp = nullptr;
+    size_t qTempBytes = 0;
     // learned acceptance (mdas_learned_enable)
     bool learned = false;
     float* lState = nullptr;            // FP32 params (MDAS_MLP_PARAMS), then a status word
@@ -228,6 +234,9 @@ void free_grid(mdas_grid* g) {
     cudaFree(g->hBoxes);
     cudaFree(g->hVisits);
     cudaFree(g->sortTemp);
+    cudaFree(g->qKeys);
+    cudaFree(g->qPerm);
+    cudaFree(g->qTemp);
     cudaFree(g->lState);
     cudaFree(g->lPacked);
     cudaFree(g->lPred);
@@ -1364,6 +1373,29 @@ int ensure_hierarchy(mdas_grid* g, int n) {
     return MDAS_OK;
 }
 
+// Point locations of at least this many queries order them by a coarse key first.
+constexpr int kLocateSortMin = 1 << 16;
+
+// Scratch of a point location over n >= kLocateSortMin queries.
+int ensure_query_scratch(mdas_grid* g, int n) {
+    if (g->qCap >= n && g->qKeys) return MDAS_OK;
+    cudaFree(g->qKeys);
+    cudaFree(g->qPerm);
+    cudaFree(g->qTemp);
+    g->qKeys = nullptr;
+    g->qPerm = nullptr;
+    g->qTemp = nullptr;
+    g->qCap = 0;
+    const size_t c = (size_t)n;
+    g->qTempBytes = mdas_order::sort_temp_bytes(n, 0, 64);
+    const bool ok = cudaMalloc(&g->qKeys, sizeof(uint64_t) * 2 * c) == cudaSuccess &&
+                    cudaMalloc(&g->qPerm, sizeof(uint32_t) * c) == cudaSuccess &&
+                    cudaMalloc(&g->qTemp, g->qTempBytes) == cudaSuccess;
+    if (!ok) return MDAS_ERR_ALLOC;
+    g->qCap = n;
+    return MDAS_OK;
+}
+
 // Leaf keys and their order (sorted keys in hSorted, slots in hOrder).
 int order_leaves(mdas_grid* g, int fineBits) {
     if (!g->initialized) return MDAS_ERR_STATE;
@@ -1448,15 +1480,36 @@ int mdas_locate(mdas_grid* g, const float* points, int n, int* leaves) {
     if (g->hierVersion != g->version) return MDAS_ERR_STATE;
     unsigned* status = g->hVisits + g->hierCap;
     cudaError_t e = cudaMemsetAsync(status, 0, sizeof(unsigned), g->stream);
+    // Many queries: threads take them in the order of a coarse Morton key, so
+    // that the points of a warp lie close together and walk the same nodes.
+    const uint32_t* perm = nullptr;
+    unsigned* sortStatus = nullptr;
+    if (e == cudaSuccess && n >= kLocateSortMin) {
+        const int rc = ensure_query_scratch(g, n);
+        if (rc) return rc;
+        const MdasDeviceGrid& d = g->dg;
+        const int fine = mdas_order::query_fine_bits(d.D, d.bitsPerDim, d.extraImgBits);
+        const int bits = mdas_order::key_bits(d.D, d.bitsPerDim, d.extraImgBits, fine);
+        e = mdas_order::morton_encode(points, n, d.D, d.bitsPerDim, d.extraImgBits, fine, d.scaleX, d.scaleY,
+                                      g->qKeys, g->stream);
+        if (e == cudaSuccess)
+            e = mdas_order::radix_sort(g->qTemp, g->qTempBytes, g->qKeys, g->qKeys + g->qCap, nullptr, g->qPerm, n, 0,
+                                       bits, g->stream, &sortStatus);
+        g->launches += 1 + mdas_order::sort_launches(n, 0, bits);
+        perm = g->qPerm;
+    }
     if (e == cudaSuccess)
-        e = mdas_order::locate(g->dg, g->hOrder, g->hierN, g->hChildren, g->hBoxes, points, n, leaves, status,
+        e = mdas_order::locate(g->dg, g->hOrder, g->hierN, g->hChildren, g->hBoxes, points, n, perm, leaves, status,
                                g->stream);
     g->launches += 1;
-    unsigned h = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, status, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream);
+    unsigned h[2] = {0u, 0u};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h[0], status, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess && sortStatus)
+        e = cudaMemcpyAsync(&h[1], sortStatus, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     if (e != cudaSuccess) return MDAS_ERR_CUDA;
-    return h ? MDAS_ERR_CAPACITY : MDAS_OK;
+    if (h[1]) return MDAS_ERR_TIMEOUT;
+    return h[0] ? MDAS_ERR_CAPACITY : MDAS_OK;
 }
 
 

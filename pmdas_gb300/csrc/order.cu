@@ -548,7 +548,9 @@ __device__ __forceinline__ unsigned atomic_add_acq_rel(unsigned* p, unsigned v) 
 // Bottom-up boxes: a thread starts at each leaf and climbs; at each node the
 // first of the two children to arrive stops, the second (which then finds both
 // child boxes written) computes the union and goes on.
-template <int D>
+// READONLY: the boxes are final (point location) and go through L1; during the
+// refit another thread writes them, so they are read through L2.
+template <int D, bool READONLY = false>
 __device__ __forceinline__ void child_box(const MdasDeviceGrid& g, const uint32_t* __restrict__ order, const float* boxes,
                                           int c, float (&mn)[D], float (&mx)[D]) {
     if (c < 0) {
@@ -559,11 +561,11 @@ __device__ __forceinline__ void child_box(const MdasDeviceGrid& g, const uint32_
             mx[j] = b[D + j];
         }
     } else {
-        const float* b = boxes + (size_t)c * 2 * D;  // written by another thread: read through L2
+        const float* b = boxes + (size_t)c * 2 * D;
 #pragma unroll
         for (int j = 0; j < D; ++j) {
-            mn[j] = __ldcg(b + j);
-            mx[j] = __ldcg(b + D + j);
+            mn[j] = READONLY ? __ldg(b + j) : __ldcg(b + j);
+            mx[j] = READONLY ? __ldg(b + D + j) : __ldcg(b + D + j);
         }
     }
 }
@@ -607,17 +609,24 @@ cudaError_t karras_refit(const MdasDeviceGrid& g, const uint32_t* order, int n, 
 // leaves in key order, so the answer is the first holding leaf in key order.
 constexpr int kStack = kMaxDepth;
 
+// perm (may be null): the queries in the order the threads take them (points
+// sorted by a coarse Morton key, so that a warp walks one region of the tree).
 template <int D>
 __global__ void k_locate(MdasDeviceGrid g, const uint32_t* __restrict__ order, int n, const int2* __restrict__ children,
                          const float* __restrict__ boxes, const float* __restrict__ points, int m,
-                         int* __restrict__ leaves, unsigned* status) {
+                         const uint32_t* __restrict__ perm, int* __restrict__ leaves, unsigned* status) {
     float domMx[D];
     {
         float dmn[D];
-        if (n == 1) child_box<D>(g, order, boxes, ~0, dmn, domMx);
-        else child_box<D>(g, order, boxes, 0, dmn, domMx);
+        if (n == 1) child_box<D, true>(g, order, boxes, ~0, dmn, domMx);
+        else child_box<D, true>(g, order, boxes, 0, dmn, domMx);
     }
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m; t += gridDim.x * blockDim.x) {
+        const int q = perm ? (int)perm[t] : t;
+        if (q < 0 || q >= m) {  // a permutation from a sort that gave up
+            atomicOr(status, 4u);
+            continue;
+        }
         float p[D];
 #pragma unroll
         for (int j = 0; j < D; ++j) p[j] = points[(size_t)q * D + j];
@@ -628,7 +637,7 @@ __global__ void k_locate(MdasDeviceGrid g, const uint32_t* __restrict__ order, i
         while (sp > 0) {
             const int c = stack[--sp];
             float mn[D], mx[D];
-            child_box<D>(g, order, boxes, c, mn, mx);
+            child_box<D, true>(g, order, boxes, c, mn, mx);
             bool in = true;
             if (c < 0) {
 #pragma unroll
@@ -657,12 +666,19 @@ __global__ void k_locate(MdasDeviceGrid g, const uint32_t* __restrict__ order, i
 }
 
 cudaError_t locate(const MdasDeviceGrid& g, const uint32_t* order, int n, const int2* children, const float* boxes,
-                   const float* points, int m, int* leaves, unsigned* status, cudaStream_t s) {
+                   const float* points, int m, const uint32_t* perm, int* leaves, unsigned* status, cudaStream_t s) {
     if (m <= 0) return cudaSuccess;
     if (n <= 0) return cudaMemsetAsync(leaves, 0xff, sizeof(int) * (size_t)m, s);
     ORDER_SWITCH_D(g.D, (k_locate<DD><<<blocks_for(m, 128), 128, 0, s>>>(g, order, n, children, boxes, points, m,
-                                                                         leaves, status)));
+                                                                         perm, leaves, status)));
     return cudaGetLastError();
+}
+
+int query_fine_bits(int D, int bitsPerDim, int extraImgBits) {
+    const int base = D * bitsPerDim + 2 * extraImgBits;
+    int fine = base >= 32 ? 0 : (32 - base) / D;
+    if (fine > 31 - bitsPerDim - extraImgBits) fine = 31 - bitsPerDim - extraImgBits;
+    return fine > 0 ? fine : 0;
 }
 
 }  // namespace mdas_order

@@ -49,8 +49,14 @@ cudaError_t karras_refit(const MdasDeviceGrid& g, const uint32_t* order, int n, 
                          const int* parents, unsigned* visits, float* boxes, cudaStream_t s);
 // For each point, the grid leaf whose box holds it (mn <= p < mx per
 // dimension, p <= mx on the domain's upper faces); the first in key order if
-// several do, -1 if none.  status: set nonzero if a traversal stack overflowed.
+// several do, -1 if none.  perm (may be null): the order in which threads take
+// the points (a permutation of 0..m-1).  status: set nonzero if a traversal
+// stack overflowed or perm held an index out of range.
 cudaError_t locate(const MdasDeviceGrid& g, const uint32_t* order, int n, const int2* children,
-                   const float* boxes, const float* points, int m, int* leaves, unsigned* status, cudaStream_t s);
+                   const float* boxes, const float* points, int m, const uint32_t* perm, int* leaves,
+                   unsigned* status, cudaStream_t s);
+// Extra bits per dimension of the coarse keys that order the queries of a
+// large point location (the keys then fit in 32 bits where the grid allows).
+int query_fine_bits(int D, int bitsPerDim, int extraImgBits);
 
 }  // namespace mdas_order
