@@ -20,6 +20,7 @@
 #include "scene.h"
 #include "order.h"
 #include "mlp.h"
+#include "leaf_raw.h"
 
 namespace {
 
@@ -104,6 +105,8 @@ struct mdas_grid {
     float* lState = nullptr;            // FP32 params (MDAS_MLP_PARAMS), then a status word
     mdas_mlp::Packed* lPacked = nullptr;
     float* lPred = nullptr;             // [maxNodes] predicted log2(error) / MDAS_MLP_TARGET_SCALE
+    float* lRaw = nullptr;              // [maxNodes * MDAS_RAW_FLOATS] raw feature rows of the split-children errors pass
+    bool rawValid = false;              // the last errors pass wrote lRaw for the leaves it recomputed
     MdasLearnedStats* lStats = nullptr;
     uint64_t lPredVersion = ~0ull;      // grid version the predictions (and the verdict) belong to
     bool lastErrorsDirty = false;       // the last errors pass visited only the split children
@@ -240,6 +243,7 @@ void free_grid(mdas_grid* g) {
     cudaFree(g->lState);
     cudaFree(g->lPacked);
     cudaFree(g->lPred);
+    cudaFree(g->lRaw);
     cudaFree(g->lStats);
     if (g->scratch) cudaFree(g->scratch);
     if (g->hcounts) cudaFreeHost(g->hcounts);
@@ -422,6 +426,7 @@ int mdas_compute_errors(mdas_grid* g) {
     if (rc) return rc;
     g->errorsClean = true;
     g->lastErrorsDirty = dirty;
+    g->rawValid = dirty && g->dg.featRaw != nullptr;
     if (g->log) *g->log << "COMPUTE ERRORS TIME\n" << last_stage_ms(g, 1) << std::endl;
     return MDAS_OK;
 }
@@ -1136,6 +1141,7 @@ int mdas_batch_create(mdas_batch** out, int n, mdas_grid* const* grids, mdas_sce
         MdasBatchImage im{};
         im.g = g->dg;
         im.g.priority = g->learned ? g->lPred : nullptr;  // learned images keep their weights and statistics
+        im.g.featRaw = nullptr;                           // (the batched kernels gather their features)
         im.g.learned = g->learned ? g->lStats : nullptr;
         im.mlp = g->learned ? g->lPacked : nullptr;
         if (g->learned) b->anyLearned = true;
@@ -1574,7 +1580,8 @@ cudaError_t learned_queue(mdas_grid* g, int L, cudaStream_t s) {
     // refresh the leaves whose error was recomputed (every leaf when the last
     // errors pass was a full one or the predictions are not from the previous
     // pass), then the exact maximum
-    const int mode = L < 0 ? 2 : (g->lastErrorsDirty && g->lPredVersion + 1 == g->version ? 1 : 0);
+    const int mode = L < 0 ? 2
+                           : (g->lastErrorsDirty && g->lPredVersion + 1 == g->version ? (g->rawValid ? 3 : 1) : 0);
     if (e == cudaSuccess)
         e = mdas_mlp::predict_leaves(g->dg, L, mode, g->lPacked, g->lPred, &st->predMax, learned_status(g), s);
     MdasDeviceGrid dg = g->dg;
@@ -1600,6 +1607,8 @@ int mdas_learned_enable(mdas_grid* g, const mdas_learned_config* cfg) {
         g->lPredVersion = ~0ull;
         g->dg.priority = nullptr;
         g->dg.learned = nullptr;
+        g->dg.featRaw = nullptr;
+        g->rawValid = false;
         return MDAS_OK;
     }
     if (!(cfg->tolerance >= 0.0f)) return MDAS_ERR_INVALID;
@@ -1607,6 +1616,7 @@ int mdas_learned_enable(mdas_grid* g, const mdas_learned_config* cfg) {
         const bool ok = cudaMalloc(&g->lState, sizeof(float) * (MDAS_MLP_PARAMS + 1)) == cudaSuccess &&
                         cudaMalloc(&g->lPacked, sizeof(mdas_mlp::Packed)) == cudaSuccess &&
                         cudaMalloc(&g->lPred, sizeof(float) * (size_t)g->dg.maxNodes) == cudaSuccess &&
+                        cudaMalloc(&g->lRaw, sizeof(float) * MDAS_RAW_FLOATS * (size_t)g->dg.maxNodes) == cudaSuccess &&
                         cudaMalloc(&g->lStats, sizeof(MdasLearnedStats)) == cudaSuccess;
         if (!ok) return MDAS_ERR_ALLOC;
     }
@@ -1622,6 +1632,8 @@ int mdas_learned_enable(mdas_grid* g, const mdas_learned_config* cfg) {
     if (rc) return rc;
     g->dg.priorityScale = MDAS_MLP_TARGET_SCALE;
     g->dg.learned = g->lStats;
+    g->dg.featRaw = g->lRaw;
+    g->rawValid = false;
     g->learned = true;
     return MDAS_OK;
 }

@@ -87,6 +87,10 @@ struct MdasDeviceGrid {
     const float* priority;
     float priorityScale;
     MdasLearnedStats* learned;
+    // learned mode: [maxNodes * MDAS_RAW_FLOATS] the raw feature inputs of each
+    // leaf the last split-children errors pass recomputed, in its item order
+    // (nullptr: not written)
+    float* featRaw;
 };
 
 // One image of a batched render (device-side descriptor).

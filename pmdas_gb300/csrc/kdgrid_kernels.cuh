@@ -36,6 +36,7 @@
 #include <cuda_runtime.h>
 #include "grid_types.h"
 #include "ieee_math.h"
+#include "leaf_raw.h"
 
 #ifndef MDAS_NS
 #error "define MDAS_NS before including kdgrid_kernels.cuh"
@@ -285,14 +286,16 @@ __global__ void __launch_bounds__(256) k_initial_sampling(MdasDeviceGrid g, int 
 //           slot range [L - newL, L)); the max over all other leaves was taken
 //           by the adaptive pass that left them unchanged (counts->gerrNext).
 // =====================================================================================
+// raw (may be null): the leaf's row of raw feature inputs (learned mode).
 template <int D>
-__device__ __forceinline__ float leaf_error(const MdasDeviceGrid& g, int nodeIndex) {
+__device__ __forceinline__ float leaf_error(const MdasDeviceGrid& g, int nodeIndex, float* raw = nullptr) {
     float mn[D], mx[D];
     const int4 node = nb_load<D>(g.nb + (size_t)nodeIndex * NbLayout<D>::FLOATS, mn, mx);
     const float volume = box_volume<D>(mn, mx);
     float3 avg = make_float3(0.0f, 0.0f, 0.0f);
     float3 loc[4];
     int sampleCount = 0;
+    MdasLumStats lum = mdas_lum_empty();
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int idx = node_get(node, i);
@@ -303,6 +306,7 @@ __device__ __forceinline__ float leaf_error(const MdasDeviceGrid& g, int nodeInd
             avg.y += loc[i].y;
             avg.z += loc[i].z;
             sampleCount++;
+            if (raw) mdas_lum_add(lum, mdas_luminance(loc[i].x, loc[i].y, loc[i].z));
         }
     }
     {
@@ -328,6 +332,7 @@ __device__ __forceinline__ float leaf_error(const MdasDeviceGrid& g, int nodeInd
     error /= float(sampleCount);
     error += 1.0e-5f;
     error *= volume;
+    if (raw) mdas_raw_store<D>(raw, mn, mx, lum, error);
     return error;
 }
 
@@ -355,7 +360,8 @@ __global__ void __launch_bounds__(256) k_compute_errors(MdasDeviceGrid g) {
         // the left one, place the right one), so a dirty item is never read
         float error = DIRTY ? -1.0f : g.errors[nodeIndex];
         if (error < 0.0f) {
-            error = leaf_error<D>(g, nodeIndex);
+            // learned mode: the item's row of raw feature inputs for the prediction
+            error = leaf_error<D>(g, nodeIndex, DIRTY && g.featRaw ? g.featRaw + (size_t)k * MDAS_RAW_FLOATS : nullptr);
             g.errors[nodeIndex] = error;
             recomputed++;
         }

@@ -18,6 +18,7 @@
 // over the tile's 128 rows on the CUDA cores, added to the global gradient
 // with atomics.
 #include "mlp.h"
+#include "leaf_raw.h"
 
 #include <cuda_bf16.h>
 #include <float.h>
@@ -297,14 +298,58 @@ __device__ __forceinline__ void put_features(const Ctx& c, const float (&f)[kIn]
 // log2(error) / 32.
 __device__ __forceinline__ float log2_err(float e) { return log2f(fmaxf(e, 1e-30f)) * (1.0f / MDAS_MLP_TARGET_SCALE); }
 
+// The raw inputs of a leaf's features (leaf_raw.h), gathered from its record
+// and sample values.
 template <int D>
-__device__ void leaf_feats(const MdasDeviceGrid& g, int leaf, int L, float (&f)[kIn], float* err) {
+__device__ __forceinline__ void leaf_raw(const MdasDeviceGrid& g, int leaf, float (&raw)[MDAS_RAW_FLOATS]) {
     const float* nb = g.nb + (size_t)leaf * g.nbFloats;
     const int4 node = *reinterpret_cast<const int4*>(nb);
+    float mn[D], mx[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+        mn[j] = nb[4 + j];
+        mx[j] = nb[4 + D + j];
+    }
+    const int idx[4] = {node.x, node.y, node.z, node.w};
+    MdasLumStats s = mdas_lum_empty();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (idx[i] >= 0) {
+            const float* p = g.values + 3 * (size_t)idx[i];
+            mdas_lum_add(s, mdas_luminance(__ldg(p), __ldg(p + 1), __ldg(p + 2)));
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 6; ++j) raw[j] = j < D ? __fsub_rn(mx[j < D ? j : 0], mn[j < D ? j : 0]) : 0.0f;
+    raw[6] = s.n;
+    raw[7] = s.sum;
+    raw[8] = s.sq;
+    raw[9] = s.mn;
+    raw[10] = s.mx;
+    raw[11] = g.errors[leaf];
+}
+
+// A row written by the errors pass (16-byte loads).
+__device__ __forceinline__ void load_raw(const float* __restrict__ row, float (&raw)[MDAS_RAW_FLOATS]) {
+    const float4* r4 = reinterpret_cast<const float4*>(row);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const float4 v = r4[q];
+        raw[4 * q] = v.x;
+        raw[4 * q + 1] = v.y;
+        raw[4 * q + 2] = v.z;
+        raw[4 * q + 3] = v.w;
+    }
+}
+
+// Features from the raw inputs and the errors of the leaf's slot neighbours.
+template <int D>
+__device__ void feats_of_raw(const MdasDeviceGrid& g, const float (&raw)[MDAS_RAW_FLOATS], int leaf, int L,
+                             float (&f)[kIn]) {
     float depth = 0.0f;
 #pragma unroll
     for (int j = 0; j < D; ++j) {
-        float e = nb[4 + D + j] - nb[4 + j];
+        float e = raw[j];
         if (j == 0) e /= g.scaleX;
         if (j == 1) e /= g.scaleY;
         const float l = log2f(fmaxf(e, 1e-30f));
@@ -313,36 +358,28 @@ __device__ void leaf_feats(const MdasDeviceGrid& g, int leaf, int L, float (&f)[
     }
 #pragma unroll
     for (int j = D; j < 5; ++j) f[j] = 0.0f;
-    const int idx[4] = {node.x, node.y, node.z, node.w};
-    float lsum = 0.0f, lsq = 0.0f, lmin = FLT_MAX, lmax = -FLT_MAX;
-    int n = 0;
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        if (idx[i] >= 0) {
-            const float* p = g.values + 3 * (size_t)idx[i];
-            const float lum = 0.2126f * __ldg(p) + 0.7152f * __ldg(p + 1) + 0.0722f * __ldg(p + 2);
-            lsum += lum;
-            lsq += lum * lum;
-            lmin = fminf(lmin, lum);
-            lmax = fmaxf(lmax, lum);
-            ++n;
-        }
-    }
-    const float inv = n ? 1.0f / (float)n : 0.0f;
-    const float mean = lsum * inv;
-    const float var = fmaxf(lsq * inv - mean * mean, 0.0f);
-    f[5] = (float)n * 0.25f;
+    const float n = raw[6];
+    const float inv = n > 0.0f ? 1.0f / n : 0.0f;
+    const float mean = raw[7] * inv;
+    const float var = fmaxf(raw[8] * inv - mean * mean, 0.0f);
+    f[5] = n * 0.25f;
     f[6] = log2f(1.0f + fabsf(mean));
     f[7] = log2f(1.0f + sqrtf(var));
-    f[8] = n ? log2f(1.0f + fabsf(lmin)) : 0.0f;
-    f[9] = n ? log2f(1.0f + fabsf(lmax)) : 0.0f;
-    const float e0 = g.errors[leaf];
-    f[10] = log2_err(e0);
+    f[8] = n > 0.0f ? log2f(1.0f + fabsf(raw[9])) : 0.0f;
+    f[9] = n > 0.0f ? log2f(1.0f + fabsf(raw[10])) : 0.0f;
+    f[10] = log2_err(raw[11]);
     f[11] = depth * (1.0f / 32.0f);
     const int nbr[4] = {leaf - 2, leaf - 1, leaf + 1, leaf + 2};
 #pragma unroll
     for (int q = 0; q < 4; ++q) f[12 + q] = nbr[q] >= 0 && nbr[q] < L ? log2_err(g.errors[nbr[q]]) : f[10];
-    if (err) *err = e0;
+}
+
+template <int D>
+__device__ void leaf_feats(const MdasDeviceGrid& g, int leaf, int L, float (&f)[kIn], float* err) {
+    float raw[MDAS_RAW_FLOATS];
+    leaf_raw<D>(g, leaf, raw);
+    feats_of_raw<D>(g, raw, leaf, L, f);
+    if (err) *err = raw[11];
 }
 
 __device__ __forceinline__ float target_of(float err) {
@@ -372,8 +409,10 @@ __global__ void __launch_bounds__(kThreads) k_forward_rows(const Packed* __restr
 // Priority of leaves: the plain log2 error (feature 10) plus the network's
 // correction.  MODE 0: every leaf; 1: the leaves whose error the last errors
 // pass recomputed (the split children of the last adaptive pass: its split
-// list and the appended right children); 2: as 1, or every leaf before the
-// first adaptive pass.  Lhost < 0: the leaf count in the device counters.
+// list and the appended right children); 3: as 1, from the raw rows that
+// errors pass wrote (g.featRaw); 2: as 3 (as 1 without rows), or every leaf
+// before the first adaptive pass.  Lhost < 0: the leaf count in the device
+// counters.
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_predict_leaves(MdasDeviceGrid g, int Lhost, int mode,
                                                              const Packed* __restrict__ w, float* __restrict__ pred,
@@ -381,7 +420,8 @@ __global__ void __launch_bounds__(kThreads) k_predict_leaves(MdasDeviceGrid g, i
     Ctx c;
     ctx_open(c, w, status);
     const int L = Lhost >= 0 ? Lhost : g.counts->L;
-    const bool dirty = mode == 1 || (mode == 2 && g.counts->passes > 0);
+    const bool dirty = mode == 1 || mode == 3 || (mode == 2 && g.counts->passes > 0);
+    const bool rows_raw = dirty && g.featRaw && mode != 1;
     const int newL = g.counts->newL;
     const int rows = dirty ? 2 * newL : L;
     const int tiles = (rows + kRows - 1) / kRows;
@@ -389,8 +429,12 @@ __global__ void __launch_bounds__(kThreads) k_predict_leaves(MdasDeviceGrid g, i
         const int r = tile * kRows + threadIdx.x;
         const int leaf = !dirty ? r : (r < newL ? g.dirty[r] : (L - newL) + (r - newL));
         float f[kIn];
-        if (r < rows) leaf_feats<D>(g, leaf, L, f, nullptr);
-        else
+        if (r < rows) {
+            float raw[MDAS_RAW_FLOATS];
+            if (rows_raw) load_raw(g.featRaw + (size_t)r * MDAS_RAW_FLOATS, raw);
+            else leaf_raw<D>(g, leaf, raw);
+            feats_of_raw<D>(g, raw, leaf, L, f);
+        } else
 #pragma unroll
             for (int i = 0; i < kIn; ++i) f[i] = 0.0f;
         put_features(c, f);

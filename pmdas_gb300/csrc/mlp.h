@@ -51,8 +51,9 @@ cudaError_t pack(const float* params, Packed* packed, cudaStream_t s);
 cudaError_t forward(const Packed* w, const float* features, int m, float* pred, unsigned* status, cudaStream_t s);
 // Priorities of the grid's leaves: log2(plain error) / 32 plus the network's
 // correction, for every leaf (mode 0), the leaves whose error the last errors
-// pass recomputed (1), or as 1 unless no adaptive pass ran yet (2); L < 0: the
-// leaf count in the device counters.  Then the largest priority over all
+// pass recomputed (1: features gathered; 3: from the raw rows that pass wrote
+// to g.featRaw), or as 3 unless no adaptive pass ran yet (2; as 1 if
+// g.featRaw is null); L < 0: the leaf count in the device counters.  Then the largest priority over all
 // leaves into *predMax (order-preserving bits; skipped if null).
 cudaError_t predict_leaves(const MdasDeviceGrid& g, int L, int mode, const Packed* w, float* pred, unsigned* predMax,
                            unsigned* status, cudaStream_t s);

@@ -191,6 +191,37 @@ def test_predictions_equal_forward_of_features(cuda):
     assert torch.equal(pred, again)
 
 
+def test_incremental_predictions_from_error_rows(cuda):
+    """After a learned pass the update refreshes only the split children, from
+    the raw feature rows the split-children errors pass wrote; their priorities
+    equal the forward pass of those leaves' gathered features, bit for bit."""
+    torch = cuda
+    g, sc = _grid(torch)
+    g.LearnedEnable(seed=7)
+    _passes(g, sc, 2)
+    g.ComputeErrors()
+    g.LearnedUpdate()                  # every leaf
+    before = g.dump_state()
+    g.AdaptiveSampling()               # learned acceptance
+    a, b = g.GetNumberOfSamples(), g.GetNewSamples()
+    sc.evaluate(g, a - b, b)
+    g.ComputeErrors()                  # the split children only, with their raw rows
+    g.LearnedUpdate()                  # those rows' priorities
+    after = g.dump_state()
+    L0, L1 = before["L"], after["L"]
+    assert L1 > L0
+    changed = np.zeros(L1, bool)
+    changed[L0:] = True                # right children
+    changed[:L0] = np.any(after["boxes"][:L0] != before["boxes"], axis=1)  # left children keep the slot
+    assert changed[:L0].sum() == L1 - L0
+    pred = g.LearnedPredictions()
+    p = torch.from_numpy(g.LearnedParams()).cuda()
+    feats = g.LeafFeatures()
+    again = feats[:, 10] + P.mlp_forward(p, feats)
+    idx = torch.from_numpy(np.nonzero(changed)[0]).cuda()
+    assert torch.equal(pred[idx], again[idx])
+
+
 def test_true_errors_match_oracle_integrand(cuda):
     torch = cuda
     from oracle import pyoracle as O
