@@ -1036,13 +1036,15 @@ __global__ void __launch_bounds__(256) k_learned_judge(MdasDeviceGrid g, int Lho
     const float gError = __uint_as_float(g.counts->gerr);
     const float predMax = mdas_float_unorder(g.learned->predMax);
     double ul = 0.0, up = 0.0;
-    auto judge = [&](int i, float e, unsigned seed, float prio) {
+    // the leaf's error into the schedules' FP32 partial sums (of four leaves at
+    // most: one FP64 add per schedule and four leaves, FP64 being a slow pipe)
+    auto judge = [&](int i, float e, unsigned seed, float prio, float& fp, float& fl) {
         if (seed == 0) seed = tea4((unsigned)i, 0);
         const float r = rnd(seed);
         const bool plain = mdas_pow(e / gError, g.alpha) >= r;
         const bool learned = mdas_pow(learned_ratio_of(prio, predMax, g.priorityScale), g.alpha) >= r;
-        if (!plain) up += (double)e;
-        if (!learned) ul += (double)e;
+        if (!plain) fp = __fadd_rn(fp, e);
+        if (!learned) fl = __fadd_rn(fl, e);
     };
     // four leaves per thread and iteration: 16-byte loads of errors, seeds and
     // priorities (all 256-byte aligned)
@@ -1051,13 +1053,20 @@ __global__ void __launch_bounds__(256) k_learned_judge(MdasDeviceGrid g, int Lho
         const float4 e = reinterpret_cast<const float4*>(g.errors)[v];
         const uint4 sd = reinterpret_cast<const uint4*>(g.seeds)[v];
         const float4 p = reinterpret_cast<const float4*>(g.priority)[v];
-        judge(4 * v, e.x, sd.x, p.x);
-        judge(4 * v + 1, e.y, sd.y, p.y);
-        judge(4 * v + 2, e.z, sd.z, p.z);
-        judge(4 * v + 3, e.w, sd.w, p.w);
+        float fp = 0.0f, fl = 0.0f;
+        judge(4 * v, e.x, sd.x, p.x, fp, fl);
+        judge(4 * v + 1, e.y, sd.y, p.y, fp, fl);
+        judge(4 * v + 2, e.z, sd.z, p.z, fp, fl);
+        judge(4 * v + 3, e.w, sd.w, p.w, fp, fl);
+        up += (double)fp;
+        ul += (double)fl;
     }
-    for (int i = 4 * L4 + blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x)
-        judge(i, g.errors[i], g.seeds[i], g.priority[i]);
+    for (int i = 4 * L4 + blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
+        float fp = 0.0f, fl = 0.0f;
+        judge(i, g.errors[i], g.seeds[i], g.priority[i], fp, fl);
+        up += (double)fp;
+        ul += (double)fl;
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         ul += __shfl_xor_sync(0xffffffffu, ul, o);
