@@ -126,6 +126,19 @@ __global__ void k_batch_reset(const MdasBatchImage* __restrict__ imgs, int n, in
 // active learned images.  A block keeps its partial results while its chunks
 // stay in one image and adds them to that image's statistics when it moves on
 // (a few atomics per block and image); the verdicts follow in k_batch_verdict.
+// Compensated FP32 sum (Kahan): a thread's unrefined errors over any number of
+// leaves within about an ulp, without a per-leaf FP64 add (a slow pipe).
+struct KahanF {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = __fsub_rn(x, c);
+        const float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
 __device__ __forceinline__ void flush_learned(MdasLearnedStats* st, int phase, unsigned best, double ul, double up) {
     if (phase == 0) {
         best = __reduce_max_sync(0xffffffffu, best);
@@ -152,14 +165,15 @@ __global__ void __launch_bounds__(256) k_batch_learned_reduce(const MdasBatchIma
     });
     int cur = -1;  // the image the block's partial results belong to (uniform across the block)
     unsigned best = 0u;
-    double ul = 0.0, up = 0.0;
+    KahanF ul, up;
     for (int ch = blockIdx.x; ch < total; ch += gridDim.x) {
         const int img = batch_image_of(s_pre, n, ch);
         if (img != cur) {
-            if (cur >= 0) flush_learned(imgs[cur].g.learned, phase, best, ul, up);
+            if (cur >= 0) flush_learned(imgs[cur].g.learned, phase, best, ul.value(), up.value());
             cur = img;
             best = 0u;
-            ul = up = 0.0;
+            ul = KahanF();
+            up = KahanF();
         }
         const MdasDeviceGrid& g = imgs[img].g;
         const int i = (ch - s_pre[img]) * 256 + threadIdx.x;
@@ -174,10 +188,10 @@ __global__ void __launch_bounds__(256) k_batch_learned_reduce(const MdasBatchIma
         unsigned seed = g.seeds[i];
         if (seed == 0) seed = tea4((unsigned)i, 0);
         const float r = rnd(seed);
-        if (!(mdas_pow(e / gError, g.alpha) >= r)) up += (double)e;
-        if (!(mdas_pow(learned_ratio(g, i, predMax), g.alpha) >= r)) ul += (double)e;
+        if (!(mdas_pow(e / gError, g.alpha) >= r)) up.add(e);
+        if (!(mdas_pow(learned_ratio(g, i, predMax), g.alpha) >= r)) ul.add(e);
     }
-    if (cur >= 0) flush_learned(imgs[cur].g.learned, phase, best, ul, up);
+    if (cur >= 0) flush_learned(imgs[cur].g.learned, phase, best, ul.value(), up.value());
 }
 
 // One thread per image: the verdict of a learned image's pass.
@@ -216,9 +230,11 @@ __global__ void __launch_bounds__(256) k_batch_errors(const MdasBatchImage* __re
         unsigned recomputed = 0;
         if (k < items) {
             const int nodeIndex = dirty ? (k < newL ? g.dirty[k] : firstRight + (k - newL)) : k;
-            float error = g.errors[nodeIndex];
+            // split children: -1 by construction (not read); learned images also
+            // leave the item's raw feature row for the prediction
+            float error = dirty ? -1.0f : g.errors[nodeIndex];
             if (error < 0.0f) {
-                error = leaf_error<D>(g, nodeIndex);
+                error = leaf_error<D>(g, nodeIndex, dirty && g.featRaw ? g.featRaw + (size_t)k * MDAS_RAW_FLOATS : nullptr);
                 g.errors[nodeIndex] = error;
                 recomputed = 1;
             }

@@ -1141,7 +1141,7 @@ int mdas_batch_create(mdas_batch** out, int n, mdas_grid* const* grids, mdas_sce
         MdasBatchImage im{};
         im.g = g->dg;
         im.g.priority = g->learned ? g->lPred : nullptr;  // learned images keep their weights and statistics
-        im.g.featRaw = nullptr;                           // (the batched kernels gather their features)
+        im.g.featRaw = g->learned ? g->lRaw : nullptr;    // raw feature rows of the batched errors pass
         im.g.learned = g->learned ? g->lStats : nullptr;
         im.mlp = g->learned ? g->lPacked : nullptr;
         if (g->learned) b->anyLearned = true;

@@ -491,8 +491,12 @@ __global__ void __launch_bounds__(kThreads) k_batch_predict(const MdasBatchImage
         const int r = (t - s_pre[lo]) * kRows + threadIdx.x;
         const int leaf = !dirty ? r : (r < newL ? g.dirty[r] : (L - newL) + (r - newL));
         float f[kIn];
-        if (r < rows) leaf_feats<D>(g, leaf, L, f, nullptr);
-        else
+        if (r < rows) {
+            float raw[MDAS_RAW_FLOATS];  // the batched errors pass's row, or gathered
+            if (dirty && g.featRaw) load_raw(g.featRaw + (size_t)r * MDAS_RAW_FLOATS, raw);
+            else leaf_raw<D>(g, leaf, raw);
+            feats_of_raw<D>(g, raw, leaf, L, f);
+        } else
 #pragma unroll
             for (int i = 0; i < kIn; ++i) f[i] = 0.0f;
         put_features(c, f);
