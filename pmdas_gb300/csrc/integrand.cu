@@ -54,24 +54,25 @@ __device__ bool cull_may_cover(const MdasScene& sc, const float* p, float x0, fl
     return !(dist > reach + 1.0e-3f * scale);
 }
 
-// One thread per (tile, mask word).
+// One warp per (tile, mask word): lane b tests disc 32 * word + b, the
+// ballot is the word.
 __global__ void __launch_bounds__(256) k_build_cull(MdasScene sc, const float* __restrict__ prims,
                                                      unsigned* __restrict__ masks) {
     constexpr int T = MDAS_CULL_TILES;
     const int words = (sc.count + 31) / 32;
     const int total = T * T * words;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < total; i += warps) {
         const int tile = i / words, w = i - tile * words;
         const int tx = tile % T, ty = tile / T;
         const float pad = 1.0e-4f;
         const float x0 = (float)tx / T - pad, x1 = (float)(tx + 1) / T + pad;
         const float y0 = (float)ty / T - pad, y1 = (float)(ty + 1) / T + pad;
-        unsigned m = 0u;
-        for (int b = 0; b < 32; ++b) {
-            const int k = 32 * w + b;
-            if (k < sc.count && cull_may_cover(sc, prims + MDAS_PRIM_STRIDE * k, x0, x1, y0, y1)) m |= 1u << b;
-        }
-        masks[i] = m;
+        const int k = 32 * w + lane;
+        const bool may = k < sc.count && cull_may_cover(sc, prims + MDAS_PRIM_STRIDE * k, x0, x1, y0, y1);
+        const unsigned m = __ballot_sync(0xffffffffu, may);
+        if (lane == 0) masks[i] = m;
     }
 }
 
@@ -375,7 +376,8 @@ cudaError_t mdas_launch_build_cull(const MdasScene& sc, const float* d_prims, un
     const size_t words = mdas_cull_words(sc);
     if (words == 0) return cudaSuccess;
     if (!masks) return cudaErrorInvalidValue;
-    k_build_cull<<<(unsigned)((words + 255) / 256), 256, 0, s>>>(sc, d_prims, masks);
+    const size_t blocks = (words + 7) / 8;  // 8 warps per block, one mask word per warp
+    k_build_cull<<<(unsigned)(blocks < 8192 ? blocks : 8192), 256, 0, s>>>(sc, d_prims, masks);
     return cudaGetLastError();
 }
 
