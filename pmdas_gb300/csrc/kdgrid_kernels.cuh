@@ -160,8 +160,6 @@ __device__ __forceinline__ void nb_store(float* __restrict__ nb, int4 n, const f
     st_floats<4 + 2 * D>(nb, v);
 }
 
-__device__ __forceinline__ int4 nb_node(const float* __restrict__ nb) { return *reinterpret_cast<const int4*>(nb); }
-
 __device__ __forceinline__ void nb_set_node(float* __restrict__ nb, int4 n) { *reinterpret_cast<int4*>(nb) = n; }
 
 // AABB::Volume (aabb.h:20-25)

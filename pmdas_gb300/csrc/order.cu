@@ -46,24 +46,58 @@ __device__ __forceinline__ uint32_t quantize(float u, int B) {
     return (uint32_t)s;  // truncation = floor for s > 0
 }
 
-__device__ __forceinline__ uint64_t point_key(const float* p, const KeyParams& k) {
+// The 8 bits of v spread D apart (bit i to bit D * i): one entry of the table a
+// key kernel keeps in shared memory, so that a key takes one lookup per byte of
+// each coordinate instead of one step per bit.
+__device__ __forceinline__ uint64_t spread_byte(unsigned v, int D) {
+    uint64_t r = 0;
+    for (int i = 0; i < 8 && D * i < 64; ++i) r |= (uint64_t)((v >> i) & 1u) << (D * i);
+    return r;
+}
+
+// The bits of x at the even positions (bit i to bit 2i).
+__device__ __forceinline__ uint64_t spread_two(uint32_t x) {
+    uint64_t v = x;
+    v = (v | (v << 16)) & 0x0000FFFF0000FFFFull;
+    v = (v | (v << 8)) & 0x00FF00FF00FF00FFull;
+    v = (v | (v << 4)) & 0x0F0F0F0F0F0F0F0Full;
+    v = (v | (v << 2)) & 0x3333333333333333ull;
+    v = (v | (v << 1)) & 0x5555555555555555ull;
+    return v;
+}
+
+// Key of point p: bit b < K of dimension j's cell coordinate goes to bit
+// D * b + (D - 1 - j); the extra image bits b in [K, K + eib) of the two image
+// axes go to bit D * K + 2 (b - K) + 1 - j (the initial-cell numbering of
+// uniformSamplingKernel, kdgrid.cu:144-160, extended to K bits).  `spread`:
+// spread_byte(v, D) for v < 256.
+__device__ __forceinline__ uint64_t point_key(const float* p, const KeyParams& k, const uint64_t* spread) {
     uint64_t key = 0;
+    const uint32_t lowMask = k.K >= 32 ? 0xffffffffu : ((1u << k.K) - 1u);
     for (int j = 0; j < k.D; ++j) {
         float u = p[j];
         if (j == 0) u = __fdiv_rn(u, k.scaleX);
         if (j == 1) u = __fdiv_rn(u, k.scaleY);
         const int B = k.K + (j < 2 ? k.eib : 0);
         const uint32_t q = quantize(u, B);
-        for (int b = 0; b < k.K; ++b) key |= (uint64_t)((q >> b) & 1u) << (k.D * b + (k.D - 1 - j));
-        if (j < 2)
-            for (int b = k.K; b < B; ++b) key |= (uint64_t)((q >> b) & 1u) << (k.D * k.K + 2 * (b - k.K) + 1 - j);
+        const uint32_t low = q & lowMask;
+        for (int m = 0; 8 * m < k.K; ++m)
+            key |= spread[(low >> (8 * m)) & 0xffu] << (k.D * 8 * m + (k.D - 1 - j));
+        if (j < 2 && k.eib > 0) key |= spread_two(q >> k.K) << (k.D * k.K + 1 - j);
     }
     return key;
 }
 
+__device__ __forceinline__ void load_spread(uint64_t* s_spread, int D) {
+    for (int v = threadIdx.x; v < 256; v += blockDim.x) s_spread[v] = spread_byte((unsigned)v, D);
+    __syncthreads();
+}
+
 __global__ void k_morton_encode(const float* __restrict__ points, int n, KeyParams kp, uint64_t* __restrict__ keys) {
+    __shared__ uint64_t s_spread[256];
+    load_spread(s_spread, kp.D);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        keys[i] = point_key(points + (size_t)i * kp.D, kp);
+        keys[i] = point_key(points + (size_t)i * kp.D, kp, s_spread);
 }
 
 // The box of cell c at K bits per dimension, as uniformSamplingKernel
@@ -98,12 +132,14 @@ __global__ void k_morton_decode(const uint64_t* __restrict__ cells, int n, KeyPa
 template <int D>
 __global__ void k_leaf_keys(const float* __restrict__ nb, int nbFloats, int L, KeyParams kp,
                             uint64_t* __restrict__ keys) {
+    __shared__ uint64_t s_spread[256];
+    load_spread(s_spread, kp.D);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
         const float* box = nb + (size_t)i * nbFloats + 4;
         float c[D];
 #pragma unroll
         for (int j = 0; j < D; ++j) c[j] = __fmul_rn(0.5f, __fadd_rn(box[j], box[D + j]));
-        keys[i] = point_key(c, kp);
+        keys[i] = point_key(c, kp, s_spread);
     }
 }
 

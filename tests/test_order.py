@@ -222,7 +222,8 @@ def max_fine(D, bpd, eib):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("D,bpd,eib,F", [(3, 1, 4, 6), (4, 1, 8, 11), (5, 1, 3, 8), (6, 0, 5, 9), (4, 2, 0, 14)])
+@pytest.mark.parametrize("D,bpd,eib,F", [(3, 1, 4, 6), (4, 1, 8, 11), (5, 1, 3, 8), (6, 0, 5, 9), (4, 2, 0, 14),
+                                         (7, 1, 3, 7), (8, 0, 0, 8)])
 def test_morton_encode_decode_match_oracle(cuda, D, bpd, eib, F):
     torch = cuda
     rng = np.random.default_rng(D + F)
