@@ -257,11 +257,14 @@ __device__ __forceinline__ void run_mma(Ctx& c, int aOff, int bOff, int KB, int 
 }
 
 // Forward of the tile whose features this thread wrote as row threadIdx.x of SM_X:
-// z2 = the layer-2 pre-activations (b2 added).
-__device__ void tile_forward(Ctx& c, float (&z2)[kH]) {
+// z2 = the layer-2 pre-activations (b2 added).  between() runs after layer 1's
+// MMA completed and before layer 2's is issued (loads for the next tile).
+template <typename Between>
+__device__ __forceinline__ void tile_forward(Ctx& c, float (&z2)[kH], Between between) {
     const float* b1 = reinterpret_cast<const float*>(c.sm + SM_VEC);
     const float* b2 = b1 + kH;
     run_mma(c, SM_X, SM_W1, 2, 1);
+    between();
     float acc[kH];
     tmem_row(c, acc);
 #pragma unroll
@@ -272,6 +275,10 @@ __device__ void tile_forward(Ctx& c, float (&z2)[kH]) {
     tmem_row(c, z2);
 #pragma unroll
     for (int i = 0; i < kH; ++i) z2[i] += b2[i];
+}
+
+__device__ __forceinline__ void tile_forward(Ctx& c, float (&z2)[kH]) {
+    tile_forward(c, z2, [] {});
 }
 
 __device__ __forceinline__ float head(const Ctx& c, const float (&z2)[kH]) {
@@ -342,9 +349,17 @@ __device__ __forceinline__ void load_raw(const float* __restrict__ row, float (&
     }
 }
 
-// Features from the raw inputs and the errors of the leaf's slot neighbours.
+// The errors of the leaf's slot neighbours (slot -2, -1, +1, +2; the leaf's own
+// where a neighbour does not exist).
+__device__ __forceinline__ void nbr_errors(const MdasDeviceGrid& g, int leaf, int L, float e0, float (&ne)[4]) {
+    const int nbr[4] = {leaf - 2, leaf - 1, leaf + 1, leaf + 2};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ne[q] = nbr[q] >= 0 && nbr[q] < L ? g.errors[nbr[q]] : e0;
+}
+
+// Features from the raw inputs and the neighbours' errors.
 template <int D>
-__device__ void feats_of_raw(const MdasDeviceGrid& g, const float (&raw)[MDAS_RAW_FLOATS], int leaf, int L,
+__device__ void feats_of_raw(const MdasDeviceGrid& g, const float (&raw)[MDAS_RAW_FLOATS], const float (&ne)[4],
                              float (&f)[kIn]) {
     float depth = 0.0f;
 #pragma unroll
@@ -369,16 +384,16 @@ __device__ void feats_of_raw(const MdasDeviceGrid& g, const float (&raw)[MDAS_RA
     f[9] = n > 0.0f ? log2f(1.0f + fabsf(raw[10])) : 0.0f;
     f[10] = log2_err(raw[11]);
     f[11] = depth * (1.0f / 32.0f);
-    const int nbr[4] = {leaf - 2, leaf - 1, leaf + 1, leaf + 2};
 #pragma unroll
-    for (int q = 0; q < 4; ++q) f[12 + q] = nbr[q] >= 0 && nbr[q] < L ? log2_err(g.errors[nbr[q]]) : f[10];
+    for (int q = 0; q < 4; ++q) f[12 + q] = log2_err(ne[q]);
 }
 
 template <int D>
 __device__ void leaf_feats(const MdasDeviceGrid& g, int leaf, int L, float (&f)[kIn], float* err) {
-    float raw[MDAS_RAW_FLOATS];
+    float raw[MDAS_RAW_FLOATS], ne[4];
     leaf_raw<D>(g, leaf, raw);
-    feats_of_raw<D>(g, raw, leaf, L, f);
+    nbr_errors(g, leaf, L, raw[11], ne);
+    feats_of_raw<D>(g, raw, ne, f);
     if (err) *err = raw[11];
 }
 
@@ -414,7 +429,7 @@ __global__ void __launch_bounds__(kThreads) k_forward_rows(const Packed* __restr
 // before the first adaptive pass.  Lhost < 0: the leaf count in the device
 // counters.
 template <int D>
-__global__ void __launch_bounds__(kThreads) k_predict_leaves(MdasDeviceGrid g, int Lhost, int mode,
+__global__ void __launch_bounds__(kThreads, 4) k_predict_leaves(MdasDeviceGrid g, int Lhost, int mode,
                                                              const Packed* __restrict__ w, float* __restrict__ pred,
                                                              unsigned* status) {
     Ctx c;
@@ -425,15 +440,60 @@ __global__ void __launch_bounds__(kThreads) k_predict_leaves(MdasDeviceGrid g, i
     const int newL = g.counts->newL;
     const int rows = dirty ? 2 * newL : L;
     const int tiles = (rows + kRows - 1) / kRows;
+    auto leaf_of = [&](int r) { return !dirty ? r : (r < newL ? g.dirty[r] : (L - newL) + (r - newL)); };
+    if (rows_raw) {
+        // The rows of the errors pass: the next tile's row and leaf index are
+        // loaded while this tile's layer-1 MMA runs, its neighbours' errors
+        // after it, so a tile's inputs are at hand when its features are formed.
+        int tile = blockIdx.x;
+        int r = tile * kRows + threadIdx.x;
+        float raw[MDAS_RAW_FLOATS], ne[4];
+        int leaf = 0;
+        if (tile < tiles && r < rows) {
+            load_raw(g.featRaw + (size_t)r * MDAS_RAW_FLOATS, raw);
+            leaf = leaf_of(r);
+            nbr_errors(g, leaf, L, raw[11], ne);
+        }
+        for (; tile < tiles; tile += gridDim.x) {
+            float f[kIn];
+            if (r < rows) feats_of_raw<D>(g, raw, ne, f);
+            else
+#pragma unroll
+                for (int i = 0; i < kIn; ++i) f[i] = 0.0f;
+            put_features(c, f);
+            const int rNext = (tile + gridDim.x) * kRows + threadIdx.x;
+            const bool more = tile + gridDim.x < tiles && rNext < rows;
+            float rawNext[MDAS_RAW_FLOATS];
+            int leafNext = 0;
+            float z2[kH];
+            tile_forward(c, z2, [&] {
+                if (more) {
+                    load_raw(g.featRaw + (size_t)rNext * MDAS_RAW_FLOATS, rawNext);
+                    leafNext = leaf_of(rNext);
+                }
+            });
+            const float p = head(c, z2);
+            if (r < rows) pred[leaf] = f[10] + p;
+            if (more) {
+#pragma unroll
+                for (int i = 0; i < MDAS_RAW_FLOATS; ++i) raw[i] = rawNext[i];
+                leaf = leafNext;
+                nbr_errors(g, leaf, L, raw[11], ne);
+            }
+            r = rNext;
+        }
+        ctx_close(c);
+        return;
+    }
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const int r = tile * kRows + threadIdx.x;
-        const int leaf = !dirty ? r : (r < newL ? g.dirty[r] : (L - newL) + (r - newL));
+        const int leaf = leaf_of(r);
         float f[kIn];
         if (r < rows) {
-            float raw[MDAS_RAW_FLOATS];
-            if (rows_raw) load_raw(g.featRaw + (size_t)r * MDAS_RAW_FLOATS, raw);
-            else leaf_raw<D>(g, leaf, raw);
-            feats_of_raw<D>(g, raw, leaf, L, f);
+            float raw[MDAS_RAW_FLOATS], ne[4];
+            leaf_raw<D>(g, leaf, raw);
+            nbr_errors(g, leaf, L, raw[11], ne);
+            feats_of_raw<D>(g, raw, ne, f);
         } else
 #pragma unroll
             for (int i = 0; i < kIn; ++i) f[i] = 0.0f;
@@ -451,7 +511,7 @@ __global__ void __launch_bounds__(kThreads) k_predict_leaves(MdasDeviceGrid g, i
 // mode 2 above); a CTA reloads the weights when its tile belongs to an image
 // with other weights.
 template <int D>
-__global__ void __launch_bounds__(kThreads) k_batch_predict(const MdasBatchImage* __restrict__ imgs, int n,
+__global__ void __launch_bounds__(kThreads, 4) k_batch_predict(const MdasBatchImage* __restrict__ imgs, int n,
                                                             unsigned* status) {
     __shared__ int s_pre[257];
     if (threadIdx.x == 0) {
@@ -492,10 +552,11 @@ __global__ void __launch_bounds__(kThreads) k_batch_predict(const MdasBatchImage
         const int leaf = !dirty ? r : (r < newL ? g.dirty[r] : (L - newL) + (r - newL));
         float f[kIn];
         if (r < rows) {
-            float raw[MDAS_RAW_FLOATS];  // the batched errors pass's row, or gathered
+            float raw[MDAS_RAW_FLOATS], ne[4];  // the batched errors pass's row, or gathered
             if (dirty && g.featRaw) load_raw(g.featRaw + (size_t)r * MDAS_RAW_FLOATS, raw);
             else leaf_raw<D>(g, leaf, raw);
-            feats_of_raw<D>(g, raw, leaf, L, f);
+            nbr_errors(g, leaf, L, raw[11], ne);
+            feats_of_raw<D>(g, raw, ne, f);
         } else
 #pragma unroll
             for (int i = 0; i < kIn; ++i) f[i] = 0.0f;
