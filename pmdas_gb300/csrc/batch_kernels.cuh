@@ -67,12 +67,13 @@ __device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; 
 template <int D>
 __global__ void __launch_bounds__(256) k_batch_init(const MdasBatchImage* __restrict__ imgs, int n) {
     __shared__ __align__(16) float s_coords[256 * 4 * D];
+    __shared__ float s_box[256 * 2 * D];
     __shared__ int s_pre[MDAS_MAX_BATCH + 1];
     __shared__ unsigned s_warp[8];
     const int total = batch_prefix(n, s_pre, s_warp, [&](int i) { return ceil_div(imgs[i].initialLeaves, 256); });
     for (int c = blockIdx.x; c < total; c += gridDim.x) {
         const int i = batch_image_of(s_pre, n, c);
-        init_chunk<D>(imgs[i].g, imgs[i].initialLeaves, (c - s_pre[i]) * 256, s_coords);
+        init_chunk<D>(imgs[i].g, imgs[i].initialLeaves, (c - s_pre[i]) * 256, s_coords, s_box);
     }
 }
 
@@ -352,14 +353,19 @@ __global__ void k_batch_clear_pixels(const MdasBatchImage* __restrict__ imgs, in
 
 template <int D>
 __global__ void __launch_bounds__(256) k_batch_integrate(const MdasBatchImage* __restrict__ imgs, int n) {
+    constexpr int H4 = (4 + 2 * D + 3) / 4;
     __shared__ int s_pre[MDAS_MAX_BATCH + 1];
     __shared__ unsigned s_warp[8];
+    __shared__ float4 s_head[8][32 * H4];
     const int total = batch_prefix(n, s_pre, s_warp, [&](int i) { return ceil_div(imgs[i].g.counts->L, 256); });
+    const int warp = threadIdx.x >> 5;
     for (int c = blockIdx.x; c < total; c += gridDim.x) {
         const int i = batch_image_of(s_pre, n, c);
-        const int leaf = (c - s_pre[i]) * 256 + threadIdx.x;
-        if (leaf < imgs[i].g.counts->L)
-            integrate_leaf<D>(imgs[i].g, leaf, imgs[i].pixels, imgs[i].width, imgs[i].height);
+        const int first = (c - s_pre[i]) * 256 + 32 * warp;
+        int4 node;
+        float mn[D], mx[D];
+        if (warp_leaf_head<D>(imgs[i].g.nb, first, imgs[i].g.counts->L, s_head[warp], node, mn, mx))
+            integrate_leaf<D>(imgs[i].g, node, mn, mx, imgs[i].pixels, imgs[i].width, imgs[i].height);
     }
 }
 

@@ -218,7 +218,6 @@ void free_grid(mdas_grid* g) {
     cudaFree(g->dg.coords);
     cudaFree(g->dg.values);
     cudaFree(g->dg.nb);
-    cudaFree(g->dg.lsc);
     cudaFree(g->dg.errors);
     cudaFree(g->dg.leafCounts);
     cudaFree(g->dg.seeds);
@@ -330,7 +329,6 @@ int mdas_create_ex(mdas_grid** out, int dim, int maxSamples, int candidatesNum, 
     bool ok = cudaMalloc(&d.coords, sizeof(float) * capSamples * dim) == cudaSuccess &&
               cudaMalloc(&d.values, sizeof(float) * 3 * capSamples) == cudaSuccess &&
               cudaMalloc(&d.nb, sizeof(float) * (size_t)d.nbFloats * (size_t)d.maxNodes) == cudaSuccess &&
-              cudaMalloc(&d.lsc, sizeof(float) * 4 * dim * (size_t)d.maxNodes) == cudaSuccess &&
               cudaMalloc(&d.errors, sizeof(float) * (size_t)d.maxNodes) == cudaSuccess &&
               cudaMalloc(&d.leafCounts, (size_t)d.maxNodes + 16) == cudaSuccess &&
               cudaMalloc(&d.seeds, sizeof(unsigned) * (size_t)d.maxNodes) == cudaSuccess &&

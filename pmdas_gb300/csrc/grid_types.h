@@ -68,9 +68,9 @@ struct MdasDeviceGrid {
     float scaleY;
     float* coords;        // [capSamples * D], AoS like the reference's Point buffer
     float* values;        // [capSamples * 3], float3
-    float* nb;            // [maxNodes * nbFloats], per leaf: node (4 sample indices) + box
-    int nbFloats;         // floats per node + box record
-    float* lsc;           // [maxNodes * 4D], per leaf: coordinates of its samples in node-slot order
+    float* nb;            // [maxNodes * nbFloats], per leaf: node (4 sample indices), box, and the
+                          // coordinates of its samples in node-slot order
+    int nbFloats;         // floats per leaf record
     float* errors;        // [maxNodes], < 0 = needs recomputation
     unsigned char* leafCounts;  // [maxNodes + 16], samples per leaf (the node's non-empty slots)
     unsigned* seeds;      // [maxNodes], 0 = not drawn yet
