@@ -462,7 +462,6 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
     constexpr int kMaxNodeSize = 4;  // KDGrid ctor: maxNodeSize(4), kdgrid.cu:611
     constexpr int K = MDAS_LEAVES_PER_THREAD;
     constexpr int TILE = MDAS_TILE_LEAVES;
-    constexpr int NB = NbLayout<D>::FLOATS;
     static_assert(TILE == 256 * K && TILE <= 2048, "tile = 256 threads x K leaves, local index in 11 bits");
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;

@@ -26,7 +26,10 @@
 #define MDAS_MLP_OFF_B2 (MDAS_MLP_OFF_W2 + MDAS_MLP_HIDDEN * MDAS_MLP_HIDDEN)
 #define MDAS_MLP_OFF_W3 (MDAS_MLP_OFF_B2 + MDAS_MLP_HIDDEN)
 #define MDAS_MLP_OFF_B3 (MDAS_MLP_OFF_W3 + MDAS_MLP_HIDDEN)
-#define MDAS_MLP_PARAMS (MDAS_MLP_OFF_B3 + 1)  // 5313
+#ifndef MDAS_MLP_PARAMS
+#define MDAS_MLP_PARAMS 5313  // as include/mdas.h declares it
+#endif
+static_assert(MDAS_MLP_OFF_B3 + 1 == MDAS_MLP_PARAMS, "the layout above fills the parameter vector");
 // priorities, network outputs and training targets are log2 quantities / MDAS_MLP_TARGET_SCALE
 #define MDAS_MLP_TARGET_SCALE 32.0f
 
