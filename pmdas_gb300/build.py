@@ -43,7 +43,7 @@ UNITS = [
     ("mlp.cu", []),
 ]
 CXX_UNITS = ["env.cpp"]
-HEADERS = ["grid_types.h", "ieee_math.h", "integrand.h", "kdgrid_kernels.cuh", "batch_kernels.cuh", "scene.h", "order.h", "mlp.h", "leaf_raw.h"]
+HEADERS = ["grid_types.h", "ieee_math.h", "integrand.h", "kdgrid_kernels.cuh", "batch_kernels.cuh", "scene.h", "order.h", "mlp.h", "leaf_raw.h", "ld_hint.h"]
 
 
 def nvcc() -> str:

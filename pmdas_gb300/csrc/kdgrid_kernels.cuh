@@ -37,6 +37,7 @@
 #include "grid_types.h"
 #include "ieee_math.h"
 #include "leaf_raw.h"
+#include "ld_hint.h"
 
 #ifndef MDAS_NS
 #error "define MDAS_NS before including kdgrid_kernels.cuh"
@@ -77,28 +78,6 @@ __device__ __forceinline__ float rnd(unsigned& prev) { return (float)lcg(prev) /
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 // Lets the next kernel (if launched programmatically) be scheduled now.
 __device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
-
-// ---- 16-byte loads with an L2 prefetch-size hint (PTX ld .L2::64B / ::128B /
-// ::256B; 0: none given).  A leaf record's head (node and box, 48 bytes at
-// D = 4) read with the 64-byte hint fetches its two sectors only: without a
-// hint, strided streams over the 128-byte records fetched more.  The "memory"
-// clobber keeps the load ordered with this thread's own stores to the record.
-template <int HINT>
-__device__ __forceinline__ float4 ld4_hint(const float* p) {
-    float4 v;
-    if constexpr (HINT == 64)
-        asm volatile("ld.global.L2::64B.v4.f32 {%0,%1,%2,%3}, [%4];"
-                     : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p) : "memory");
-    else if constexpr (HINT == 128)
-        asm volatile("ld.global.L2::128B.v4.f32 {%0,%1,%2,%3}, [%4];"
-                     : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p) : "memory");
-    else if constexpr (HINT == 256)
-        asm volatile("ld.global.L2::256B.v4.f32 {%0,%1,%2,%3}, [%4];"
-                     : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p) : "memory");
-    else
-        v = *reinterpret_cast<const float4*>(p);
-    return v;
-}
 
 // ---- vector loads and stores of NF floats from a 16-byte aligned address ---------
 template <int NF, int HINT = 0>

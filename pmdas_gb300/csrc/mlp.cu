@@ -19,6 +19,7 @@
 // with atomics.
 #include "mlp.h"
 #include "leaf_raw.h"
+#include "ld_hint.h"
 
 #include <cuda_bf16.h>
 #include <float.h>
@@ -309,13 +310,14 @@ __device__ __forceinline__ float log2_err(float e) { return log2f(fmaxf(e, 1e-30
 // and sample values.
 template <int D>
 __device__ __forceinline__ void leaf_raw(const MdasDeviceGrid& g, int leaf, float (&raw)[MDAS_RAW_FLOATS]) {
-    const float* nb = g.nb + (size_t)leaf * g.nbFloats;
-    const int4 node = *reinterpret_cast<const int4*>(nb);
+    float h[(4 + 2 * D + 3) / 4 * 4];  // node and box (the record extends past them)
+    ld_head64<4 + 2 * D>(g.nb + (size_t)leaf * g.nbFloats, h);
+    const int4 node = make_int4(__float_as_int(h[0]), __float_as_int(h[1]), __float_as_int(h[2]), __float_as_int(h[3]));
     float mn[D], mx[D];
 #pragma unroll
     for (int j = 0; j < D; ++j) {
-        mn[j] = nb[4 + j];
-        mx[j] = nb[4 + D + j];
+        mn[j] = h[4 + j];
+        mx[j] = h[4 + D + j];
     }
     const int idx[4] = {node.x, node.y, node.z, node.w};
     MdasLumStats s = mdas_lum_empty();

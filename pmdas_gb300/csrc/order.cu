@@ -3,6 +3,7 @@
 // depend on one division and one multiplication per coordinate, which a CPU
 // restatement must be able to repeat bit for bit).
 #include "order.h"
+#include "ld_hint.h"
 
 namespace mdas_order {
 
@@ -135,10 +136,11 @@ __global__ void k_leaf_keys(const float* __restrict__ nb, int nbFloats, int L, K
     __shared__ uint64_t s_spread[256];
     load_spread(s_spread, kp.D);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
-        const float* box = nb + (size_t)i * nbFloats + 4;
+        float h[(4 + 2 * D + 3) / 4 * 4];  // node and box of the record (it extends past them)
+        ld_head64<4 + 2 * D>(nb + (size_t)i * nbFloats, h);
         float c[D];
 #pragma unroll
-        for (int j = 0; j < D; ++j) c[j] = __fmul_rn(0.5f, __fadd_rn(box[j], box[D + j]));
+        for (int j = 0; j < D; ++j) c[j] = __fmul_rn(0.5f, __fadd_rn(h[4 + j], h[4 + D + j]));
         keys[i] = point_key(c, kp, s_spread);
     }
 }
