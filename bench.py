@@ -111,8 +111,8 @@ class ClockSampler:
 # DRAM traffic of the dominant stage per pass, from the committed ncu capture of
 # every launch (dram__bytes_read.sum + dram__bytes_write.sum, mean per pass of
 # decide + scan + place): profiles/kernels_dram_dof1024.md
-MEASURED_TRAFFIC = {"dof1024": (207.0e6, "profiles/kernels_dram_dof1024.md (ncu: decide 27.7 + scan 0.0 + place "
-                                         "179.3 MB, mean per pass)")}
+MEASURED_TRAFFIC = {"dof1024": (139.0e6, "profiles/kernels_dram_dof1024.md (ncu: decide 27.7 + scan 0.0 + place "
+                                         "111.3 MB, mean per pass)")}
 
 
 def workload_label(wl) -> str:
