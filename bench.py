@@ -431,6 +431,9 @@ def time_to_target(points, target):
     return None, None
 
 
+LADDER_REPEATS = 3  # timed renders per ladder point (after one warm-up render)
+
+
 def learned_block(peaks: dict, name: str = "mbdof1080", batched: bool = False,
                   ladder=(16, 32, 64, 128, 256, 512), target: float = 1e-3, host: bool = False) -> dict:
     """Time to rel-MSE `target`, learned vs plain, on one workload (its scene seed
@@ -480,19 +483,22 @@ def learned_block(peaks: dict, name: str = "mbdof1080", batched: bool = False,
                 return P.render_graph(g, scene, budget, pixels, W, H)
 
             render()  # build + warm
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record()
-            st = render()
-            b.record()
-            torch.cuda.synchronize()
-            ms = a.elapsed_time(b)
+            times = []
+            for _ in range(LADDER_REPEATS):  # median of a few renders: one render can catch a stall
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                st = render()
+                b.record()
+                torch.cuda.synchronize()
+                times.append(a.elapsed_time(b))
+            ms = statistics.median(times)
             img = pixels[..., :3].double()
             rel = float(torch.nan_to_num((ref - img) ** 2 / (ref ** 2 + 1e-2), nan=0.0).mean().item())
             row = {"spp": spp, "samples": st.numberOfSamples, "passes": st.passes, "ms": round(ms, 3),
                    "rel_mse": rel}
             if mode == "learned":
                 ls = g.LearnedStats()
-                row["passes_judged_plain"] = ls["plain"] // 2  # two renders
+                row["passes_judged_plain"] = ls["plain"] // (1 + LADDER_REPEATS)  # every render judged alike
             rows.append(row)
             pts.append((ms, rel))
             if batch is not None:

@@ -592,11 +592,12 @@ template <int D, bool READONLY = false>
 __device__ __forceinline__ void child_box(const MdasDeviceGrid& g, const uint32_t* __restrict__ order, const float* boxes,
                                           int c, float (&mn)[D], float (&mx)[D]) {
     if (c < 0) {
-        const float* b = g.nb + (size_t)order[~c] * g.nbFloats + 4;
+        float h[(4 + 2 * D + 3) / 4 * 4];  // the leaf record's node and box (the record extends past them)
+        ld_head64<4 + 2 * D>(g.nb + (size_t)order[~c] * g.nbFloats, h);
 #pragma unroll
         for (int j = 0; j < D; ++j) {
-            mn[j] = b[j];
-            mx[j] = b[D + j];
+            mn[j] = h[4 + j];
+            mx[j] = h[4 + D + j];
         }
     } else {
         const float* b = boxes + (size_t)c * 2 * D;
