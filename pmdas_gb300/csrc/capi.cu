@@ -862,7 +862,7 @@ int build_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, i
     const int gDecide = g->numSMs * (g->occ[MDAS_K_DECIDE] > 0 ? g->occ[MDAS_K_DECIDE] : 1);
     const int gPlace = g->numSMs * (g->occ[MDAS_K_ADAPTIVE] > 0 ? g->occ[MDAS_K_ADAPTIVE] : 1);
     const int gInt = g->numSMs * (g->occ[MDAS_K_INTEGRATE] > 0 ? g->occ[MDAS_K_INTEGRATE] : 1);
-    const int gEval = g->numSMs * 8;
+    const int gEval = g->numSMs * 16;  // integrand CTAs (16 per SM measured 1 % faster per render than 8)
     cudaStream_t cs = g->captureStream, bs = g->bodyStream;
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
