@@ -373,11 +373,14 @@ void integrate(int L, int W, int H, float sx, float sy, const int* nodes, const 
 }
 
 // ---- KDGrid::Validate, kdgrid.cu:848-961 -------------------------------------------
+// The leaf volumes are summed in double: the reference's float sum (:858, :903) drifts
+// past its own 1 % tolerance (:910) at a few million leaves (about 1.2 % at 6 M
+// leaves of similar size), which would fail a valid partition.
 template <int D>
 int validate(int N, int L, float sx, float sy, const float* coords, const int* nodes, const float* boxes) {
     int bad = 0;
     std::vector<int> hist((size_t)N, 0);
-    float totalVolume = 0.0f;
+    double totalVolume = 0.0;
     int64_t total = 0;
     for (int k = 0; k < L; ++k) {
         const float* box = boxes + (int64_t)k * 2 * D;
@@ -398,8 +401,8 @@ int validate(int N, int L, float sx, float sy, const float* coords, const int* n
         }
         totalVolume += box_volume<D>(box);
     }
-    const float rootVolume = sx * sy;
-    if (fabsf(totalVolume - rootVolume) > 1.0e-2f * rootVolume) bad |= 2;
+    const double rootVolume = (double)(sx * sy);
+    if (fabs(totalVolume - rootVolume) > 1.0e-2 * rootVolume) bad |= 2;
     if (total != N) bad |= 4;
     for (int i = 0; i < N; ++i)
         if (hist[i] != 1) bad |= 4;

@@ -643,7 +643,9 @@ int mdas_validate(mdas_grid* g, int* valid) {
     if (rc) return rc;
     bool ok = true;
     std::vector<int> hist(N, 0);
-    float totalVolume = 0.0f;
+    // summed in double: the reference's float sum (kdgrid.cu:858, :903) drifts past its
+    // own 1 % tolerance (:910) at a few million leaves
+    double totalVolume = 0.0;
     size_t total = 0;
     for (size_t k = 0; k < L; ++k) {
         const float* box = boxes.data() + k * 2 * D;
@@ -665,8 +667,8 @@ int mdas_validate(mdas_grid* g, int* valid) {
             total++;
         }
     }
-    const float rootVolume = g->dg.scaleX * g->dg.scaleY;
-    if (fabsf(totalVolume - rootVolume) > 1.0e-2f * rootVolume) ok = false;
+    const double rootVolume = (double)(g->dg.scaleX * g->dg.scaleY);
+    if (fabs(totalVolume - rootVolume) > 1.0e-2 * rootVolume) ok = false;
     if (total != N) ok = false;
     for (size_t i = 0; i < N; ++i)
         if (hist[i] != 1) ok = false;

@@ -357,3 +357,85 @@ def test_device_views_and_stream(cuda):
     g.SamplingPass()
     assert g.GetNewSamples() > 0 and g.Validate()
     assert g.launch_count() >= 4
+
+
+# ---- the dof1024 workload at full size (4-D, 1024x1024, 16 spp) ---------------------
+def _full_size(arith):
+    from pmdas_gb300.workloads import WORKLOADS
+    w = WORKLOADS["dof1024"]
+    g = P.KDGrid(w.dim, w.maxSamples, w.candidatesNum, w.bitsPerDim, w.extraImgBits, w.alpha, w.scaleX, w.scaleY,
+                 arith=arith)
+    sc = P.Scene(w.scene_kind, w.scene_seed, w.scene_count, w.scaleX, w.scaleY, w.width, w.height)
+    return w, g, sc
+
+
+@pytest.mark.slow
+def test_full_size_graph_equals_host_loop_and_partitions(cuda):
+    """16.8 M samples in about 6 M leaves, checked through properties that need
+    no CPU restatement: the device-side loop and the host loop end in the same
+    state bit for bit, the images agree within the atomic-order tolerance, and
+    the leaves partition the domain with every sample in exactly one leaf,
+    inside its box."""
+    torch = cuda
+    w, a, sc = _full_size(P.ARITH_REFERENCE)
+    _, b, _ = _full_size(P.ARITH_REFERENCE)
+    pa = torch.zeros(w.height, w.width, 4, device="cuda")
+    pb = torch.zeros(w.height, w.width, 4, device="cuda")
+    sa = P.render_graph(a, sc, w.budget, pa, w.width, w.height)
+    sb = P.render(b, sc, w.budget, pb, w.width, w.height)
+    assert (sa.numberOfSamples, sa.numberOfNodes, sa.passes) == (sb.numberOfSamples, sb.numberOfNodes, sb.passes)
+    assert sa.numberOfSamples >= w.budget and sa.numberOfNodes > 4_000_000
+    assert_states_equal(a.dump_state(), b.dump_state(), keys=("coords", "values", "nodes", "boxes", "errors", "seeds"),
+                        what="dof1024 graph vs host loop")
+    ok, worst = rel_close(pa.cpu().numpy(), pb.cpu().numpy())
+    assert ok, worst
+    assert torch.isfinite(pa).all() and float(pa[..., :3].min()) >= 0.0
+    assert a.Validate()
+
+
+@pytest.mark.slow
+def test_full_size_pass_matches_reference_kernels(cuda, refgrid_cls):
+    """From the final state of a full-size dof1024 render: one more errors pass
+    and adaptive pass equal the reference's kernels on the same state (slot
+    order canonicalised), and the reconstruction agrees within 1e-5."""
+    torch = cuda
+    w, g, sc = _full_size(P.ARITH_REFERENCE)
+    px = torch.zeros(w.height, w.width, 4, device="cuda")
+    P.render_graph(g, sc, w.budget, px, w.width, w.height)
+    ref = refgrid_cls(w.dim, w.maxSamples, w.candidatesNum, w.bitsPerDim, w.extraImgBits, w.alpha, w.scaleX, w.scaleY)
+    try:
+        s0 = g.dump_state()
+        ref.load_state(s0)
+        rpx = torch.zeros(w.height, w.width, 4, device="cuda")
+        assert refgrid_cls.lib().ref_integrate(ref.h, rpx.data_ptr(), w.width, w.height) == 0
+        g.Integrate(px, w.width, w.height)
+        ok, worst = rel_close(px.cpu().numpy(), rpx.cpu().numpy())
+        assert ok, worst
+        gref = ref.compute_errors()
+        g.ComputeErrors()
+        assert g.GetGError() == gref
+        assert np.array_equal(g.dump_state()["errors"].view(np.uint32), ref.dump_state()["errors"].view(np.uint32))
+        ref.adaptive_sampling()
+        g.AdaptiveSampling()
+        assert_pass_equivalent(s0, g.dump_state(), ref.dump_state(), w.dim, what="dof1024 full-size pass")
+        assert g.Validate()
+    finally:
+        ref.close()
+
+
+@pytest.mark.slow
+def test_full_size_ieee_pass_matches_oracle(cuda):
+    """The strict-IEEE build at full size: from the final state of a dof1024
+    render, one more sampling pass (errors, acceptance, candidates, splits over
+    about 6 M leaves) is the CPU oracle's, bit for bit and slot for slot."""
+    torch = cuda
+    w, g, sc = _full_size(P.ARITH_IEEE)
+    P.render_graph(g, sc, w.budget, torch.zeros(w.height, w.width, 4, device="cuda"), w.width, w.height)
+    o = O.OracleGrid(w.dim, w.maxSamples, w.candidatesNum, w.bitsPerDim, w.extraImgBits, w.alpha, w.scaleX, w.scaleY)
+    o.load_state(g.dump_state())
+    g.SamplingPass()
+    o.sampling_pass()
+    assert g.GetGError() == o.gerr
+    assert g.GetNewSamples() == o.newN > 0
+    assert_states_equal(g.dump_state(), o.dump_state(), keys=("coords", "nodes", "boxes", "errors", "seeds"),
+                        what="dof1024 full-size pass vs oracle")

@@ -333,3 +333,37 @@ def test_oracle_render_invariants():
     px, n, l, passes, t, _ = O.render(3, 1, 3, 4, 0.25, W, H, 8 * W * H, 60000, sc, W, H, threads=2)
     assert n >= 8 * W * H and passes > 0
     assert np.all(np.isfinite(px)) and px[..., :3].min() >= 0.0 and px[..., :3].max() <= 1.0 + 1e-5
+
+
+def test_validate_sums_volumes_without_drift():
+    """A valid partition of the image into 2048 x 2048 cells of uneven size: a
+    float running sum of the cell volumes drifts past the 1 % tolerance of the
+    volume check, the oracle's (and the library's) double sum does not, so the
+    partition passes; a missing cell still fails it."""
+    D, n, sx, sy = 3, 2048, 1024.0, 1024.0
+    rng = np.random.default_rng(5)
+
+    def cuts(extent):
+        w = rng.integers(1, 8, n).astype(np.float64)
+        c = np.concatenate([[0.0], np.cumsum(w) / w.sum() * extent]).astype(np.float32)
+        c[-1] = np.float32(extent)
+        return c
+
+    cx, cy = cuts(sx), cuts(sy)
+    iy, ix = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    ix, iy = ix.ravel(), iy.ravel()
+    L = n * n
+    boxes = np.zeros((L, 2 * D), np.float32)
+    boxes[:, 0], boxes[:, D] = cx[ix], cx[ix + 1]
+    boxes[:, 1], boxes[:, D + 1] = cy[iy], cy[iy + 1]
+    boxes[:, D + 2] = 1.0
+    vol = (boxes[:, D] - boxes[:, 0]) * (boxes[:, D + 1] - boxes[:, 1]) * (boxes[:, D + 2] - boxes[:, 2])
+    drift = abs(float(np.cumsum(vol, dtype=np.float32)[-1]) - sx * sy) / (sx * sy)
+    assert drift > 1e-2, drift  # the float sum would reject this partition
+    coords = np.ascontiguousarray(0.5 * (boxes[:, :D] + boxes[:, D:]), np.float32)
+    nodes = np.full((L, 4), ~D, np.int32)
+    nodes[:, 0] = np.arange(L, dtype=np.int32)
+    v = lambda m: O.load().orc_validate(D, m, m, np.float32(sx), np.float32(sy), coords.ctypes.data,
+                                        nodes.ctypes.data, boxes.ctypes.data)
+    assert v(L) == 0
+    assert v(L - 128 * n) & 2  # the last 128 rows of cells (about 6 % of the volume) are missing
