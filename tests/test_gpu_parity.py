@@ -360,9 +360,9 @@ def test_device_views_and_stream(cuda):
 
 
 # ---- the dof1024 workload at full size (4-D, 1024x1024, 16 spp) ---------------------
-def _full_size(arith):
+def _full_size(arith, name="dof1024"):
     from pmdas_gb300.workloads import WORKLOADS
-    w = WORKLOADS["dof1024"]
+    w = WORKLOADS[name]
     g = P.KDGrid(w.dim, w.maxSamples, w.candidatesNum, w.bitsPerDim, w.extraImgBits, w.alpha, w.scaleX, w.scaleY,
                  arith=arith)
     sc = P.Scene(w.scene_kind, w.scene_seed, w.scene_count, w.scaleX, w.scaleY, w.width, w.height)
@@ -394,12 +394,14 @@ def test_full_size_graph_equals_host_loop_and_partitions(cuda):
 
 
 @pytest.mark.slow
-def test_full_size_pass_matches_reference_kernels(cuda, refgrid_cls):
-    """From the final state of a full-size dof1024 render: one more errors pass
+@pytest.mark.parametrize("name", ["dof1024", "mbdof1080"])
+def test_full_size_pass_matches_reference_kernels(cuda, refgrid_cls, name):
+    """From the final state of a full-size render (dof1024: 4-D, 16.8 M samples;
+    mbdof1080: 5-D, 1920x1080 at 32 spp, 66 M samples): one more errors pass
     and adaptive pass equal the reference's kernels on the same state (slot
     order canonicalised), and the reconstruction agrees within 1e-5."""
     torch = cuda
-    w, g, sc = _full_size(P.ARITH_REFERENCE)
+    w, g, sc = _full_size(P.ARITH_REFERENCE, name)
     px = torch.zeros(w.height, w.width, 4, device="cuda")
     P.render_graph(g, sc, w.budget, px, w.width, w.height)
     ref = refgrid_cls(w.dim, w.maxSamples, w.candidatesNum, w.bitsPerDim, w.extraImgBits, w.alpha, w.scaleX, w.scaleY)
@@ -417,19 +419,20 @@ def test_full_size_pass_matches_reference_kernels(cuda, refgrid_cls):
         assert np.array_equal(g.dump_state()["errors"].view(np.uint32), ref.dump_state()["errors"].view(np.uint32))
         ref.adaptive_sampling()
         g.AdaptiveSampling()
-        assert_pass_equivalent(s0, g.dump_state(), ref.dump_state(), w.dim, what="dof1024 full-size pass")
+        assert_pass_equivalent(s0, g.dump_state(), ref.dump_state(), w.dim, what=f"{name} full-size pass")
         assert g.Validate()
     finally:
         ref.close()
 
 
 @pytest.mark.slow
-def test_full_size_ieee_pass_matches_oracle(cuda):
-    """The strict-IEEE build at full size: from the final state of a dof1024
-    render, one more sampling pass (errors, acceptance, candidates, splits over
-    about 6 M leaves) is the CPU oracle's, bit for bit and slot for slot."""
+@pytest.mark.parametrize("name", ["dof1024", "mbdof1080"])
+def test_full_size_ieee_pass_matches_oracle(cuda, name):
+    """The strict-IEEE build at full size: from the final state of a render,
+    one more sampling pass (errors, acceptance, candidates, splits over all its
+    leaves) is the CPU oracle's, bit for bit and slot for slot."""
     torch = cuda
-    w, g, sc = _full_size(P.ARITH_IEEE)
+    w, g, sc = _full_size(P.ARITH_IEEE, name)
     P.render_graph(g, sc, w.budget, torch.zeros(w.height, w.width, 4, device="cuda"), w.width, w.height)
     o = O.OracleGrid(w.dim, w.maxSamples, w.candidatesNum, w.bitsPerDim, w.extraImgBits, w.alpha, w.scaleX, w.scaleY)
     o.load_state(g.dump_state())
@@ -438,4 +441,4 @@ def test_full_size_ieee_pass_matches_oracle(cuda):
     assert g.GetGError() == o.gerr
     assert g.GetNewSamples() == o.newN > 0
     assert_states_equal(g.dump_state(), o.dump_state(), keys=("coords", "nodes", "boxes", "errors", "seeds"),
-                        what="dof1024 full-size pass vs oracle")
+                        what=f"{name} full-size pass vs oracle")
