@@ -111,8 +111,8 @@ class ClockSampler:
 # DRAM traffic of the dominant stage per pass, from the committed ncu capture of
 # every launch (dram__bytes_read.sum + dram__bytes_write.sum, mean per pass of
 # decide + scan + place): profiles/kernels_dram_dof1024.md
-MEASURED_TRAFFIC = {"dof1024": (139.0e6, "profiles/kernels_dram_dof1024.md (ncu: decide 27.7 + scan 0.0 + place "
-                                         "111.3 MB, mean per pass)")}
+MEASURED_TRAFFIC = {"dof1024": (144.9e6, "profiles/kernels_dram_dof1024.md (ncu: decide 27.7 + scan 0.0 + place "
+                                         "117.2 MB, mean per pass)")}
 
 
 def workload_label(wl) -> str:
@@ -125,27 +125,30 @@ def stage_bytes(D: int, W: int, H: int, L0: int, passes: list, N_final: int, L_f
 
     init     : per initial leaf 4 samples * D floats + node 16 + box 8D + error 4 + seed 4 + sample count 1
                = 24D + 25
-    errors   : first pass (every leaf): error read 4 per leaf; later passes visit only the split
-               children (whose errors the pass set to -1, not read): dirty-list entry 4 per split; per recomputed
-               leaf error write 4 + node 16 + box 8D + its sample values (12 B each; 4 per leaf
-               on the first pass, 5 per split pair after)
+    errors   : first pass (every leaf): error read 4 per leaf, per recomputed leaf error write 4 +
+               node 16 + box 8D + its 4 sample values (12 B each); later passes visit only the split
+               children (whose errors the pass set to -1, not read): per child its split-list entry
+               16 (sample indices, slot, box volume), error write 4 and its sample values (5 per
+               split pair)
     adaptive : error + seed read, seed write, sample count read: 13 per leaf; per accepted leaf:
                its entry in the accepted list written and read 16, node + box 16 + 8D, new
                coordinate 4D, 4D per sample coordinate it holds (its private copy); per append:
                node 16 + the new coordinate in the private copy 4D + count 1; per split: left
                node 16 + left mx 4 + left copy 8D + right node + box 16 + 8D + right copy 12D +
-               two errors 8 + right seed 4 + dirty entry 4 + two counts 2
+               two errors 8 + right seed 4 + dirty entry 4 + two counts 2 + two split-list
+               entries 32
     integrate: per leaf node 16 + box 8D, 12 per sample value, pixels cleared and written 32 per pixel
     """
     init = L0 * (24 * D + 25)
     err = adap = 0
     for k, p in enumerate(passes):
         L, R = p["L"], p["recomputed"]
-        V = 4 * R if k == 0 else (5 * R) // 2
-        scan = 4 * L if k == 0 else 2 * R
-        err += scan + R * (4 + 16 + 8 * D) + 12 * V
+        if k == 0:
+            err += 4 * L + R * (4 + 16 + 8 * D) + 12 * 4 * R
+        else:
+            err += R * (16 + 4) + 12 * ((5 * R) // 2)
         S, P, G = p["selected"], p["splits"], p["gathered"]
-        adap += 13 * L + S * (32 + 12 * D) + 4 * D * G + (S - P) * (17 + 4 * D) + P * (54 + 28 * D)
+        adap += 13 * L + S * (32 + 12 * D) + 4 * D * G + (S - P) * (17 + 4 * D) + P * (86 + 28 * D)
     integ = L_final * (16 + 8 * D) + 12 * N_final + 32 * W * H
     return {"init": init, "errors": err, "adaptive": adap, "integrate": integ}
 

@@ -229,7 +229,17 @@ __global__ void __launch_bounds__(256) k_batch_errors(const MdasBatchImage* __re
         const int k = (ch - s_pre[i]) * 256 + threadIdx.x;
         float maxError = dirty ? __uint_as_float(cnt->gerrNext) : 0.0f;
         unsigned recomputed = 0;
-        if (k < items) {
+        if (k < items && dirty && !g.featRaw) {
+            // split children from the splitting pass's lists (no leaf record read)
+            const bool left = k < newL;
+            const int4 sp = left ? g.splitL[k] : g.splitR[k - newL];
+            const int nodeIndex = left ? sp.z : firstRight + (k - newL);
+            const float error = node_error<D>(g, make_int4(sp.x, sp.y, left ? ~D : sp.z, ~D), __int_as_float(sp.w),
+                                              nullptr);
+            g.errors[nodeIndex] = error;
+            recomputed = 1;
+            maxError = fmaxf(maxError, error);
+        } else if (k < items) {
             const int nodeIndex = dirty ? (k < newL ? g.dirty[k] : firstRight + (k - newL)) : k;
             // split children: -1 by construction (not read); learned images also
             // leave the item's raw feature row for the prediction

@@ -228,6 +228,8 @@ void free_grid(mdas_grid* g) {
     cudaFree(g->dg.accepted);
     cudaFree(g->dg.chunkTile);
     cudaFree(g->dg.dirty);
+    cudaFree(g->dg.splitL);
+    cudaFree(g->dg.splitR);
     cudaFree(g->hKeys);
     cudaFree(g->hSorted);
     cudaFree(g->hOrder);
@@ -339,6 +341,8 @@ int mdas_create_ex(mdas_grid** out, int dim, int maxSamples, int candidatesNum, 
               cudaMalloc(&d.accepted, sizeof(uint2) * (size_t)d.maxTiles * MDAS_TILE_LEAVES) == cudaSuccess &&
               cudaMalloc(&d.chunkTile, sizeof(int) * ((size_t)d.maxNodes / 256 + 2)) == cudaSuccess &&
               cudaMalloc(&d.dirty, sizeof(int) * ((size_t)d.maxNodes / 2 + 1)) == cudaSuccess &&
+              cudaMalloc(&d.splitL, sizeof(int4) * ((size_t)d.maxNodes / 2 + 1)) == cudaSuccess &&
+              cudaMalloc(&d.splitR, sizeof(int4) * ((size_t)d.maxNodes / 2 + 1)) == cudaSuccess &&
               cudaMallocHost(&g->hcounts, sizeof(MdasCounts)) == cudaSuccess;
     if (ok) {
         ok = cudaMemset(d.counts, 0, sizeof(MdasCounts)) == cudaSuccess &&

@@ -82,6 +82,11 @@ struct MdasDeviceGrid {
     int* chunkTile;       // [maxNodes/256 + 2] tile of the first entry of each 256-entry chunk of accepted leaves
     int maxTiles;
     int* dirty;           // [maxNodes/2 + 1], slots of the left children of the last pass's splits
+    // [maxNodes/2 + 1] per split of the last pass, for the next errors pass:
+    // left child {sample 0, sample 1, slot, volume bits}, right child
+    // {sample 0, sample 1, sample 2, volume bits} (its slot is L - newL + split rank)
+    int4* splitL;
+    int4* splitR;
     // learned acceptance (nullptr: the reference's plain error ratio): predicted
     // log2(error) / priorityScale per leaf, and the pass's statistics and verdict
     const float* priority;

@@ -309,12 +309,11 @@ __global__ void __launch_bounds__(256) k_initial_sampling(MdasDeviceGrid g, int 
 //           slot range [L - newL, L)); the max over all other leaves was taken
 //           by the adaptive pass that left them unchanged (counts->gerrNext).
 // =====================================================================================
-// raw (may be null): the leaf's row of raw feature inputs (learned mode).
+// The error of a leaf with sample list `node` and box volume `volume`; lumOut
+// (may be null) receives the luminance statistics of its samples.
 template <int D>
-__device__ __forceinline__ float leaf_error(const MdasDeviceGrid& g, int nodeIndex, float* raw = nullptr) {
-    float mn[D], mx[D];
-    const int4 node = nb_load<D, 64>(g.nb + (size_t)nodeIndex * NbLayout<D>::FLOATS, mn, mx);
-    const float volume = box_volume<D>(mn, mx);
+__device__ __forceinline__ float node_error(const MdasDeviceGrid& g, const int4 node, const float volume,
+                                            MdasLumStats* lumOut) {
     float3 avg = make_float3(0.0f, 0.0f, 0.0f);
     float3 loc[4];
     int sampleCount = 0;
@@ -329,7 +328,7 @@ __device__ __forceinline__ float leaf_error(const MdasDeviceGrid& g, int nodeInd
             avg.y += loc[i].y;
             avg.z += loc[i].z;
             sampleCount++;
-            if (raw) mdas_lum_add(lum, mdas_luminance(loc[i].x, loc[i].y, loc[i].z));
+            if (lumOut) mdas_lum_add(lum, mdas_luminance(loc[i].x, loc[i].y, loc[i].z));
         }
     }
     {
@@ -355,6 +354,18 @@ __device__ __forceinline__ float leaf_error(const MdasDeviceGrid& g, int nodeInd
     error /= float(sampleCount);
     error += 1.0e-5f;
     error *= volume;
+    if (lumOut) *lumOut = lum;
+    return error;
+}
+
+// raw (may be null): the leaf's row of raw feature inputs (learned mode).
+template <int D>
+__device__ __forceinline__ float leaf_error(const MdasDeviceGrid& g, int nodeIndex, float* raw = nullptr) {
+    float mn[D], mx[D];
+    const int4 node = nb_load<D, 64>(g.nb + (size_t)nodeIndex * NbLayout<D>::FLOATS, mn, mx);
+    const float volume = box_volume<D>(mn, mx);
+    MdasLumStats lum;
+    const float error = node_error<D>(g, node, volume, raw ? &lum : nullptr);
     if (raw) mdas_raw_store<D>(raw, mn, mx, lum, error);
     return error;
 }
@@ -377,18 +388,34 @@ __global__ void __launch_bounds__(256) k_compute_errors(MdasDeviceGrid g) {
         items = g.counts->L;
     }
     unsigned recomputed = 0;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < items; k += gridDim.x * blockDim.x) {
-        const int nodeIndex = DIRTY ? (k < newL ? g.dirty[k] : firstRight + (k - newL)) : k;
-        // the last pass set the error of both children of each split to -1 (decide
-        // the left one, place the right one), so a dirty item is never read
-        float error = DIRTY ? -1.0f : g.errors[nodeIndex];
-        if (error < 0.0f) {
-            // learned mode: the item's row of raw feature inputs for the prediction
-            error = leaf_error<D>(g, nodeIndex, DIRTY && g.featRaw ? g.featRaw + (size_t)k * MDAS_RAW_FLOATS : nullptr);
+    if (DIRTY && !g.featRaw) {
+        // the split children's sample lists, slots and box volumes, as the
+        // splitting pass left them (no leaf record read)
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < items; k += gridDim.x * blockDim.x) {
+            const bool left = k < newL;
+            const int4 sp = left ? g.splitL[k] : g.splitR[k - newL];
+            const int nodeIndex = left ? sp.z : firstRight + (k - newL);
+            const int4 node = make_int4(sp.x, sp.y, left ? ~D : sp.z, ~D);
+            const float error = node_error<D>(g, node, __int_as_float(sp.w), nullptr);
             g.errors[nodeIndex] = error;
             recomputed++;
+            maxError = fmaxf(maxError, error);
         }
-        maxError = fmaxf(maxError, error);
+    } else {
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < items; k += gridDim.x * blockDim.x) {
+            const int nodeIndex = DIRTY ? (k < newL ? g.dirty[k] : firstRight + (k - newL)) : k;
+            // the last pass set the error of both children of each split to -1 (decide
+            // the left one, place the right one), so a dirty item is never read
+            float error = DIRTY ? -1.0f : g.errors[nodeIndex];
+            if (error < 0.0f) {
+                // learned mode: the item's row of raw feature inputs for the prediction
+                error = leaf_error<D>(g, nodeIndex,
+                                      DIRTY && g.featRaw ? g.featRaw + (size_t)k * MDAS_RAW_FLOATS : nullptr);
+                g.errors[nodeIndex] = error;
+                recomputed++;
+            }
+            maxError = fmaxf(maxError, error);
+        }
     }
     // max of non-negative floats == max of their bit patterns
     unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(maxError));
@@ -839,6 +866,15 @@ __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, i
         // (decide wrote the left child's error -1 and count 2)
         g.errors[nodeOffset] = -1.0f;
         g.leafCounts[nodeOffset] = 3;
+        // the children's sample lists and box volumes for the next errors pass
+        // (the volumes of the boxes written above, by the same arithmetic)
+        {
+            float lmx[D];
+#pragma unroll
+            for (int i = 0; i < D; ++i) lmx[i] = (i == axis) ? splitPosition : mx[i];
+            g.splitL[rank_] = make_int4(l0, l1, nodeIndex, __float_as_int(box_volume<D>(mn, lmx)));
+            g.splitR[rank_] = make_int4(r0, r1, r2, __float_as_int(box_volume<D>(rmn, mx)));
+        }
         // a new slot starts without a seed: the reference's seed buffer is zeroed
         // once at InitialSampling (kdgrid.cu:637) and right-child slots are never
         // written before; writing the 0 here makes that memset unnecessary
