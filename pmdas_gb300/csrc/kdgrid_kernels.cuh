@@ -373,7 +373,7 @@ __device__ __forceinline__ float leaf_error(const MdasDeviceGrid& g, int nodeInd
 // MODE 0: full, 1: dirty, 2: dirty unless no adaptive pass ran since the
 // initial sampling (the device-side budget loop, where passes alternate).
 template <int D, int MODE>
-__global__ void __launch_bounds__(256) k_compute_errors(MdasDeviceGrid g) {
+__global__ void __launch_bounds__(256, 6) k_compute_errors(MdasDeviceGrid g) {
     __shared__ unsigned s_max[8];
     __shared__ unsigned s_cnt[8];
     const bool DIRTY = MODE == 1 || (MODE == 2 && g.counts->passes > 0);
