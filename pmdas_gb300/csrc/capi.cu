@@ -196,16 +196,26 @@ int ensure_scratch(mdas_grid* g, size_t bytes) {
     return MDAS_OK;
 }
 
-int read_counts(mdas_grid* g) {
-    cudaError_t e = cudaMemcpyAsync(g->hcounts, g->dg.counts, sizeof(MdasCounts), cudaMemcpyDeviceToHost, g->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
-    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+// The device counters to the page-locked host copy, queued on the grid's stream.
+cudaError_t counts_copy_async(mdas_grid* g) {
+    return cudaMemcpyAsync(g->hcounts, g->dg.counts, sizeof(MdasCounts), cudaMemcpyDeviceToHost, g->stream);
+}
+
+// The host copy of the counters (the stream has completed the copy) into the grid's state.
+int counts_apply(mdas_grid* g) {
     g->N = g->hcounts->N;
     g->L = g->hcounts->L;
     g->version += 1;
     g->newN = g->hcounts->newN;
     g->newL = g->hcounts->newL;
     return g->hcounts->status ? g->hcounts->status : MDAS_OK;
+}
+
+int read_counts(mdas_grid* g) {
+    cudaError_t e = counts_copy_async(g);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    return counts_apply(g);
 }
 
 void free_grid(mdas_grid* g) {
@@ -948,8 +958,10 @@ int build_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, i
 
 }  // namespace
 
-int mdas_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, int width, int height,
-                      mdas_render_stats* stats) {
+namespace {
+
+// The render graph launched and the counter read queued behind it (no wait).
+int render_graph_launch(mdas_grid* g, mdas_scene* s, int budget, float* pixels, int width, int height) {
     if (!g || !s || !pixels || width <= 0 || height <= 0 || s->desc.dim > g->dg.D) return MDAS_ERR_INVALID;
     int rc = scene_upload(s, g->stream);
     if (rc) return rc;
@@ -962,8 +974,13 @@ int mdas_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, in
     }
     cudaError_t e = cudaGraphLaunch(g->graph.exec, g->stream);
     g->launches += 1;
-    if (e != cudaSuccess) return MDAS_ERR_CUDA;
-    rc = read_counts(g);  // synchronises the stream
+    if (e == cudaSuccess) e = counts_copy_async(g);
+    return e == cudaSuccess ? MDAS_OK : MDAS_ERR_CUDA;
+}
+
+// After the stream completed a launched render: the grid's state and the stats.
+int render_graph_finish(mdas_grid* g, mdas_render_stats* stats) {
+    const int rc = counts_apply(g);
     if (rc) return rc;
     g->initialized = true;
     g->errorsClean = false;
@@ -976,6 +993,16 @@ int mdas_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, in
         for (double& x : stats->stageMs) x = 0.0;
     }
     return MDAS_OK;
+}
+
+}  // namespace
+
+int mdas_render_graph(mdas_grid* g, mdas_scene* s, int budget, float* pixels, int width, int height,
+                      mdas_render_stats* stats) {
+    int rc = render_graph_launch(g, s, budget, pixels, width, height);
+    if (rc) return rc;
+    if (cudaStreamSynchronize(g->stream) != cudaSuccess) return MDAS_ERR_CUDA;
+    return render_graph_finish(g, stats);
 }
 
 // ---- batched rendering ------------------------------------------------------------------
@@ -1291,11 +1318,13 @@ int mdas_render_host(mdas_grid* g, mdas_scene* s, const float* hostPrims, int bu
         if (e == cudaSuccess) e = mdas_launch_build_cull(s->desc, s->d_prims, s->d_cull, g->stream);  // new primitives
         if (e != cudaSuccess) return MDAS_ERR_CUDA;
     }
-    rc = mdas_render_graph(g, s, budget, g->scratch, width, height, stats);
+    // the image copy queued behind the render and its counter read: one wait
+    rc = render_graph_launch(g, s, budget, g->scratch, width, height);
     if (rc) return rc;
     cudaError_t e = cudaMemcpyAsync(hostPixels, g->scratch, bytes, cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
-    return status_of(e);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    return render_graph_finish(g, stats);
 }
 
 // ---- Morton keys, radix sort, leaf order, hierarchy, point location
