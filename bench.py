@@ -10,12 +10,21 @@ for the new samples, then Integrate.
 
 metric: final sample count / (initial sampling + errors + adaptive sampling +
 integrate time): the reference's `total_mdas_time` (SDK/data/Scripts/
-parse_logs.py:148-154), integrand excluded.  Stage times are CUDA events on the
-grid's stream.
+parse_logs.py:148-154), integrand excluded.  `value` counts the stages'
+kernels only (CUDA events around the launches); `value_api` counts each
+adaptive pass until the host holds its new counts, which is how the
+reference's own log times it (its stop event follows its two blocking counter
+reads, SDK/lib/mdas/kdgrid.cu:753-768).  `reference_cuda` gives both numbers
+for the reference's own kernels on the same GPU.
 
 e2e: the same metric through the host-buffer C-ABI call (mdas_render_host:
 scene primitives uploaded from host memory, float4 image copied back), timed by
 the host clock around each call, integrand included.
+
+config.all_configs: every benchmark configuration of the build next to the
+headline: the 3-D 256x256 motion blur (with extraImgBits 8 and 6), the 5-D
+1920x1080 and 4-D direct-lighting 3840x2160 workloads (plain throughput and
+learned-vs-plain time to rel-MSE 1e-3), and the 64-image batch.
 
 --impl reference: the CPU restatement of the reference's MDAS step (the
 reference has no CPU implementation of its own) on all host cores.
@@ -54,6 +63,10 @@ def parse_args():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain comparison")
     ap.add_argument("--learned-host", action="store_true",
                     help="render the learned-vs-plain ladders through the host loop (mdas_render) instead of graphs")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other benchmark configurations")
+    ap.add_argument("--ncu-traffic", default=None, metavar="CSV",
+                    help="print the per-stage DRAM traffic of an ncu launch list (gpu__time_duration.sum, "
+                         "dram__bytes_read.sum, dram__bytes_write.sum; --csv) of this bench, and exit")
     return ap.parse_args()
 
 
@@ -108,11 +121,43 @@ class ClockSampler:
 
 
 # ---- traffic accounting -------------------------------------------------------------
-# DRAM traffic of the dominant stage per pass, from the committed ncu capture of
-# every launch (dram__bytes_read.sum + dram__bytes_write.sum, mean per pass of
-# decide + scan + place): profiles/kernels_dram_dof1024.md
-MEASURED_TRAFFIC = {"dof1024": (144.9e6, "profiles/kernels_dram_dof1024.md (ncu: decide 27.7 + scan 0.0 + place "
-                                         "117.2 MB, mean per pass)")}
+STAGE_OF_KERNEL = (("k_initial_sampling", "init"), ("k_compute_errors", "errors"), ("k_adaptive_decide", "adaptive"),
+                   ("k_adaptive_scan", "adaptive"), ("k_adaptive_place", "adaptive"), ("k_integrate", "integrate"))
+
+
+def ncu_stage_traffic(path: str) -> dict:
+    """DRAM bytes (read + write) and device time per stage from an ncu launch list
+    (--csv --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum)
+    of the sampler kernels: totals per stage and the launch counts."""
+    import csv
+    launches = {}
+    with open(path, newline="") as f:
+        rows = [r for r in csv.reader(f) if r]
+    head = next(i for i, r in enumerate(rows) if "Metric Name" in r)
+    cols = rows[head]
+    ki, ni, vi, ui = cols.index("ID"), cols.index("Kernel Name"), cols.index("Metric Value"), cols.index("Metric Unit")
+    mi = cols.index("Metric Name")
+    scale = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "nsecond": 1e-3, "usecond": 1.0,
+             "msecond": 1e3, "second": 1e6}
+    for r in rows[head + 1:]:
+        if len(r) <= max(ki, ni, vi, mi):
+            continue
+        stage = next((st for k, st in STAGE_OF_KERNEL if k in r[ni]), None)
+        if stage is None:
+            continue
+        d = launches.setdefault(r[ki], {"stage": stage, "kernel": r[ni], "bytes": 0.0, "us": 0.0})
+        v = float(r[vi].replace(",", "")) * scale.get(r[ui], 1.0)
+        if r[mi].startswith("dram__bytes"):
+            d["bytes"] += v
+        elif r[mi] == "gpu__time_duration.sum":
+            d["us"] += v
+    out = {}
+    for d in launches.values():
+        o = out.setdefault(d["stage"], {"launches": 0, "dram_bytes": 0.0, "us": 0.0})
+        o["launches"] += 1
+        o["dram_bytes"] += d["bytes"]
+        o["us"] += d["us"]
+    return out
 
 
 def workload_label(wl) -> str:
@@ -225,12 +270,12 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     ev0.record()
-    stage_ms = [0.0] * 5
+    stage_ms = [0.0] * 6
     results = []
     for _ in range(args.steps):
         flush.zero_()  # L2 flushed between steps (outside the stage events)
         n, l, L0, t, passes = one_render(record=not results)
-        for i in range(5):
+        for i in range(6):
             stage_ms[i] += t[i]
         results.append((n, l, L0, passes))
     ev1.record()
@@ -240,10 +285,15 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     launches = grid.launch_count() - launches0
 
     mdas_ms = sum(stage_ms[:4])
+    # the adaptive passes until the host holds their counts (the reference log's window)
+    api_ms = stage_ms[0] + stage_ms[1] + stage_ms[5] + stage_ms[3]
     n_final, l_final, L0, passes = results[0]
     total_samples = sum(r[0] for r in results)
+    samples_1 = total_samples
     mdas_ms, wall_ms, total_samples = reduce_across_ranks(mdas_ms, wall_ms, total_samples, world, "cuda")
+    api_ms, _, _ = reduce_across_ranks(api_ms, api_ms, samples_1, world, "cuda")
     value = total_samples / (mdas_ms / 1e3) / 1e6
+    value_api = total_samples / (api_ms / 1e3) / 1e6
 
     # roofline of the dominant kernel
     by = stage_bytes(D, W, H, L0, passes, n_final, l_final)
@@ -262,6 +312,12 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
     all_bytes = sum(by.values())
     overall_gbs = all_bytes * args.steps / (mdas_ms / 1e3) / 1e9
+    # every stage: algorithmic bytes per render / its kernels' device time per render
+    stages = {}
+    for i, k in enumerate(names):
+        ms_i = stage_ms[i] / args.steps
+        gbs = by[k] / (ms_i / 1e3) / 1e9 if ms_i > 0 else 0.0
+        stages[k] = {"ms": round(ms_i, 4), "bytes": int(by[k]), "gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
 
     # the same render as one CUDA graph (device-side loop): device time per render,
     # integrand included
@@ -324,38 +380,34 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
                            "reconstruction, one counter read, image copy (page-locked host buffers)"}
 
     order = None if args.no_order else order_block(grid, wl, peak)
-    learned = None
-    if not args.no_learned and world == 1:
-        learned = {"config2_single": learned_block(peaks, "mbdof1080", host=args.learned_host),
-                   "config4_batched": learned_block(peaks, "dl4k", batched=not args.learned_host,
-                                                    ladder=(1, 2, 4, 8, 16, 32, 64), target=1e-4,
-                                                    host=args.learned_host)}
-
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(mdas_ms / args.steps, 4), "higher_is_better": True,
+        "value_api": round(value_api, 3),
+        "timing": "value: the stages' kernels (CUDA events around the launches); value_api: each adaptive pass "
+                  "until the host holds its counts, the window of the reference's own log",
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded analytic integrand)",
         "config": {"workload": workload_label(wl),
                    "final_samples": n_final, "final_leaves": l_final, "initial_leaves": L0,
                    "passes": len(passes), "maxSamples": wl.maxSamples, "arith": "reference (fast-math)",
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
         "stage_ms_per_step": {k: round(stage_ms[i] / args.steps, 4)
-                              for i, k in enumerate(["init", "errors", "adaptive", "integrate", "integrand"])},
+                              for i, k in enumerate(["init", "errors", "adaptive", "integrate", "integrand",
+                                                     "adaptive_api"])},
         "wall_ms_per_step": round(wall_ms / args.steps, 3),
         "graph_render_ms": round(graph_ms, 3) if graph_ms else None,
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "traffic": MEASURED_TRAFFIC[wl.name][0] if dom == 2 and wl.name in MEASURED_TRAFFIC else None,
-                     "traffic_source": MEASURED_TRAFFIC[wl.name][1] if dom == 2 and wl.name in MEASURED_TRAFFIC
-                     else None,
+                     "traffic": None,
+                     "traffic_note": "not measured in this run: DRAM bytes per launch come from an ncu launch "
+                                     "list of this bench (bench.py --ncu-traffic CSV prints them per stage)",
                      "algorithmic_bytes_per_launch": int(per_launch_bytes), "launches_per_step": launches_of,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s",
-                     "all_stages_gbs": round(overall_gbs, 1)},
+                     "all_stages_gbs": round(overall_gbs, 1), "stages": stages},
         "stage_bytes_per_step": by,
         "e2e": e2e,
         "quality": quality,
         "leaf_order": order,
-        "learned": learned,
         "gpu_launches": int(launches),
         "clocks": clk,
     }
@@ -438,66 +490,114 @@ def time_to_target(points, target):
 LADDER_REPEATS = 3  # timed renders per ladder point (after one warm-up render)
 
 
-def learned_block(peaks: dict, name: str = "mbdof1080", batched: bool = False,
-                  ladder=(16, 32, 64, 128, 256, 512), target: float = 1e-3, host: bool = False) -> dict:
-    """Time to rel-MSE `target`, learned vs plain, on one workload (its scene seed
-    is the evaluation scene; the weights were trained on seeds 1-32): both render
-    a ladder of budgets until the image's rel-MSE against the FP64 4096-spp
-    reference reaches the target.  Plain renders use the device-side loop of one
-    image; learned renders use it too, or (batched) the batch API's graph."""
+def target_summary(plain: dict, learned: dict, target: float) -> dict:
+    """Learned-vs-plain time to `target` as measured: a ratio where both arms reached
+    the target on their ladders; where plain did not, a bound (plain took longer than
+    its last ladder point); extrapolations are labelled as such."""
+    out = {"target_rel_mse": target}
+    tl, hl = learned["ms_to_target"], learned["to_target"]
+    tp, hp = plain["ms_to_target"], plain["to_target"]
+    measured_l = tl if hl in ("measured", "interpolated") else None
+    measured_p = tp if hp in ("measured", "interpolated") else None
+    if measured_l is not None:
+        out["learned_ms"] = measured_l
+    if measured_p is not None:
+        out["plain_ms"] = measured_p
+    last_plain = plain["ladder"][-1] if plain["ladder"] else None
+    if measured_l is not None and measured_p is not None:
+        out["ratio"] = round(measured_l / measured_p, 4)
+        out["how"] = "both arms reached the target on their ladders (log-log interpolation between points)"
+    elif measured_l is not None and last_plain is not None and last_plain["rel_mse"] > target:
+        out["plain_ms_lower_bound"] = last_plain["ms"]
+        out["ratio_upper_bound"] = round(measured_l / last_plain["ms"], 4)
+        out["how"] = (f"plain did not reach the target: rel-MSE {last_plain['rel_mse']:.3g} at its last ladder "
+                      f"point ({last_plain['spp']} spp, {last_plain['ms']} ms), so the ratio is a measured bound")
+        if tp and hp == "extrapolated":
+            out["plain_ms_extrapolated"] = tp
+            out["ratio_extrapolated"] = round(measured_l / tp, 4)
+    else:
+        out["how"] = "learned did not reach the target on its ladder"
+    return out
+
+
+def rel_mse_of(ref, pixels) -> float:
+    """rel-MSE of an image against its FP64 reference (parse_logs.py:48-50)."""
+    import torch
+    img = pixels[..., :3].double()
+    return float(torch.nan_to_num((ref - img) ** 2 / (ref ** 2 + 1e-2), nan=0.0).mean().item())
+
+
+def _weights(name: str):
     import numpy as np
+    wpath = os.path.join(ROOT, "pmdas_gb300", "weights", f"priority_{name}.f32")
+    if not os.path.exists(wpath):
+        return None, wpath
+    return np.fromfile(wpath, dtype="<f4"), wpath
+
+
+def _grid_for_budget(P, wl, budget: int):
+    cap = min(max(budget * 3 // 2, 4 * wl.initial_leaves + 1), (1 << 30) - 1)
+    return P.KDGrid(wl.dim, cap, wl.candidatesNum, wl.bitsPerDim, wl.extraImgBits, wl.alpha, wl.scaleX, wl.scaleY)
+
+
+def _timed_median(render, repeats: int = LADDER_REPEATS):
+    import torch
+    render()  # build + warm
+    times = []
+    st = None
+    for _ in range(repeats):  # median of a few renders: one render can catch a stall
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        st = render()
+        b.record()
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    return statistics.median(times), st
+
+
+def learned_block(peaks: dict, name: str = "mbdof1080", ladder=(16, 32, 64, 128, 256, 512), target: float = 1e-3,
+                  host: bool = False, ref=None, scene=None) -> dict:
+    """Time to rel-MSE `target`, learned vs plain, on one image of one workload (its
+    scene seed is the evaluation scene; the weights were trained on seeds 1-32):
+    both render a ladder of budgets until the image's rel-MSE against the FP64
+    4096-spp reference reaches the target; each point is the median of a few
+    renders through the device-side loop (or the host loop)."""
     import torch
 
     import pmdas_gb300 as P
     from pmdas_gb300.workloads import WORKLOADS
 
     wl = WORKLOADS[name]
-    wpath = os.path.join(ROOT, "pmdas_gb300", "weights", f"priority_{name}.f32")
-    if not os.path.exists(wpath):
+    params, wpath = _weights(name)
+    if params is None:
         return {"unavailable": f"no trained weights for {name} (python -m pmdas_gb300.train_priority)"}
-    params = np.fromfile(wpath, dtype="<f4")
     W, H = wl.width, wl.height
-    scene = P.Scene(wl.scene_kind, wl.scene_seed, wl.scene_count, wl.scaleX, wl.scaleY, W, H)
-    ref = scene.reference_image(W, H, spp=4096)
+    own_scene = scene is None
+    if own_scene:
+        scene = P.Scene(wl.scene_kind, wl.scene_seed, wl.scene_count, wl.scaleX, wl.scaleY, W, H)
+    if ref is None:
+        ref = scene.reference_image(W, H, spp=4096)
     out = {"workload": f"{wl.name}: {wl.dim}-D {W}x{H}, scene seed {wl.scene_seed}, alpha {wl.alpha}",
            "weights": os.path.relpath(wpath, ROOT), "target_rel_mse": target,
            "timing": ("host loop (mdas_render)" if host else "whole render on the device (one CUDA graph)") +
-                     ", integrand included, CUDA events",
-           "learned_path": "batch API (one image per batch)" if batched else
-                           ("host loop of one grid" if host else "device-side loop of one grid")}
+                     ", integrand included, CUDA events, median of 3",
+           "learned_path": "host loop of one grid" if host else "device-side loop of one grid"}
     pixels = torch.zeros(H, W, 4, device="cuda")
     for mode in ("plain", "learned"):
         pts, rows = [], []
         for spp in ladder:
             budget = int(spp * W * H)
-            ms_cap = min(max(budget * 3 // 2, 4 * wl.initial_leaves + 1), (1 << 30) - 1)
-            g = P.KDGrid(wl.dim, ms_cap, wl.candidatesNum, wl.bitsPerDim, wl.extraImgBits, wl.alpha, wl.scaleX,
-                         wl.scaleY)
-            batch = None
+            g = _grid_for_budget(P, wl, budget)
             if mode == "learned":
                 g.LearnedEnable(params=params)
-                if batched:
-                    batch = P.Batch([g], [scene], [budget], [pixels], [W], [H])
 
             def render():
-                if batch is not None:
-                    return batch.render()[0]
                 if host:
                     return P.render(g, scene, budget, pixels, W, H)
                 return P.render_graph(g, scene, budget, pixels, W, H)
 
-            render()  # build + warm
-            times = []
-            for _ in range(LADDER_REPEATS):  # median of a few renders: one render can catch a stall
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record()
-                st = render()
-                b.record()
-                torch.cuda.synchronize()
-                times.append(a.elapsed_time(b))
-            ms = statistics.median(times)
-            img = pixels[..., :3].double()
-            rel = float(torch.nan_to_num((ref - img) ** 2 / (ref ** 2 + 1e-2), nan=0.0).mean().item())
+            ms, st = _timed_median(render)
+            rel = rel_mse_of(ref, pixels)
             row = {"spp": spp, "samples": st.numberOfSamples, "passes": st.passes, "ms": round(ms, 3),
                    "rel_mse": rel}
             if mode == "learned":
@@ -505,16 +605,260 @@ def learned_block(peaks: dict, name: str = "mbdof1080", batched: bool = False,
                 row["passes_judged_plain"] = ls["plain"] // (1 + LADDER_REPEATS)  # every render judged alike
             rows.append(row)
             pts.append((ms, rel))
-            if batch is not None:
-                batch.close()
             g.close()
             if rel <= target:
                 break
         t, how = time_to_target(pts, target)
         out[mode] = {"ladder": rows, "ms_to_target": round(t, 3) if t else None, "to_target": how}
-    tp, tl = out["plain"]["ms_to_target"], out["learned"]["ms_to_target"]
-    out["learned_over_plain_time"] = round(tl / tp, 4) if tp and tl else None
-    scene.close()
+    out["summary"] = target_summary(out["plain"], out["learned"], target)
+    if own_scene:
+        scene.close()
+    return out
+
+
+def learned_batch_block(peaks: dict, name: str = "dl4k", seeds=(100, 101, 102, 103),
+                        ladder=(0.5, 0.75, 1, 2, 4), target: float = 1e-3) -> dict:
+    """Learned + batched against plain on a real multi-image batch: the images of
+    `name` with the given (held-out) scene seeds in one batched learned render (one
+    CUDA graph for all of them) against the plain sampler rendering each image
+    alone (device-side loop), one after another.  rel-MSE is the mean over the
+    images, each against its own FP64 4096-spp reference; times cover all images."""
+    import torch
+
+    import pmdas_gb300 as P
+    from pmdas_gb300.workloads import WORKLOADS
+
+    wl = WORKLOADS[name]
+    params, wpath = _weights(name)
+    if params is None:
+        return {"unavailable": f"no trained weights for {name}"}
+    W, H = wl.width, wl.height
+    scenes = [P.Scene(wl.scene_kind, sd, wl.scene_count, wl.scaleX, wl.scaleY, W, H) for sd in seeds]
+    refs = [sc.reference_image(W, H, spp=4096) for sc in scenes]
+    pix = [torch.zeros(H, W, 4, device="cuda") for _ in seeds]
+    out = {"workload": f"{wl.name}: {wl.dim}-D {W}x{H}, {len(seeds)} images (scene seeds "
+                       f"{seeds[0]}-{seeds[-1]}, none used in training), alpha {wl.alpha}",
+           "weights": os.path.relpath(wpath, ROOT), "target_rel_mse": target,
+           "timing": "all images; learned: one batched render (one CUDA graph); plain: each image alone through "
+                     "the device-side loop, one after another; integrand included, CUDA events, median of 3"}
+    for mode in ("plain", "learned", "plain_batched"):
+        pts, rows = [], []
+        for spp in ladder:
+            budget = int(spp * W * H)
+            grids = [_grid_for_budget(P, wl, budget) for _ in seeds]
+            batch = None
+            if mode == "learned":
+                for g in grids:
+                    g.LearnedEnable(params=params)
+            if mode != "plain":
+                batch = P.Batch(grids, scenes, [budget] * len(seeds), pix, [W] * len(seeds), [H] * len(seeds))
+
+            def render():
+                if batch is not None:
+                    return batch.render()
+                return [P.render_graph(g, sc, budget, p, W, H) for g, sc, p in zip(grids, scenes, pix)]
+
+            ms, sts = _timed_median(render)
+            rel = statistics.mean(rel_mse_of(r, p) for r, p in zip(refs, pix))
+            row = {"spp": spp, "samples": sum(st.numberOfSamples for st in sts),
+                   "passes": max(st.passes for st in sts), "ms": round(ms, 3), "rel_mse": rel}
+            if mode == "learned":
+                row["passes_judged_plain"] = sum(g.LearnedStats()["plain"] for g in grids) // (1 + LADDER_REPEATS)
+            rows.append(row)
+            pts.append((ms, rel))
+            if batch is not None:
+                batch.close()
+            for g in grids:
+                g.close()
+            if rel <= target:
+                break
+        t, how = time_to_target(pts, target)
+        out[mode] = {"ladder": rows, "ms_to_target": round(t, 3) if t else None, "to_target": how}
+    out["summary"] = target_summary(out["plain"], out["learned"], target)
+    for sc in scenes:
+        sc.close()
+    return out
+
+
+def measure_plain(wl, steps: int = 3, warmup: int = 1, ref=None, scene=None) -> dict:
+    """One workload's plain throughput (the headline's metric and windows) over a few
+    host-loop renders with the L2 flushed between them, and its rel-MSE."""
+    import torch
+
+    import pmdas_gb300 as P
+
+    W, H = wl.width, wl.height
+    grid = P.KDGrid(wl.dim, wl.maxSamples, wl.candidatesNum, wl.bitsPerDim, wl.extraImgBits, wl.alpha, wl.scaleX,
+                    wl.scaleY, arith=P.ARITH_REFERENCE)
+    own_scene = scene is None
+    if own_scene:
+        scene = P.Scene(wl.scene_kind, wl.scene_seed, wl.scene_count, wl.scaleX, wl.scaleY, W, H)
+    pixels = torch.zeros(H, W, 4, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    grid.set_timing(True)
+
+    def one():
+        grid.stage_times(reset=True)
+        grid.InitialSampling()
+        scene.evaluate(grid, 0, grid.GetNumberOfSamples())
+        passes = 0
+        while True:
+            n, _, l, _ = grid._counts()
+            if n >= wl.budget or n + l > wl.maxSamples:
+                break
+            grid.SamplingPass()
+            passes += 1
+            n2, nn, _, _ = grid._counts()
+            scene.evaluate(grid, n2 - nn, nn)
+        grid.Integrate(pixels, W, H)
+        return grid.stage_times(reset=True), passes
+
+    for _ in range(warmup):
+        one()
+    ts = []
+    passes = 0
+    for _ in range(steps):
+        flush.zero_()
+        t, passes = one()
+        ts.append(t)
+    n = grid.GetNumberOfSamples()
+    ms = statistics.median(sum(t[:4]) for t in ts)
+    ms_api = statistics.median(t[0] + t[1] + t[5] + t[3] for t in ts)
+    out = {"value": round(n / (ms / 1e3) / 1e6, 3), "value_api": round(n / (ms_api / 1e3) / 1e6, 3),
+           "ms": round(ms, 4), "samples": n, "leaves": grid.GetNumberOfNodes(), "passes": passes,
+           "stage_ms": {k: round(ts[-1][i], 4) for i, k in enumerate(("init", "errors", "adaptive", "integrate"))}}
+    if ref is None:
+        ref = scene.reference_image(W, H, spp=4096)
+    out["rel_mse"] = rel_mse_of(ref, pixels)
+    grid.close()
+    if own_scene:
+        scene.close()
+    return out
+
+
+def render_tallies(grid, scene, wl, pixels) -> dict:
+    """Algorithmic bytes of one host-loop render of `wl` (timing off), from the
+    per-pass tallies the kernels report."""
+    grid.InitialSampling()
+    L0 = grid.GetNumberOfNodes()
+    scene.evaluate(grid, 0, grid.GetNumberOfSamples())
+    passes = []
+    while True:
+        n, _, l, _ = grid._counts()
+        if n >= wl.budget or n + l > wl.maxSamples:
+            break
+        grid.SamplingPass()
+        ps = grid.pass_stats()
+        ps["L"] = l
+        passes.append(ps)
+        n2, nn, _, _ = grid._counts()
+        scene.evaluate(grid, n2 - nn, nn)
+    grid.Integrate(pixels, wl.width, wl.height)
+    n, _, l, _ = grid._counts()
+    return stage_bytes(wl.dim, wl.width, wl.height, L0, passes, n, l)
+
+
+def batch_block(steps: int, warmup: int, peak: float, first_seed: int = 200, n_images: int = 64) -> dict:
+    """Config 3: 64 images of uneven resolution, spp and dimension (seeds 200-263)
+    in one batched render (one CUDA graph, device-side loop), autotuned; against
+    the same images rendered one after another as single-image graph renders."""
+    import torch
+
+    import pmdas_gb300 as P
+    from pmdas_gb300.workloads import batch_workloads
+
+    wls = batch_workloads(first_seed, n_images)
+    grids, scenes, pix = [], [], []
+    for wl in wls:
+        grids.append(P.KDGrid(wl.dim, wl.maxSamples, wl.candidatesNum, wl.bitsPerDim, wl.extraImgBits, wl.alpha,
+                              wl.scaleX, wl.scaleY, arith=P.ARITH_REFERENCE))
+        scenes.append(P.Scene(wl.scene_kind, wl.scene_seed, wl.scene_count, wl.scaleX, wl.scaleY, wl.width,
+                              wl.height))
+        pix.append(torch.zeros(wl.height, wl.width, 4, device="cuda"))
+    # algorithmic bytes of every image (a batched render equals the single renders bit for bit)
+    nbytes = 0
+    for g, sc, p, wl in zip(grids, scenes, pix, wls):
+        nbytes += sum(render_tallies(g, sc, wl, p).values())
+    batch = P.Batch(grids, scenes, [w.budget for w in wls], pix, [w.width for w in wls], [w.height for w in wls])
+    best, tuned_ms = batch.autotune(repeats=1)
+    for _ in range(warmup):
+        stats = batch.render()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        stats = batch.render()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    samples = sum(st.numberOfSamples for st in stats)
+    t_single = 0.0
+    for g, sc, p, wl in zip(grids, scenes, pix, wls):
+        P.render_graph(g, sc, wl.budget, p, wl.width, wl.height)  # build + warm
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record()
+        P.render_graph(g, sc, wl.budget, p, wl.width, wl.height)
+        a1.record()
+        torch.cuda.synchronize()
+        t_single += a0.elapsed_time(a1)
+    gbs = nbytes / (ms / 1e3) / 1e9
+    batch.close()
+    for g in grids:
+        g.close()
+    for sc in scenes:
+        sc.close()
+    return {"workload": "batch64: 64 images, resolution in {256^2, 512^2, 1280x720, 1920x1080}, spp in {4, 8, 16, "
+                        "32}, 3-D motion blur or 4-D depth of field, scene seeds 200-263",
+            "value": round(samples / (ms / 1e3) / 1e6, 3), "unit": UNIT, "ms": round(ms, 3),
+            "per_image_ms": round(ms / len(wls), 4), "samples": samples,
+            "sequential_single_image_ms": round(t_single, 3), "speedup_vs_sequential": round(t_single / ms, 3),
+            "autotuned_ctas_per_sm": best, "autotune_best_ms": round(tuned_ms, 3),
+            "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(gbs / peak, 4), "algorithmic_bytes": int(nbytes),
+                         "note": "all stages of all images over the whole batched render (integrand included)"},
+            "timing": "whole batched render incl. integrand (one CUDA graph), CUDA events"}
+
+
+def all_configs(args, peak: float, peaks: dict, headline: dict) -> dict:
+    """Every benchmark configuration next to the headline (rank 0, one GPU)."""
+    import pmdas_gb300 as P
+    from pmdas_gb300.workloads import WORKLOADS
+
+    out = {}
+    for name in ("mb256", "mb256_eib6"):
+        wl = WORKLOADS[name]
+        r = measure_plain(wl, steps=5, warmup=2)
+        r["workload"] = workload_label(wl)
+        if r["passes"] == 0:
+            r["note"] = "the initial grid (32 spp) exceeds the 8-spp budget: the reference's loop runs no pass"
+        out[f"c0_{name}"] = r
+    out["c1_dof1024"] = {"value": headline["value"], "value_api": headline["value_api"],
+                         "rel_mse": (headline.get("quality") or {}).get("rel_mse"), "note": "the headline line"}
+    for key, name in (("c2_mbdof1080", "mbdof1080"), ("c4_dl4k", "dl4k")):
+        wl = WORKLOADS[name]
+        scene = P.Scene(wl.scene_kind, wl.scene_seed, wl.scene_count, wl.scaleX, wl.scaleY, wl.width, wl.height)
+        ref = scene.reference_image(wl.width, wl.height, spp=4096)
+        r = measure_plain(wl, steps=2, warmup=1, ref=ref, scene=scene)
+        r["workload"] = workload_label(wl)
+        out[key] = {"plain": r}
+        if not args.no_learned:
+            if name == "mbdof1080":
+                lb = learned_block(peaks, name, host=args.learned_host, ref=ref, scene=scene)
+                out[key]["learned_vs_plain"] = lb.get("summary", lb)
+                out[key]["learned_ladders"] = {m: lb[m]["ladder"] for m in ("plain", "learned") if m in lb}
+            else:
+                lb = learned_batch_block(peaks, name)
+                out[key]["learned_batched_vs_plain"] = lb.get("summary", lb)
+                out[key]["learned_batched_ladders"] = {m: lb[m]["ladder"] for m in ("plain", "learned",
+                                                                                    "plain_batched") if m in lb}
+                # the rel-MSE 1e-4 target, chosen by this build (BASELINE states 1e-3), one image
+                lb4 = learned_block(peaks, name, ladder=(1, 2, 4, 8, 16, 32, 64), target=1e-4,
+                                    host=args.learned_host, ref=ref, scene=scene)
+                s4 = lb4.get("summary", lb4)
+                s4["note"] = "target chosen by this build, not the benchmark's; one image, device-side loop"
+                out[key]["learned_vs_plain_1e-4_one_image"] = s4
+        scene.close()
+    out["c3_batch64"] = batch_block(max(2, args.steps // 5), 2, peak)
     return out
 
 
@@ -599,50 +943,87 @@ def cpu_baseline(wl, threads: int, budget_s: float = 30.0) -> dict:
                       f"{t[4] / 1e3:.2f} s excluded", "wall_s": round(wall, 2)}
 
 
+def parse_reference_log(path: str) -> dict:
+    """Per-stage ms summed from the reference's own .exr.log keys (kdgrid.cu:664-665,
+    711, 767-768, 815-816), as its scripts read them (parse_logs.py:117-154)."""
+    keys = {"INITIAL SAMPLING TIME": "init", "COMPUTE ERRORS TIME": "errors", "ADAPTIVE SAMPLING TIME": "adaptive",
+            "INTEGRATE TIME": "integrate"}
+    out = {v: 0.0 for v in keys.values()}
+    with open(path) as f:
+        lines = [ln.strip() for ln in f]
+    for k, v in zip(lines, lines[1:]):
+        if k in keys:
+            out[keys[k]] += float(v)
+    return out
+
+
 def reference_cuda(wl, steps: int = 2) -> dict | None:
     """The reference's own CUDA kernels (oracle/_ref, patched copy of SDK/lib/mdas/kdgrid.cu)
-    on the same GPU, same workload, same integrand; per-stage CUDA events."""
-    import torch
+    on the same GPU, same workload, same integrand.  Two timings:
+      api    — the reference's own log (its KDGrid methods record events around
+               each stage; the adaptive window ends after its two blocking counter
+               reads), summed as parse_logs.py does: the window of `value_api`;
+      device — the same log for initial sampling, errors and integrate (kernel-only
+               windows already) with each adaptive kernel timed alone (its counter
+               reads after the window): the window of `value`."""
+    import ctypes as C
 
     import pmdas_gb300 as P
     from oracle import pyoracle as O
     if not O.RefGrid.available():
         return None
+    import torch
     lib = O.RefGrid.lib()
     ref = O.RefGrid(wl.dim, wl.maxSamples, wl.candidatesNum, wl.bitsPerDim, wl.extraImgBits, wl.alpha, wl.scaleX,
                     wl.scaleY)
     scene = P.Scene(wl.scene_kind, wl.scene_seed, wl.scene_count, wl.scaleX, wl.scaleY, wl.width, wl.height)
     pixels = torch.zeros(wl.height, wl.width, 4, device="cuda")
     coords, values = ref.ptr(0), ref.ptr(1)
-    s0 = torch.cuda.default_stream()
+    fd, log = tempfile.mkstemp(suffix=".exr.log")
+    os.close(fd)
 
-    def timed(fn):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(s0)
-        rc = fn()
-        b.record(s0)
-        assert rc == 0, rc
-        return a, b
-
-    totals = []
-    n = 0
-    for it in range(steps + 1):
-        evs = []
-        evs.append(timed(lambda: lib.ref_initial_sampling_async(ref.h)))
+    def one(kernel_only: bool):
+        assert lib.ref_set_log(ref.h, log.encode()) == 0
+        assert lib.ref_initial_sampling_async(ref.h) == 0
         n, _, l, _ = ref.counts()
         scene.evaluate_buffers(coords, values, wl.dim, 0, n)
+        adaptive_ms = 0.0
         while n < wl.budget and n + l <= wl.maxSamples:
-            evs.append(timed(lambda: lib.ref_compute_errors_async(ref.h)))
-            evs.append(timed(lambda: lib.ref_adaptive_sampling_async(ref.h)))
+            assert lib.ref_compute_errors_async(ref.h) == 0
+            if kernel_only:
+                ms = C.c_float()
+                assert lib.ref_adaptive_sampling_kernel_timed(ref.h, C.byref(ms)) == 0
+                adaptive_ms += ms.value
+            else:
+                assert lib.ref_adaptive_sampling_async(ref.h) == 0
             n, nn, l, _ = ref.counts()
             scene.evaluate_buffers(coords, values, wl.dim, n - nn, nn)
-        evs.append(timed(lambda: lib.ref_integrate_async(ref.h, pixels.data_ptr(), wl.width, wl.height)))
+        assert lib.ref_integrate_async(ref.h, pixels.data_ptr(), wl.width, wl.height) == 0
         torch.cuda.synchronize()
+        assert lib.ref_set_log(ref.h, None) == 0
+        t = parse_reference_log(log)
+        if kernel_only:
+            t["adaptive"] = adaptive_ms
+        return n, t
+
+    api, dev = [], []
+    n = 0
+    for it in range(steps + 1):
+        n, ta = one(False)
+        _, td = one(True)
         if it > 0:
-            totals.append(sum(a.elapsed_time(b) for a, b in evs))
+            api.append(ta)
+            dev.append(td)
+    os.unlink(log)
     ref.close()
-    ms = statistics.median(totals)
-    return {"value": round(n / (ms / 1e3) / 1e6, 3), "unit": UNIT, "ms_per_step": round(ms, 3),
+    ms_api = statistics.median(sum(t.values()) for t in api)
+    ms_dev = statistics.median(sum(t.values()) for t in dev)
+    return {"value": round(n / (ms_dev / 1e3) / 1e6, 3), "value_api": round(n / (ms_api / 1e3) / 1e6, 3),
+            "unit": UNIT, "ms_per_step": round(ms_dev, 3), "ms_per_step_api": round(ms_api, 3),
+            "stage_ms": {k: round(v, 4) for k, v in dev[-1].items()},
+            "stage_ms_api": {k: round(v, 4) for k, v in api[-1].items()},
+            "timing": "the reference's own log (events around each stage); value: the adaptive kernel alone, "
+                      "value_api: its window incl. the two counter reads",
             "source": "SDK/lib/mdas/kdgrid.cu (four CUDA-13 edits), --use_fast_math, sm_103a, managed memory"}
 
 
@@ -672,6 +1053,9 @@ def main():
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.ncu_traffic:
+        print(json.dumps(ncu_stage_traffic(args.ncu_traffic), indent=1), flush=True)
+        return
     if args.impl == "reference":
         if rank != 0:
             return
@@ -701,6 +1085,14 @@ def main():
                 line["reference_cuda"] = reference_cuda(wl)
             except Exception as e:
                 line["reference_cuda"] = {"error": str(e)}
+        if not args.no_configs and world == 1:
+            peaks = {}
+            try:
+                with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                    peaks = json.load(f)
+            except Exception:
+                pass
+            line["config"]["all_configs"] = all_configs(args, line["roofline"]["peak"], peaks, line)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.barrier()

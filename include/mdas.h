@@ -131,29 +131,35 @@ int mdas_load_state(mdas_grid* g, int numberOfSamples, int numberOfNodes, const 
  * reference; it exists for callers of this library that cannot allocate).
  *
  * mdas_create allocates the sampler's state with cudaMalloc.  Some callers
- * cannot allocate when they sample: a renderer that records its frame into a
- * CUDA graph by stream capture (allocating during capture is an error), a
- * plugin host that hands out all device memory up front, or a process whose
- * device memory belongs to another framework's allocator.  This call runs one
- * pass of KDGrid::AdaptiveSampling on buffers the caller owns, laid out like
- * the reference's sampler: coords (dim floats per sample, room for maxSamples
+ * cannot allocate when they sample: a plugin host that hands out all device
+ * memory up front and forbids allocations afterwards, a process whose device
+ * memory belongs to another framework's caching allocator (a library's own
+ * cudaMalloc can fail for memory the pool holds, or fragment it), or a
+ * frame-paced renderer for which cudaMalloc/cudaFree inside a frame cost too
+ * much (they can synchronise the device).  This call runs one pass of
+ * KDGrid::AdaptiveSampling on buffers the caller owns, laid out like the
+ * reference's sampler: coords (dim floats per sample, room for maxSamples
  * samples), nodes (4 ints per leaf, ~dim = empty), boxes (mn[dim] then
  * mx[dim] per leaf), errors and seeds (one per leaf; nodes, boxes, errors and
  * seeds with room for nodeCapacity leaves).  gError is the max leaf error of
  * the caller's errors pass.  The results equal mdas_adaptive_sampling's in
  * the reference arithmetic; the new counts are returned in *newSamples and
- * *newNodes (the call synchronises `stream`, like mdas_adaptive_sampling).
+ * *newNodes: the call copies them to the host and synchronises `stream`
+ * before it returns, like mdas_adaptive_sampling.
  *
- * Its only scratch (per-tile counts of 1024 leaves) lives in a fixed array of
- * device memory inside this library, so a pass takes at most
- * MDAS_STATIC_MAX_LEAVES leaves; larger passes return MDAS_ERR_INVALID, and
- * passes that could write past maxSamples samples or nodeCapacity leaves
- * return MDAS_ERR_CAPACITY.  Nothing in the array needs clearing between
- * calls: every call overwrites the entries it reads.  All calls share that
- * one array, so calls that overlap on the GPU (two streams, two threads)
- * race and must be serialised by the caller.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress); make that first
- * call before any stream capture that should contain later calls. */
+ * Its only scratch (per-tile counts of 1024 leaves, 64 KB) lives in a fixed
+ * array of device memory inside this library, so a pass takes at most
+ * MDAS_STATIC_MAX_LEAVES leaves; larger passes return MDAS_ERR_INVALID.  The
+ * capacity check is the worst case, stricter than the reference's own sizes:
+ * every leaf may take one sample and split into one more leaf, so it needs
+ * maxSamples >= numberOfSamples + numberOfNodes and nodeCapacity >=
+ * 2 * numberOfNodes, and returns MDAS_ERR_CAPACITY otherwise, before any
+ * work.  Nothing in the array needs clearing between calls: every call
+ * overwrites the entries it reads.  All calls share that one array, so calls
+ * that overlap on the GPU (two streams, two threads) race and must be
+ * serialised by the caller.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) and keeps it; the call must not be
+ * used across a cudaDeviceReset. */
 #define MDAS_STATIC_MAX_LEAVES (1 << 22)
 int mdas_adaptive_sampling_static(int dim, int numberOfSamples, int numberOfNodes, int candidatesNum, float alpha,
                                   float gError, int maxSamples, int nodeCapacity, float* coords, int* nodes,
@@ -165,6 +171,11 @@ int mdas_adaptive_sampling_static(int dim, int numberOfSamples, int numberOfNode
  * [3] integrate, [4] integrand.  Timing is off until mdas_set_timing(g, 1). */
 int mdas_set_timing(mdas_grid* g, int on);
 int mdas_get_stage_times(mdas_grid* g, double* ms5, int reset);
+/* The same n <= 6 times; [5] is the adaptive pass as the caller sees it, from
+ * its launch until the host holds the new counts (the window of the
+ * reference's own ADAPTIVE SAMPLING TIME, which ends after its two blocking
+ * counter reads, kdgrid.cu:753-768); [2] is its kernels' device time only. */
+int mdas_get_stage_times_ex(mdas_grid* g, double* ms, int n, int reset);
 
 /* Tallies of the last sampling pass (for traffic accounting): leaves whose error
  * was recomputed, leaves accepted, leaves split, and sample coordinates the

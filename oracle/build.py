@@ -3,7 +3,8 @@
 * ``build_oracle()`` compiles the CPU restatement ``oracle/mdas_oracle.cpp``
   into ``oracle/_build/liboracle.so`` (g++, -ffp-contract=off, OpenMP).
 * ``prepare_ref_sources()`` — only where the reference checkout exists
-  (``/root/reference``) — copies the reference's MDAS sources and the headers
+  (``$MDAS_REFERENCE_ROOT``, else a checkout named ``reference`` beside this
+  repository) — copies the reference's MDAS sources and the headers
   they include into ``oracle/_ref/src`` and applies four mechanical edits
   that CUDA 13 needs (texture references were removed in CUDA 12; the
   reference also relies on an MSVC leniency for a missing ``typename``):
@@ -38,7 +39,8 @@ ORACLE_LIB = os.path.join(BUILD, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_SRC = os.path.join(REF_DIR, "src")
 REF_LIB = os.path.join(REF_DIR, "libmdas_ref.so")
-REFERENCE = os.environ.get("MDAS_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: $MDAS_REFERENCE_ROOT, else ../reference relative to the repository
+REFERENCE = os.environ.get("MDAS_REFERENCE_ROOT") or os.path.normpath(os.path.join(ROOT, os.pardir, "reference"))
 
 # (path in the reference checkout, path under oracle/_ref/src)
 REF_FILES = [

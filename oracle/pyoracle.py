@@ -303,6 +303,7 @@ class RefGrid:
                 "ref_initial_sampling_async": (_I, [_P]),
                 "ref_compute_errors_async": (_I, [_P]),
                 "ref_adaptive_sampling_async": (_I, [_P]),
+                "ref_adaptive_sampling_kernel_timed": (_I, [_P, C.POINTER(_F)]),
                 "ref_integrate_async": (_I, [_P, _P, _I, _I]),
                 "ref_integrate": (_I, [_P, _P, _I, _I]),
                 "ref_convert_to_bytes": (_I, [_P, _P, _P, _I, _I]),
@@ -311,6 +312,7 @@ class RefGrid:
                 "ref_set_counts": (_I, [_P, _I, _I]),
                 "ref_get_gerror": (_F, []),
                 "ref_ptr": (_P, [_P, _I]),
+                "ref_set_log": (_I, [_P, C.c_char_p]),
             }
             for name, (res, args) in sig.items():
                 fn = getattr(lib, name)

@@ -42,6 +42,7 @@ struct RefBase {
     virtual void initial() = 0;
     virtual void errors() = 0;
     virtual void adaptive() = 0;
+    virtual float adaptive_kernel_ms() = 0;
     virtual void integrate(float4* p, int w, int h) = 0;
     virtual void bytes(float4* p, uchar4* b, int w, int h) = 0;
     virtual void density(float4* p, int w, int h) = 0;
@@ -49,11 +50,13 @@ struct RefBase {
     virtual void set_counts(int N, int L) = 0;
     virtual void* ptr(int which) = 0;
     virtual int dim() = 0;
+    virtual int set_log(const char* path) = 0;
 };
 
 template <class P>
 struct Ref : RefBase {
     mdas::KDGrid<P> g;
+    std::ofstream logFile;
     Ref(int maxSamples, int cand, int bpd, int eib, float alpha, float sx, float sy)
         : g(maxSamples, cand, bpd, eib, alpha, sx, sy, nullptr) {
         g.newSamples = 0;
@@ -62,6 +65,37 @@ struct Ref : RefBase {
     void initial() override { g.InitialSampling(); }
     void errors() override { g.ComputeErrors(); }
     void adaptive() override { g.AdaptiveSampling(); }
+    // KDGrid::AdaptiveSampling (kdgrid.cu:718-773) with its two counter reads
+    // outside the timed window: the counters are zeroed, the kernel is launched
+    // with the reference's own launch shape between two events, and the counts
+    // are read back afterwards; returns the kernel's device time in ms.
+    float adaptive_kernel_ms() override {
+        const int zero = 0;
+        cudaMemcpyToSymbol(mdas::g_warpCounter0, &zero, sizeof(int));
+        cudaMemcpyToSymbol(mdas::g_warpCounter1, &zero, sizeof(int));
+        int minGridSize = 0, blockSize = 0;
+        cudaOccupancyMaxPotentialBlockSize(&minGridSize, &blockSize, mdas::adaptiveSamplingKernel<P>, 0, 0);
+        const int gridSize = (g.numberOfNodes + blockSize - 1) / blockSize;
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, 0);
+        mdas::adaptiveSamplingKernel<P><<<gridSize, blockSize>>>(g.numberOfNodes, g.numberOfSamples, g.maxNodeSize,
+                                                                 g.candidatesNum, g.alpha, g.nodeErrors.Data(),
+                                                                 g.nodes.Data(), g.nodeBoxes.Data(),
+                                                                 g.sampleCoordinates.Data(), g.seeds.Data());
+        cudaEventRecord(b, 0);
+        cudaMemcpyFromSymbol(&g.newSamples, mdas::g_warpCounter0, sizeof(int), 0);
+        g.numberOfSamples += g.newSamples;
+        cudaMemcpyFromSymbol(&g.newNodes, mdas::g_warpCounter1, sizeof(int), 0);
+        g.numberOfNodes += g.newNodes;
+        float ms = 0.0f;
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(&ms, a, b);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        return ms;
+    }
     void integrate(float4* p, int w, int h) override { g.Integrate(p, w, h); }
     void bytes(float4* p, uchar4* b, int w, int h) override { g.ConvertToBytes(p, b, w, h); }
     void density(float4* p, int w, int h) override { g.SamplingDensity(p, w, h); }
@@ -87,6 +121,19 @@ struct Ref : RefBase {
         return nullptr;
     }
     int dim() override { return P::DIM; }
+    // The reference's own per-stage log (the `log` constructor argument of
+    // kdgrid.cu:600-631): path NULL closes it and stops the logging.
+    int set_log(const char* path) override {
+        if (logFile.is_open()) logFile.close();
+        g.log = nullptr;
+        g.logStats = false;
+        if (!path) return 0;
+        logFile.open(path, std::ios::out | std::ios::trunc);
+        if (!logFile.good()) return 1;
+        g.log = &logFile;
+        g.logStats = true;
+        return 0;
+    }
 };
 
 }  // namespace
@@ -118,6 +165,12 @@ int ref_adaptive_sampling(void* h) { ((RefBase*)h)->adaptive(); return (int)cuda
 int ref_initial_sampling_async(void* h) { ((RefBase*)h)->initial(); return (int)cudaGetLastError(); }
 int ref_compute_errors_async(void* h) { ((RefBase*)h)->errors(); return (int)cudaGetLastError(); }
 int ref_adaptive_sampling_async(void* h) { ((RefBase*)h)->adaptive(); return (int)cudaGetLastError(); }
+// The adaptive pass with only its kernel between the events (the counter reads
+// follow the window); *kernelMs receives that device time.
+int ref_adaptive_sampling_kernel_timed(void* h, float* kernelMs) {
+    *kernelMs = ((RefBase*)h)->adaptive_kernel_ms();
+    return (int)cudaGetLastError();
+}
 int ref_integrate_async(void* h, float* pixels, int w, int hgt) {
     ((RefBase*)h)->integrate((float4*)pixels, w, hgt);
     return (int)cudaGetLastError();
@@ -150,5 +203,6 @@ float ref_get_gerror() {
     return v;
 }
 void* ref_ptr(void* h, int which) { return ((RefBase*)h)->ptr(which); }
+int ref_set_log(void* h, const char* path) { return ((RefBase*)h)->set_log(path); }
 
 }  // extern "C"

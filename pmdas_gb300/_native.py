@@ -88,6 +88,7 @@ SIGNATURES = {
                                            C.POINTER(_I), _P]),
     "mdas_set_timing": (_I, [_P, _I]),
     "mdas_get_stage_times": (_I, [_P, C.POINTER(C.c_double), _I]),
+    "mdas_get_stage_times_ex": (_I, [_P, C.POINTER(C.c_double), _I, _I]),
     "mdas_get_launch_count": (_I, [_P, C.POINTER(C.c_uint64)]),
     "mdas_get_pass_stats": (_I, [_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_int64)]),
     "mdas_status_string": (C.c_char_p, [_I]),

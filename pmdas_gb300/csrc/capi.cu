@@ -73,7 +73,9 @@ struct mdas_grid {
     MdasCounts* hcounts = nullptr;  // pinned mirror of the device counters
     std::ofstream* log = nullptr;
     bool timing = false;
-    double stageMs[5] = {0, 0, 0, 0, 0};
+    // [0..4] device time of the stages' kernels; [5] the adaptive pass as the
+    // caller sees it: from its launch until the host holds the new counts
+    double stageMs[6] = {0, 0, 0, 0, 0, 0};
     uint64_t launches = 0;
     float* scratch = nullptr;  // density / host-render image
     size_t scratchBytes = 0;
@@ -454,13 +456,28 @@ int mdas_adaptive_sampling(mdas_grid* g) {
     const int gridDecide = grid_for(g, MDAS_K_DECIDE, tiles * 256);
     const int gridPlace = grid_for(g, MDAS_K_ADAPTIVE, g->L);  // one thread per accepted leaf (<= L)
     g->dg.priority = g->learned && g->lPredVersion == g->version ? g->lPred : nullptr;
+    cudaEvent_t apiA = nullptr;
+    if (g->timing) {
+        apiA = pool_get(g);
+        cudaEventRecord(apiA, g->stream);
+    }
     int rc = timed(g, 2, [&]() { return launch_adaptive(g, gridDecide, gridPlace); });
     g->dg.priority = nullptr;
     g->dirtyValid = g->errorsClean;
     g->errorsClean = false;
     g->launches += 3;
-    if (rc) return rc;
+    if (rc) {
+        if (apiA) g->eventPool.push_back(apiA);
+        return rc;
+    }
     rc = read_counts(g);
+    if (apiA) {
+        // recorded once the host holds the counts, as the reference's log records its
+        // stop event after its two blocking counter reads (kdgrid.cu:753-768)
+        cudaEvent_t apiB = pool_get(g);
+        cudaEventRecord(apiB, g->stream);
+        g->pending.push_back({5, apiA, apiB});
+    }
     if (g->log) {
         const double t = last_stage_ms(g, 2);
         *g->log << "SAMPLES\n" << g->newN << std::endl;
@@ -700,6 +717,15 @@ int mdas_get_stage_times(mdas_grid* g, double* ms5, int reset) {
     if (!g || !ms5) return MDAS_ERR_INVALID;
     flush_timing(g);
     for (int i = 0; i < 5; ++i) ms5[i] = g->stageMs[i];
+    if (reset)
+        for (double& x : g->stageMs) x = 0.0;
+    return MDAS_OK;
+}
+
+int mdas_get_stage_times_ex(mdas_grid* g, double* ms, int n, int reset) {
+    if (!g || !ms || n < 0) return MDAS_ERR_INVALID;
+    flush_timing(g);
+    for (int i = 0; i < n && i < 6; ++i) ms[i] = g->stageMs[i];
     if (reset)
         for (double& x : g->stageMs) x = 0.0;
     return MDAS_OK;

@@ -1,17 +1,23 @@
 // noalloc.cu — one adaptive sampling pass that allocates no memory.
 //
-// Some callers cannot call cudaMalloc when they run a sampling pass: a renderer
-// that records its frame into a CUDA graph by stream capture (an allocation
-// during capture is an error), a plugin host that hands out all device memory
-// up front and forbids allocations afterwards, or a process whose device memory
-// belongs to another framework's allocator.  mdas_create allocates the sampler
-// state, so those callers cannot use a grid.  This entry point runs one pass of
-// KDGrid::AdaptiveSampling on buffers the caller already owns, in the layout of
-// the reference's sampler (nodes as int4, boxes as mn[D] + mx[D], AoS sample
-// coordinates, per-leaf errors and seeds), and keeps its own scratch — the
-// per-tile counts and their prefix — in a fixed-size array in device memory
-// that is part of this library (every GPU that loads the library holds it until
-// the process exits).
+// Some callers cannot call cudaMalloc when they run a sampling pass:
+//   * a plugin host that hands out all device memory up front and forbids
+//     allocations afterwards (its budget is fixed when the plugin loads);
+//   * a process whose device memory belongs to another framework's caching
+//     allocator, where a library's own cudaMalloc can fail for lack of memory
+//     the pool is holding, or fragment it;
+//   * a frame-paced renderer for which cudaMalloc/cudaFree are too costly
+//     inside the frame: they can synchronise the device and stall it.
+// mdas_create allocates the sampler state, so those callers cannot use a grid.
+// This entry point runs one pass of KDGrid::AdaptiveSampling on buffers the
+// caller already owns, in the layout of the reference's sampler (nodes as
+// int4, boxes as mn[D] + mx[D], AoS sample coordinates, per-leaf errors and
+// seeds), and keeps its own scratch — the per-tile counts and their prefix —
+// in a fixed-size array in device memory that is part of this library (every
+// GPU that loads the library holds it until the process exits).
+//
+// The call reads the new counts back to the host and synchronises the
+// caller's stream before it returns, as mdas_adaptive_sampling does.
 //
 // The pass computes what mdas_adaptive_sampling computes in the reference
 // arithmetic (this file is built with --use_fast_math like kdgrid_fast.cu):
@@ -349,7 +355,10 @@ __global__ void __launch_bounds__(256) k_static_place(PassArgs a) {
     }
 }
 
-// Device address of the scratch array, looked up once per device.
+// Device address of the scratch array, looked up once per device (at the first
+// call with that device current) and kept for the life of the process.  After
+// cudaDeviceReset the library's module is loaded again and the kept address
+// is stale, so the call must not be used across a device reset.
 std::mutex g_scratchMutex;
 void* g_scratchPtr[64] = {nullptr};
 

@@ -200,8 +200,10 @@ class KDGrid:
         N.check(self._lib.mdas_set_timing(self._h, 1 if on else 0), "set_timing")
 
     def stage_times(self, reset: bool = False) -> list:
-        a = (C.c_double * 5)()
-        N.check(self._lib.mdas_get_stage_times(self._h, a, 1 if reset else 0), "stage_times")
+        """Per-stage ms since the last reset: init, errors, adaptive (kernels),
+        integrate, integrand, and the adaptive pass until the host holds its counts."""
+        a = (C.c_double * 6)()
+        N.check(self._lib.mdas_get_stage_times_ex(self._h, a, 6, 1 if reset else 0), "stage_times")
         return list(a)
 
     def pass_stats(self) -> dict:

@@ -1,14 +1,14 @@
 """The adaptive pass that allocates nothing (mdas_adaptive_sampling_static),
 checked against the grid's own pass (mdas_adaptive_sampling) on two passes in a
-row.
+row, for every point dimension (3..6) and on states of several 1024-leaf tiles.
 
 Who uses it: callers that cannot allocate device memory at the moment they
-sample — a renderer that records its frame into a CUDA graph by stream capture
-(allocating during capture is an error), a plugin host that hands out all
-device memory up front, or a process whose device memory belongs to another
-allocator.  They keep the sampler state in buffers they allocated themselves,
-in the reference's layout, and the pass keeps its scratch in a fixed array
-inside the library.  Its results must be exactly those of the grid's pass.
+sample — a plugin host that hands out all device memory up front, a process
+whose device memory belongs to another framework's caching allocator, or a
+frame-paced renderer for which cudaMalloc/cudaFree inside a frame cost too much.
+They keep the sampler state in buffers they allocated themselves, in the
+reference's layout, and the pass keeps its scratch in a fixed array inside the
+library.  Its results must be exactly those of the grid's pass.
 
 This file is collected last so that a run stopping at the first failure has
 already run every other test; it also passes on its own in a fresh process.
@@ -24,13 +24,28 @@ from pmdas_gb300 import _native as N
 pytestmark = pytest.mark.gpu
 
 
-def test_static_pass_equals_grid_pass_two_calls(cuda):
+# (dim, scene kind, width, height, extraImgBits, candidates): every state spans
+# 16 to 32 tiles of 1024 leaves, so the cross-tile prefix of the scan is
+# exercised in each dimension
+CASES = {
+    "mb3d": (3, P.SCENE_DISCS_MB, 128, 96, 6, 4),
+    "dof4d": (4, P.SCENE_DISCS_DOF, 128, 96, 5, 4),
+    "mbdof5d": (5, P.SCENE_DISCS_MBDOF, 96, 64, 5, 3),
+    "mbdof6d": (6, P.SCENE_DISCS_MBDOF, 64, 64, 4, 2),
+}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_static_pass_equals_grid_pass_two_calls(cuda, case):
     import torch
-    D, W, H = 4, 128, 96
-    maxSamples, cand, bpd, eib, alpha = 400000, 4, 1, 4, 0.25
+    D, kind, W, H, eib, cand = CASES[case]
+    bpd, alpha = 1, 0.25
+    L0 = (1 << (bpd * D)) << (2 * eib)
+    maxSamples = 12 * L0
     nodeCap = 2 * maxSamples - 1  # what the reference allocates for leaves
+    assert L0 >= 16 * 1024
     grid = P.KDGrid(D, maxSamples, cand, bpd, eib, alpha, W, H)  # reference arithmetic, as the static pass
-    scene = P.Scene(P.SCENE_DISCS_DOF, 3, 64, W, H, W, H)
+    scene = P.Scene(kind, 3, 64, W, H, W, H)
     grid.InitialSampling()
     scene.evaluate(grid, 0, grid.GetNumberOfSamples())
 
