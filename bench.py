@@ -137,8 +137,9 @@ def ncu_stage_traffic(path: str) -> dict:
     cols = rows[head]
     ki, ni, vi, ui = cols.index("ID"), cols.index("Kernel Name"), cols.index("Metric Value"), cols.index("Metric Unit")
     mi = cols.index("Metric Name")
-    scale = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "nsecond": 1e-3, "usecond": 1.0,
-             "msecond": 1e3, "second": 1e6}
+    scale = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "KB": 1e3, "MB": 1e6, "GB": 1e9,
+             "ns": 1e-3, "nsecond": 1e-3, "us": 1.0, "usecond": 1.0, "ms": 1e3, "msecond": 1e3, "s": 1e6,
+             "second": 1e6}
     for r in rows[head + 1:]:
         if len(r) <= max(ki, ni, vi, mi):
             continue
@@ -157,6 +158,9 @@ def ncu_stage_traffic(path: str) -> dict:
         o["launches"] += 1
         o["dram_bytes"] += d["bytes"]
         o["us"] += d["us"]
+    for o in out.values():  # per launch, as the roofline counts them
+        o["dram_mb_per_launch"] = round(o["dram_bytes"] / o["launches"] / 1e6, 2)
+        o["us_per_launch"] = round(o["us"] / o["launches"], 2)
     return out
 
 

@@ -166,6 +166,15 @@ int mdas_adaptive_sampling_static(int dim, int numberOfSamples, int numberOfNode
                                   float* boxes, float* errors, uint32_t* seeds, int* newSamples, int* newNodes,
                                   void* stream);
 
+/* Test hook (no counterpart in the reference): the number of polls after which
+ * the library's bounded device-side waits report MDAS_ERR_TIMEOUT (polls <= 0
+ * restores their own limits).  The radix sort's look-back then gives up and
+ * its output is incomplete (its scatter stays in bounds); the waits for the
+ * tensor-core MMAs of the priority MLP record the timeout and wait on with
+ * their own limit, so their results stay complete and no MMA is in flight
+ * when a kernel ends.  Process-wide; needs a current CUDA device. */
+int mdas_test_set_wait_limit(int polls);
+
 /* Per-stage CUDA-event times accumulated since the last reset, in ms:
  * [0] initial sampling, [1] compute errors, [2] adaptive sampling,
  * [3] integrate, [4] integrand.  Timing is off until mdas_set_timing(g, 1). */

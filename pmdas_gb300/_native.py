@@ -89,6 +89,7 @@ SIGNATURES = {
     "mdas_set_timing": (_I, [_P, _I]),
     "mdas_get_stage_times": (_I, [_P, C.POINTER(C.c_double), _I]),
     "mdas_get_stage_times_ex": (_I, [_P, C.POINTER(C.c_double), _I, _I]),
+    "mdas_test_set_wait_limit": (_I, [_I]),
     "mdas_get_launch_count": (_I, [_P, C.POINTER(C.c_uint64)]),
     "mdas_get_pass_stats": (_I, [_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_int64)]),
     "mdas_status_string": (C.c_char_p, [_I]),

@@ -118,6 +118,20 @@ namespace {
 
 int status_of(cudaError_t e) { return e == cudaSuccess ? MDAS_OK : MDAS_ERR_CUDA; }
 
+// tea<4>(v, 0) of SDK/cuda/random.h:31-46: the seed a leaf slot's first draw
+// starts from.  The grid stores it in slots that were never drawn from; the
+// reference stores 0 there (kdgrid.cu:323-324, 637), and the state dump and
+// load translate between the two.
+uint32_t host_tea4(uint32_t val0) {
+    uint32_t v0 = val0, v1 = 0, s0 = 0;
+    for (int n = 0; n < 4; n++) {
+        s0 += 0x9e3779b9u;
+        v0 += ((v1 << 4) + 0xa341316cu) ^ (v1 + s0) ^ ((v1 >> 5) + 0xc8013ea4u);
+        v1 += ((v0 << 4) + 0xad90777du) ^ (v0 + s0) ^ ((v0 >> 5) + 0x7e95761eu);
+    }
+    return v0;
+}
+
 cudaEvent_t pool_get(mdas_grid* g) {
     if (!g->eventPool.empty()) {
         cudaEvent_t e = g->eventPool.back();
@@ -607,6 +621,9 @@ int mdas_dump_state(mdas_grid* g, float* coords, float* values, int* nodes, floa
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     if (stage) cudaFree(stage);
+    if (e == cudaSuccess && seeds)
+        for (size_t i = 0; i < L; ++i)
+            if (seeds[i] == host_tea4((uint32_t)i)) seeds[i] = 0u;  // never drawn: the reference's 0
     return status_of(e);
 }
 
@@ -617,6 +634,8 @@ int mdas_load_state(mdas_grid* g, int numberOfSamples, int numberOfNodes, const 
         return MDAS_ERR_INVALID;
     const MdasDeviceGrid& d = g->dg;
     const size_t N = (size_t)numberOfSamples, L = (size_t)numberOfNodes;
+    for (size_t k = 0; k < 4 * L; ++k)
+        if (nodes[k] >= (int)N) return MDAS_ERR_INVALID;  // a node names a sample that does not exist
     cudaError_t e = cudaSuccess;
     auto cp = [&](void* dst, const void* src, size_t bytes) {
         if (bytes && e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, g->stream);
@@ -624,12 +643,14 @@ int mdas_load_state(mdas_grid* g, int numberOfSamples, int numberOfNodes, const 
     cp(d.coords, coords, sizeof(float) * N * d.D);
     cp(d.values, values, sizeof(float) * 3 * N);
     cp(d.errors, errors, sizeof(float) * L);
-    cp(d.seeds, seeds, sizeof(unsigned) * L);
+    // a never-drawn seed (0) is stored as the seed its first draw starts from
+    std::vector<uint32_t> stored(seeds, seeds + L);
+    for (size_t i = 0; i < L; ++i)
+        if (stored[i] == 0u) stored[i] = host_tea4((uint32_t)i);
+    cp(d.seeds, stored.data(), sizeof(unsigned) * L);
     // build the leaf records from the nodes, boxes and (already loaded) coordinates
     void* stage = nullptr;
     if (L && e == cudaSuccess) {
-        for (size_t k = 0; k < 4 * L; ++k)
-            if (nodes[k] >= (int)N) return MDAS_ERR_INVALID;  // a node names a sample that does not exist
         const size_t nb = sizeof(int4) * L, bb = sizeof(float) * 2 * d.D * L;
         e = cudaMalloc(&stage, nb + bb);
         if (e == cudaSuccess) {
@@ -705,6 +726,11 @@ int mdas_validate(mdas_grid* g, int* valid) {
         if (hist[i] != 1) ok = false;
     *valid = ok ? 1 : 0;
     return MDAS_OK;
+}
+
+int mdas_test_set_wait_limit(int polls) {
+    mdas_order::set_test_wait_limit(polls);
+    return status_of(mdas_mlp::set_test_wait_limit(polls));
 }
 
 int mdas_set_timing(mdas_grid* g, int on) {

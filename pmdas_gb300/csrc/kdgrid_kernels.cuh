@@ -876,9 +876,14 @@ __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, i
             g.splitR[rank_] = make_int4(r0, r1, r2, __float_as_int(box_volume<D>(rmn, mx)));
         }
         // a new slot starts without a seed: the reference's seed buffer is zeroed
-        // once at InitialSampling (kdgrid.cu:637) and right-child slots are never
-        // written before; writing the 0 here makes that memset unnecessary
-        g.seeds[nodeOffset] = 0u;
+        // once at InitialSampling (kdgrid.cu:637), and a slot's first draw starts
+        // from tea<4>(slot, 0) when its seed is 0 (kdgrid.cu:323-324).  The slot
+        // stores that starting seed here instead of the 0, so that decide never
+        // computes tea<4> (a warp paid for it whenever one of its leaves was new);
+        // mdas_dump_state reports such a never-drawn seed as 0, as the reference
+        // holds it (a drawn seed is tea<4>(slot, 0) advanced by >= 1 LCG steps,
+        // which never returns to its start within the generator's 2^32 period)
+        g.seeds[nodeOffset] = tea4((unsigned)nodeOffset, 0);
         g.dirty[rank_] = nodeIndex;  // for the next errors pass
     }
 }

@@ -225,10 +225,34 @@ __device__ void ctx_close(Ctx& c) {
     }
 }
 
+// Polls after which an MMA wait reports a timeout (0: kWaitLimit).  A test sets
+// it small to drive the timeout path: the wait then polls without suspending
+// (a suspending poll could sit out the MMA), records the timeout in the status
+// word and waits on with kWaitLimit, so that the accumulator is complete before
+// it is read and no MMA is in flight when the tensor memory is freed.
+__device__ int test_wait_limit = 0;
+
+__device__ __forceinline__ bool mbar_test_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
 __device__ __forceinline__ void mma_wait(Ctx& c) {
+    const int polls = test_wait_limit;
     bool ok = false;
-    for (int i = 0; i < kWaitLimit && !ok; ++i) ok = mbar_try_wait(c.bar, c.phase);
-    if (!ok) atomicOr(c.status, 1u);
+    if (polls > 0)
+        for (int i = 0; i < polls && !ok; ++i) ok = mbar_test_wait(c.bar, c.phase);
+    else
+        for (int i = 0; i < kWaitLimit && !ok; ++i) ok = mbar_try_wait(c.bar, c.phase);
+    if (!ok) {
+        atomicOr(c.status, 1u);
+        for (int i = 0; i < kWaitLimit && !ok; ++i) ok = mbar_try_wait(c.bar, c.phase);
+    }
     c.phase ^= 1u;
     tc_fence_after();
 }
@@ -803,6 +827,11 @@ cudaError_t set_smem(K kernel, int bytes) {
 cudaError_t pack(const float* params, Packed* packed, cudaStream_t s) {
     k_pack<<<1, 1024, 0, s>>>(params, packed);
     return cudaGetLastError();
+}
+
+cudaError_t set_test_wait_limit(int polls) {
+    const int v = polls > 0 ? polls : 0;
+    return cudaMemcpyToSymbol(test_wait_limit, &v, sizeof(int));
 }
 
 cudaError_t forward(const Packed* w, const float* features, int m, float* pred, unsigned* status, cudaStream_t s) {

@@ -76,4 +76,7 @@ cudaError_t gradients(const Packed* w, const float* features, const float* targe
 cudaError_t adam(float* params, float* m1, float* m2, float* grads, int step, float lr, Packed* packed,
                  cudaStream_t s);
 
+// Polls after which the MMA waits report a timeout (<= 0: their own limit); a test hook.
+cudaError_t set_test_wait_limit(int polls);
+
 }  // namespace mdas_mlp

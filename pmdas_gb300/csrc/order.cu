@@ -278,7 +278,12 @@ struct SweepArgs {
     unsigned* lookback;          // [tiles * 256], zeroed
     unsigned* tileCounter;       // zeroed
     unsigned* status;
+    int spinLimit;               // polls of one look-back word before giving up
 };
+
+// The look-back's poll limit (0: kSpinLimit); a test sets it small to drive the
+// timeout path (set_test_wait_limit).
+int g_sortSpinLimit = 0;
 
 #ifndef MDAS_SORT_MIN_CTAS
 #define MDAS_SORT_MIN_CTAS 4  // 64 registers: 4 CTAs per SM (3 at 80 registers: 12 % slower)
@@ -372,7 +377,7 @@ __global__ void __launch_bounds__(kThreads, MDAS_SORT_MIN_CTAS) k_onesweep(Sweep
             if (done) break;
             t -= q;
             if (q < kWindow) {  // tile t has not published yet
-                if (++spins > kSpinLimit || ld_relaxed(a.status) != 0u) {
+                if (++spins > a.spinLimit || ld_relaxed(a.status) != 0u) {
                     atomicOr(a.status, 1u);
                     break;
                 }
@@ -520,6 +525,7 @@ cudaError_t radix_sort(void* temp, size_t tempBytes, const uint64_t* keysIn, uin
         a.lookback = reinterpret_cast<unsigned*>(base + l.lookback) + (size_t)p * tiles * kBins;
         a.tileCounter = counters + p;
         a.status = status;
+        a.spinLimit = g_sortSpinLimit > 0 ? g_sortSpinLimit : kSpinLimit;
         k_onesweep<<<(unsigned)tiles, kThreads, kSweepSmem, s>>>(a);
         srcK = a.keysOut;
         srcV = a.valuesOut;
@@ -719,5 +725,7 @@ int query_fine_bits(int D, int bitsPerDim, int extraImgBits) {
     if (fine > 31 - bitsPerDim - extraImgBits) fine = 31 - bitsPerDim - extraImgBits;
     return fine > 0 ? fine : 0;
 }
+
+void set_test_wait_limit(int polls) { g_sortSpinLimit = polls > 0 ? polls : 0; }
 
 }  // namespace mdas_order

@@ -59,4 +59,7 @@ cudaError_t locate(const MdasDeviceGrid& g, const uint32_t* order, int n, const 
 // large point location (the keys then fit in 32 bits where the grid allows).
 int query_fine_bits(int D, int bitsPerDim, int extraImgBits);
 
+// Polls of the sort's look-back before it gives up (<= 0: its own limit); a test hook.
+void set_test_wait_limit(int polls);
+
 }  // namespace mdas_order

@@ -163,6 +163,45 @@ def test_batch_equals_single_renders(cuda, arith):
     batch.close()
 
 
+def test_batch_ieee_matches_oracle_directly(cuda):
+    """A strict-IEEE batch of three images of different dimension, compared with
+    the CPU oracle's own budget loop for each image (not only with single GPU
+    renders): the whole final state bit for bit and the image within 1e-5."""
+    import torch
+    specs = [  # (kind, D, W, H, spp, bpd, eib, alpha, cand, seed, prims)
+        (P.SCENE_DISCS_MB, 3, 48, 32, 8, 1, 3, 0.25, 4, 21, 32),
+        (P.SCENE_DISCS_DOF, 4, 64, 48, 12, 1, 3, 0.25, 4, 22, 48),
+        (P.SCENE_DISCS_MBDOF, 5, 32, 32, 10, 1, 2, 0.0625, 3, 23, 32),
+    ]
+    grids, scenes, pix, budgets = [], [], [], []
+    for kind, D, W, H, spp, bpd, eib, alpha, cand, seed, prims in specs:
+        budget = spp * W * H
+        ms = 2 * budget + 8 * ((1 << (bpd * D)) << (2 * eib))
+        scenes.append(P.Scene(kind, seed, prims, W, H, W, H))
+        grids.append(P.KDGrid(D, ms, cand, bpd, eib, alpha, W, H, arith=P.ARITH_IEEE))
+        pix.append(torch.zeros(H, W, 4, device="cuda"))
+        budgets.append(budget)
+    batch = P.Batch(grids, scenes, budgets, pix, [sp[2] for sp in specs], [sp[3] for sp in specs])
+    stats = batch.render()
+    for i, (kind, D, W, H, spp, bpd, eib, alpha, cand, seed, prims) in enumerate(specs):
+        ms = grids[i].GetMaxSamples()
+        o = O.OracleGrid(D, ms, cand, bpd, eib, alpha, W, H)
+        desc = scenes[i].export()
+        o.initial_sampling()
+        o.evaluate(desc, 0, o.N)
+        passes = 0
+        while o.N < budgets[i] and o.N + o.L <= ms:
+            o.sampling_pass()
+            o.evaluate(desc, o.N - o.newN, o.newN)
+            passes += 1
+        assert stats[i].passes == passes and passes > 0, (i, stats[i].passes, passes)
+        assert_states_equal(grids[i].dump_state(), o.dump_state(),
+                            keys=("coords", "values", "nodes", "boxes", "errors", "seeds"), what=f"image {i}")
+        ok, worst = rel_close(pix[i].cpu().numpy(), o.integrate(W, H))
+        assert ok, (i, worst)
+    batch.close()
+
+
 def test_reference_build_close_to_oracle(cuda):
     """The fast-math build differs from IEEE only in the last bits of divisions,
     square roots and powf: same initial grid (power-of-two extents), errors within
