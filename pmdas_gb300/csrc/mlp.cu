@@ -13,10 +13,10 @@
 // matrices of 128 contiguous bytes, K-blocks of one row group adjacent.
 //
 // Training (gradients) runs the same forward, then on the tensor cores
-// dH1 = dZ2 . W2 (M 128, N 64, K 64, W2 transposed as the K-major B operand),
-// and the weight gradients dW2 = dZ2^T H1, dW1 = dZ1^T X as per-CTA reductions
-// over the tile's 128 rows on the CUDA cores, added to the global gradient
-// with atomics.
+// dH1 = dZ2 . W2 (M 128, N 64, K 64, W2 transposed as the K-major B operand)
+// and the weight gradients dW2 = dZ2^T H1, dW1 = dZ1^T X as one GEMM per tile
+// (M 128, N 80, K 128 over the tile's rows) accumulated in tensor memory over
+// all tiles of a persistent CTA, added to the global gradient once per CTA.
 #include "mlp.h"
 #include "leaf_raw.h"
 #include "ld_hint.h"
@@ -104,11 +104,14 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
 }
 constexpr uint32_t kIdesc = idesc_bf16(kRows, kH);
 
-__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t accumulate) {
+__device__ __forceinline__ void mma_bf16_id(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d),
-        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
         : "memory");
+}
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t accumulate) {
+    mma_bf16_id(d, a, b, kIdesc, accumulate);
 }
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
@@ -176,7 +179,7 @@ __device__ __forceinline__ void warp_sum64(float (&v)[kH], float* out) {
 // ---- per-CTA setup / teardown -------------------------------------------------------
 struct Ctx {
     uint8_t* sm;
-    uint32_t base, bar, tmem, phase;
+    uint32_t base, bar, tmem, phase, cols;
     unsigned* status;
 };
 
@@ -195,11 +198,13 @@ __device__ __forceinline__ void copy_weights(uint8_t* sm, const Packed* w) {
     for (int i = threadIdx.x; i < n16; i += kThreads) dst[i] = src[i];
 }
 
-__device__ void ctx_open(Ctx& c, const Packed* w, unsigned* status) {
+// cols: tensor-memory columns of the CTA (a power of 2, >= 32)
+__device__ void ctx_open(Ctx& c, const Packed* w, unsigned* status, uint32_t cols = kTmemCols) {
     c.sm = aligned_smem();
     c.base = smem_u32(c.sm);
     c.bar = c.base + SM_BAR;
     c.phase = 0;
+    c.cols = cols;
     c.status = status;
     if (w) copy_weights(c.sm, w);
     if (threadIdx.x == 0) {
@@ -207,7 +212,7 @@ __device__ void ctx_open(Ctx& c, const Packed* w, unsigned* status) {
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (threadIdx.x < 32) {
-        tmem_alloc(c.base + SM_BAR + 8, kTmemCols);
+        tmem_alloc(c.base + SM_BAR + 8, cols);
         tmem_relinquish();
     }
     tc_fence_before();
@@ -221,7 +226,7 @@ __device__ void ctx_close(Ctx& c) {
     __syncthreads();
     if (threadIdx.x < 32) {
         tc_fence_after();
-        tmem_dealloc(c.tmem, kTmemCols);
+        tmem_dealloc(c.tmem, c.cols);
     }
 }
 
@@ -633,135 +638,161 @@ __global__ void k_leaf_features(MdasDeviceGrid g, int L, float* __restrict__ out
     }
 }
 
-// One CTA per tile of 128 rows: forward, backward, per-CTA gradient, atomics.
+// Training: persistent CTAs over tiles of 128 rows.  Per tile: forward, then
+// dZ2 (CUDA cores), dH1 = dZ2 . W2 on the tensor cores, dZ1; the weight
+// gradients of both layers as one more tensor-core GEMM per tile,
+//   [dZ2^T ; dZ1^T] (128 x 128 rows) . [H1 | X] (128 rows x 80)
+// whose 64 x 64 top-left block is dW2 and 64 x 16 bottom-right block is dW1
+// (the other blocks are not used), accumulated in tensor memory over all the
+// CTA's tiles; the bias-like gradients as warp reductions into shared memory.
+// At the end each CTA adds its gradient to the global one (a few thousand
+// atomics per CTA, not per tile).  BF16 operands (dZ rounded like the other
+// GEMM inputs), FP32 accumulation.
+constexpr int SM_AG = SM_Z2F;            // [dZ2^T ; dZ1^T]: 128 x 128 BF16, K-major, 16 K-blocks per row group
+constexpr int SM_BG = SM_Z1F;            // [H1 | X]^T: 80 x 128 BF16, K-major, 16 K-blocks per row group
+constexpr int kGradN = kH + kIn;         // 80 columns of the weight-gradient accumulator
+constexpr uint32_t kGradCol = 128;       // its first tensor-memory column
+constexpr uint32_t kTrainCols = 256;     // tensor-memory columns of a training CTA
+constexpr uint32_t kGradIdesc = idesc_bf16(kRows, kGradN);
+static_assert(kRows * kRows * 2 <= SM_D - SM_Z2F, "the A tile of the weight gradients fits");
+static_assert(kGradN * kRows * 2 <= SM_G - SM_Z1F, "the B tile of the weight gradients fits");
+static_assert(kGradCol + kGradN <= kTrainCols, "tensor-memory columns");
+
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_gradients(const Packed* __restrict__ w, const float* __restrict__ feats,
                                                         const float* __restrict__ targets, MdasDeviceGrid g, int L,
                                                         int offset, int stride, int m, float* __restrict__ grads,
                                                         float* __restrict__ lossSum, unsigned* status) {
     Ctx c;
-    ctx_open(c, w, status);
+    ctx_open(c, w, status, kTrainCols);
     float* sg = reinterpret_cast<float*>(c.sm + SM_G);
     for (int i = threadIdx.x; i < MDAS_MLP_PARAMS; i += kThreads) sg[i] = 0.0f;
     const float* vec = reinterpret_cast<const float*>(c.sm + SM_VEC);
     const float* w3 = vec + 2 * kH;
-    float* z2f = reinterpret_cast<float*>(c.sm + SM_Z2F);
-    float* z1f = reinterpret_cast<float*>(c.sm + SM_Z1F);
-    const int t = threadIdx.x;
-    const int r = blockIdx.x * kRows + t;
-    const bool valid = r < m;
-    float f[kIn];
-    float y = 0.0f;
-    if (!valid) {
-#pragma unroll
-        for (int i = 0; i < kIn; ++i) f[i] = 0.0f;
-    } else if (feats) {
-#pragma unroll
-        for (int i = 0; i < kIn; ++i) f[i] = feats[(size_t)r * kIn + i];
-        y = targets[r];
-    } else {
-        const int leaf = (int)(((long long)offset + (long long)r * stride) % L);
-        float err;
-        leaf_feats<D>(g, leaf, L, f, &err);
-        y = target_of(err);
-    }
-    put_features(c, f);
-    float z2[kH];
-    tile_forward(c, z2);
-    const float e = valid ? head(c, z2) - y : 0.0f;
-    const float dpred = 2.0f * e / (float)m;  // 0 on rows past m
+    uint8_t* ag = c.sm + SM_AG;
+    uint8_t* bg = c.sm + SM_BG;
     float* red = reinterpret_cast<float*>(c.sm + SM_RED);
+    const int t = threadIdx.x;
     const int warp = t >> 5;
-    float dz[kH];
-    {
-        float v[kH];
+    const int tiles = (m + kRows - 1) / kRows;
+    float lossPart = 0.0f;
+    bool first = true;
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int r = tile * kRows + t;
+        const bool valid = r < m;
+        float f[kIn];
+        float y = 0.0f;
+        if (!valid) {
+#pragma unroll
+            for (int i = 0; i < kIn; ++i) f[i] = 0.0f;
+        } else if (feats) {
+#pragma unroll
+            for (int i = 0; i < kIn; ++i) f[i] = feats[(size_t)r * kIn + i];
+            y = targets[r];
+        } else {
+            const int leaf = (int)(((long long)offset + (long long)r * stride) % L);
+            float err;
+            leaf_feats<D>(g, leaf, L, f, &err);
+            y = target_of(err);
+        }
+        put_features(c, f);
+        float z2[kH];
+        tile_forward(c, z2);
+        const float e = valid ? head(c, z2) - y : 0.0f;
+        const float dpred = 2.0f * e / (float)m;  // 0 on rows past m
+        float dz[kH];
+        {
+            float v[kH];
+#pragma unroll
+            for (int j = 0; j < kH; ++j) {
+                v[j] = dpred * fmaxf(z2[j], 0.0f);
+                dz[j] = z2[j] > 0.0f ? dpred * w3[j] : 0.0f;
+            }
+            warp_sum64(v, red + (0 * 4 + warp) * kH);  // dw3
+#pragma unroll
+            for (int j = 0; j < kH; ++j) v[j] = dz[j];
+            warp_sum64(v, red + (1 * 4 + warp) * kH);  // db2
+            float d3 = dpred;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) d3 += __shfl_xor_sync(0xffffffffu, d3, o);
+            __syncthreads();  // sg zeroed (first tile); red written
+            if ((t & 31) == 0) atomicAdd(&sg[MDAS_MLP_OFF_B3], d3);
+        }
+#pragma unroll
+        for (int kb = 0; kb < kH / 8; ++kb) st_row8(c.sm + SM_D, t, kb, 8, dz + 8 * kb);
+        // dH1 = dZ2 . W2 on the tensor cores (B = W2 transposed, K-major)
+        run_mma(c, SM_D, SM_W2T, 8, kH / 16);
+        float dh[kH];
+        tmem_row(c, dh);
+        float h1[kH];
+#pragma unroll
+        for (int kb = 0; kb < kH / 8; ++kb) ld_row8(c.sm + SM_H, t, kb, 8, h1 + 8 * kb);
+#pragma unroll
+        for (int i = 0; i < kH; ++i) dh[i] = h1[i] > 0.0f ? dh[i] : 0.0f;  // dZ1 (0 on rows past m)
+        // the operands of the weight-gradient GEMM, this thread's row r as column r
+        // (K) of [dZ2^T ; dZ1^T] and of [H1 | X]^T (the previous tile's GEMM has
+        // completed: its wait came before this tile's dH1 GEMM)
+        uint16_t* a16 = reinterpret_cast<uint16_t*>(ag);
+        uint16_t* b16 = reinterpret_cast<uint16_t*>(bg);
 #pragma unroll
         for (int j = 0; j < kH; ++j) {
-            v[j] = dpred * fmaxf(z2[j], 0.0f);
-            dz[j] = z2[j] > 0.0f ? dpred * w3[j] : 0.0f;
-            z2f[t * 65 + j] = dz[j];
+            a16[core_off(j, t, kRows / 8)] = bf16_bits(dz[j]);
+            a16[core_off(kH + j, t, kRows / 8)] = bf16_bits(dh[j]);
+            b16[core_off(j, t, kRows / 8)] = bf16_bits(h1[j]);
         }
-        warp_sum64(v, red + (0 * 4 + warp) * kH);  // dw3
 #pragma unroll
-        for (int j = 0; j < kH; ++j) v[j] = dz[j];
-        warp_sum64(v, red + (1 * 4 + warp) * kH);  // db2
-        float d3 = dpred;
+        for (int k = 0; k < kIn; ++k) b16[core_off(kH + k, t, kRows / 8)] = bf16_bits(f[k]);
+        warp_sum64(dh, red + (2 * 4 + warp) * kH);  // db1
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (t < kH) {
+            float a = 0.0f, b2 = 0.0f, d1 = 0.0f;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) d3 += __shfl_xor_sync(0xffffffffu, d3, o);
-        __syncthreads();  // sg zeroed
-        if ((t & 31) == 0) atomicAdd(&sg[MDAS_MLP_OFF_B3], d3);
-    }
-#pragma unroll
-    for (int kb = 0; kb < kH / 8; ++kb) st_row8(c.sm + SM_D, t, kb, 8, dz + 8 * kb);
-    // dH1 = dZ2 . W2 on the tensor cores (B = W2 transposed, K-major)
-    run_mma(c, SM_D, SM_W2T, 8, kH / 16);
-    float dh[kH];
-    tmem_row(c, dh);
-#pragma unroll
-    for (int kb = 0; kb < kH / 8; ++kb) {
-        float h[8];
-        ld_row8(c.sm + SM_H, t, kb, 8, h);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int i = 8 * kb + q;
-            dh[i] = h[q] > 0.0f ? dh[i] : 0.0f;  // dZ1 (0 on rows past m: their dZ2 is 0)
-            z1f[t * 65 + i] = dh[i];
-        }
-    }
-    warp_sum64(dh, red + (2 * 4 + warp) * kH);  // db1
-    __syncthreads();
-    if (t < kH) {
-        float a = 0.0f, b = 0.0f, d = 0.0f;
-#pragma unroll
-        for (int w = 0; w < 4; ++w) {
-            a += red[(0 * 4 + w) * kH + t];
-            b += red[(1 * 4 + w) * kH + t];
-            d += red[(2 * 4 + w) * kH + t];
-        }
-        sg[MDAS_MLP_OFF_W3 + t] = a;
-        sg[MDAS_MLP_OFF_B2 + t] = b;
-        sg[MDAS_MLP_OFF_B1 + t] = d;
-    }
-    // dW2[j][i] = sum_r dZ2[r][j] H1[r][i]: thread t owns j = t / 2, i in [32 (t % 2), +32)
-    {
-        const int j = t >> 1, i0 = (t & 1) * 32;
-        float acc[32];
-#pragma unroll
-        for (int q = 0; q < 32; ++q) acc[q] = 0.0f;
-        for (int row = 0; row < kRows; ++row) {
-            const float d = z2f[row * 65 + j];
-#pragma unroll
-            for (int kb = 0; kb < 4; ++kb) {
-                float h[8];
-                ld_row8(c.sm + SM_H, row, i0 / 8 + kb, 8, h);
-#pragma unroll
-                for (int q = 0; q < 8; ++q) acc[8 * kb + q] += d * h[q];
+            for (int q = 0; q < 4; ++q) {
+                a += red[(0 * 4 + q) * kH + t];
+                b2 += red[(1 * 4 + q) * kH + t];
+                d1 += red[(2 * 4 + q) * kH + t];
             }
+            sg[MDAS_MLP_OFF_W3 + t] += a;
+            sg[MDAS_MLP_OFF_B2 + t] += b2;
+            sg[MDAS_MLP_OFF_B1 + t] += d1;
         }
-#pragma unroll
-        for (int q = 0; q < 32; ++q) sg[MDAS_MLP_OFF_W2 + j * kH + i0 + q] += acc[q];
-    }
-    // dW1[i][k] = sum_r dZ1[r][i] X[r][k]: thread t owns i = t / 2, k in [8 (t % 2), +8)
-    {
-        const int i = t >> 1, kb = t & 1;
-        float acc[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) acc[q] = 0.0f;
-        for (int row = 0; row < kRows; ++row) {
-            const float d = z1f[row * 65 + i];
-            float x[8];
-            ld_row8(c.sm + SM_X, row, kb, 2, x);
-#pragma unroll
-            for (int q = 0; q < 8; ++q) acc[q] += d * x[q];
+        if (t == 0) {
+            tc_fence_after();
+            const uint32_t sbo = (uint32_t)(kRows / 8) * 128u;
+            for (int ks = 0; ks < kRows / 16; ++ks)
+                mma_bf16_id(c.tmem + kGradCol, smem_desc(c.base + SM_AG + 256 * ks, 128, sbo),
+                            smem_desc(c.base + SM_BG + 256 * ks, 128, sbo), kGradIdesc,
+                            (first && ks == 0) ? 0u : 1u);
+            mma_commit(c.bar);
         }
-#pragma unroll
-        for (int q = 0; q < 8; ++q) sg[MDAS_MLP_OFF_W1 + i * kIn + 8 * kb + q] += acc[q];
+        mma_wait(c);
+        lossPart += e * e;
+        first = false;
     }
-    // loss
-    float l = e * e;
+    // this CTA's sums into the global gradient
+    float l = lossPart;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
-    if ((t & 31) == 0) atomicAdd(lossSum, l);
+    if ((t & 31) == 0 && l != 0.0f) atomicAdd(lossSum, l);
+    if (!first) {
+        // the weight gradients: lane t of the accumulator is row t of [dZ2^T ; dZ1^T] . [H1 | X]
+        float acc[kGradN];
+        const uint32_t lane = (threadIdx.x & ~31u) << 16;
+#pragma unroll
+        for (int q = 0; q < kGradN / 16; ++q) tmem_ld16(c.tmem + lane + kGradCol + 16 * q, acc + 16 * q);
+        tmem_wait_ld();
+        if (t < kH) {
+#pragma unroll
+            for (int i = 0; i < kH; ++i)
+                if (acc[i] != 0.0f) atomicAdd(&grads[MDAS_MLP_OFF_W2 + t * kH + i], acc[i]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < kIn; ++k)
+                if (acc[kH + k] != 0.0f) atomicAdd(&grads[MDAS_MLP_OFF_W1 + (t - kH) * kIn + k], acc[kH + k]);
+        }
+    }
     __syncthreads();
     for (int i = t; i < MDAS_MLP_PARAMS; i += kThreads) {
         const float v = sg[i];
@@ -889,8 +920,9 @@ cudaError_t gradients(const Packed* w, const float* features, const float* targe
     none.D = 4;
     const MdasDeviceGrid& gg = g ? *g : none;
     cudaError_t e = cudaSuccess;
+    const int grid = tiles < sm_count() ? tiles : sm_count();  // persistent: one CTA per SM (shared memory)
     MLP_SWITCH_D(gg.D, (e = set_smem(k_gradients<DD>, kTrainSmem),
-                        e == cudaSuccess ? (k_gradients<DD><<<tiles, kThreads, kTrainSmem, s>>>(
+                        e == cudaSuccess ? (k_gradients<DD><<<grid, kThreads, kTrainSmem, s>>>(
                                                 w, features, targets, gg, L, offset, stride, m, grads, lossSum, status),
                                             0)
                                          : 0));

@@ -49,11 +49,11 @@ def ref_gradients(p, x, y):
     g[OFF_B3] = dpred.sum()
     dz2 = dpred[:, None] * w3[None, :] * (z2 > 0)
     g[OFF_B2:OFF_W3] = dz2.sum(0)
-    g[OFF_W2:OFF_B2] = (dz2.T @ h1).reshape(-1)
+    g[OFF_W2:OFF_B2] = (bf(dz2).T @ h1).reshape(-1)  # the weight gradients: a BF16 tensor-core GEMM
     dh1 = bf(dz2) @ bf(W2)
     dz1 = dh1 * (h1 > 0)
     g[OFF_B1:OFF_W2] = dz1.sum(0)
-    g[OFF_W1:OFF_B1] = (dz1.T @ X).reshape(-1)
+    g[OFF_W1:OFF_B1] = (bf(dz1).T @ X).reshape(-1)
     return g, float((e * e).mean())
 
 
@@ -80,7 +80,7 @@ def test_mlp_forward_matches_torch(cuda, m):
     assert (got - want).abs().median().item() / scale < 1e-5
 
 
-@pytest.mark.parametrize("m", [64, 128, 1000, 16384])
+@pytest.mark.parametrize("m", [64, 128, 1000, 16384, 100003])  # (the last: several tiles per persistent CTA)
 def test_mlp_gradients_match_torch(cuda, m):
     torch = cuda
     p = make_params(torch, 7 + m)
