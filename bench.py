@@ -784,7 +784,7 @@ def batch_block(steps: int, warmup: int, peak: float, first_seed: int = 200, n_i
     for g, sc, p, wl in zip(grids, scenes, pix, wls):
         nbytes += sum(render_tallies(g, sc, wl, p).values())
     batch = P.Batch(grids, scenes, [w.budget for w in wls], pix, [w.width for w in wls], [w.height for w in wls])
-    best, tuned_ms = batch.autotune(repeats=1)
+    best, tile, tuned_ms, evaluated = batch.autotune_ex(repeats=1)
     for _ in range(warmup):
         stats = batch.render()
     torch.cuda.synchronize()
@@ -816,7 +816,8 @@ def batch_block(steps: int, warmup: int, peak: float, first_seed: int = 200, n_i
             "value": round(samples / (ms / 1e3) / 1e6, 3), "unit": UNIT, "ms": round(ms, 3),
             "per_image_ms": round(ms / len(wls), 4), "samples": samples,
             "sequential_single_image_ms": round(t_single, 3), "speedup_vs_sequential": round(t_single / ms, 3),
-            "autotuned_ctas_per_sm": best, "autotune_best_ms": round(tuned_ms, 3),
+            "autotuned_ctas_per_sm": best, "autotuned_decide_tile_leaves": tile, "autotune_candidates": evaluated,
+            "autotune_best_ms": round(tuned_ms, 3),
             "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(gbs / peak, 4), "algorithmic_bytes": int(nbytes),
                          "note": "all stages of all images over the whole batched render (integrand included)"},
@@ -884,7 +885,7 @@ def run_batch(args, rank: int, world: int, local_rank: int) -> dict:
                               wl.height))
         pix.append(torch.zeros(wl.height, wl.width, 4, device="cuda"))
     batch = P.Batch(grids, scenes, [w.budget for w in wls], pix, [w.width for w in wls], [w.height for w in wls])
-    best, tuned_ms = batch.autotune(repeats=1)
+    best, tile, tuned_ms, evaluated = batch.autotune_ex(repeats=1)
     for _ in range(args.warmup):
         stats = batch.render()
     torch.cuda.synchronize()
@@ -922,7 +923,8 @@ def run_batch(args, rank: int, world: int, local_rank: int) -> dict:
         "config": {"workload": "batch64: 64 images, resolution in {256^2, 512^2, 1280x720, 1920x1080}, spp in "
                                "{4, 8, 16, 32}, 3-D motion blur or 4-D depth of field, seeds 200-263",
                    "total_samples": samples, "timing": "whole batched render incl. integrand (one CUDA graph)",
-                   "autotuned_ctas_per_sm": best, "autotune_ms": round(tuned_ms, 3)},
+                   "autotuned_ctas_per_sm": best, "autotuned_decide_tile_leaves": tile,
+                   "autotune_candidates": evaluated, "autotune_ms": round(tuned_ms, 3)},
         "per_image_ms": round(ms / len(wls), 4),
         "sequential_single_image_ms": round(t_single, 3),
         "batch_speedup_vs_sequential": round(t_single / ms, 3),

@@ -280,8 +280,17 @@ int mdas_batch_render(mdas_batch* b, mdas_render_stats* stats);
 /* Persistent CTAs per SM of the errors, decide, place and integrate/integrand
  * launches (rebuilds the graph). */
 int mdas_batch_set_tuning(mdas_batch* b, const int* ctasPerSm4);
-/* Times a set of candidate tunings on this batch (`repeats` renders each),
- * keeps the fastest and returns it with its time per render. */
+/* mdas_batch_set_tuning plus the tile size of the adaptive pass's decide
+ * kernel (leavesPerTile: 1024 or 2048 leaves per 256-thread tile). */
+int mdas_batch_set_tiling(mdas_batch* b, const int* ctasPerSm4, int leavesPerTile);
+/* The batch's autotuner: times candidate tunings on this batch (`repeats`
+ * renders each after a warm one) by coordinate descent from the default — the
+ * decide tile size, then each stage's CTAs per SM in turn — keeps the fastest
+ * and returns it (each pointer optional) with its time per render and the
+ * number of candidates timed. */
+int mdas_batch_autotune_ex(mdas_batch* b, int repeats, int* best4, int* bestLeavesPerTile, double* bestMs,
+                           int* evaluated);
+/* mdas_batch_autotune_ex without the tile size and the count. */
 int mdas_batch_autotune(mdas_batch* b, int repeats, int* best4, double* bestMs);
 
 /* ---- Leaf ordering: Morton keys, radix sort, Karras hierarchy, point location.

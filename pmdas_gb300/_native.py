@@ -109,6 +109,8 @@ SIGNATURES = {
     "mdas_batch_render": (_I, [_P, C.POINTER(RenderStats)]),
     "mdas_batch_set_tuning": (_I, [_P, C.POINTER(_I)]),
     "mdas_batch_autotune": (_I, [_P, _I, C.POINTER(_I), C.POINTER(C.c_double)]),
+    "mdas_batch_set_tiling": (_I, [_P, C.POINTER(_I), _I]),
+    "mdas_batch_autotune_ex": (_I, [_P, _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_double), C.POINTER(_I)]),
     "mdas_morton_key_bits": (_I, [_I, _I, _I, _I]),
     "mdas_morton_encode": (_I, [_I, _I, _I, _I, _F, _F, _P, _I, _P, _P]),
     "mdas_morton_decode": (_I, [_I, _I, _I, _F, _F, _P, _I, _P, _P]),

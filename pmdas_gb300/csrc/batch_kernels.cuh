@@ -273,14 +273,14 @@ __global__ void __launch_bounds__(256) k_batch_errors(const MdasBatchImage* __re
 }
 
 // ---- adaptive pass: decide
-template <int D>
+template <int D, int K>
 __global__ void __launch_bounds__(256) k_batch_decide(const MdasBatchImage* __restrict__ imgs, int n) {
     pdl_launch_dependents();
     __shared__ int s_pre[MDAS_MAX_BATCH + 1];
     __shared__ unsigned s_warp[8];
     const int total = batch_prefix(n, s_pre, s_warp, [&](int i) {
         const MdasCounts* c = imgs[i].g.counts;
-        return c->active ? ceil_div(c->L, MDAS_TILE_LEAVES) : 0;
+        return c->active ? ceil_div(c->L, 256 * K) : 0;
     });
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
         const int i = batch_image_of(s_pre, n, t);
@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(256) k_batch_decide(const MdasBatchImage* __re
         const float gError = __uint_as_float(g.counts->gerr);
         float keptMax = 0.0f;
         unsigned gathered = 0;
-        decide_tile<D>(g, t - s_pre[i], L, gError, imgs[i].jumpA, imgs[i].jumpC, s_warp, keptMax, gathered);
+        decide_tile<D, K>(g, t - s_pre[i], L, gError, imgs[i].jumpA, imgs[i].jumpC, s_warp, keptMax, gathered);
         const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(keptMax));
         const unsigned c = __reduce_add_sync(0xffffffffu, gathered);
         if ((threadIdx.x & 31) == 0) {
@@ -416,8 +416,13 @@ cudaError_t batch_learned_judge(const MdasBatchImage* imgs, int n, int grid, cud
     return cudaGetLastError();
 }
 
-cudaError_t batch_decide(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s) {
-    MDAS_BATCH_SWITCH_D(D, (k_batch_decide<DD><<<grid, 256, 0, s>>>(imgs, n)));
+// K: leaves per thread of decide (4 or 8); every image of the group has tileK == K.
+cudaError_t batch_decide(const MdasBatchImage* imgs, int n, int D, int K, int grid, cudaStream_t s) {
+    if (K == 4) {
+        MDAS_BATCH_SWITCH_D(D, (k_batch_decide<DD, 4><<<grid, 256, 0, s>>>(imgs, n)));
+    } else {
+        MDAS_BATCH_SWITCH_D(D, (k_batch_decide<DD, 8><<<grid, 256, 0, s>>>(imgs, n)));
+    }
     return cudaGetLastError();
 }
 

@@ -352,7 +352,8 @@ int mdas_create_ex(mdas_grid** out, int dim, int maxSamples, int candidatesNum, 
     d.alpha = alpha;
     d.scaleX = scaleX;
     d.scaleY = scaleY;
-    d.maxTiles = (d.maxNodes + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
+    d.tileK = MDAS_LEAVES_PER_THREAD;
+    d.maxTiles = (d.maxNodes + MDAS_TILE_LEAVES_MIN - 1) / MDAS_TILE_LEAVES_MIN;  // (room for the smallest tiles)
     const size_t capSamples = ((size_t)maxSamples + 127) / 128 * 128;  // roundUp(maxSamples, 128), kdgrid.cu:625-626
     bool ok = cudaMalloc(&d.coords, sizeof(float) * capSamples * dim) == cudaSuccess &&
               cudaMalloc(&d.values, sizeof(float) * 3 * capSamples) == cudaSuccess &&
@@ -364,7 +365,7 @@ int mdas_create_ex(mdas_grid** out, int dim, int maxSamples, int candidatesNum, 
               cudaMalloc(&d.ctl, sizeof(MdasCtl)) == cudaSuccess &&
               cudaMalloc(&d.tileCounts, sizeof(uint2) * (size_t)d.maxTiles) == cudaSuccess &&
               cudaMalloc(&d.tilePrefix, sizeof(uint2) * (size_t)d.maxTiles) == cudaSuccess &&
-              cudaMalloc(&d.accepted, sizeof(uint2) * (size_t)d.maxTiles * MDAS_TILE_LEAVES) == cudaSuccess &&
+              cudaMalloc(&d.accepted, sizeof(uint2) * (size_t)d.maxTiles * MDAS_TILE_LEAVES_MIN) == cudaSuccess &&
               cudaMalloc(&d.chunkTile, sizeof(int) * ((size_t)d.maxNodes / 256 + 2)) == cudaSuccess &&
               cudaMalloc(&d.dirty, sizeof(int) * ((size_t)d.maxNodes / 2 + 1)) == cudaSuccess &&
               cudaMalloc(&d.splitL, sizeof(int4) * ((size_t)d.maxNodes / 2 + 1)) == cudaSuccess &&
@@ -466,7 +467,7 @@ int mdas_adaptive_sampling(mdas_grid* g) {
     // each, so the leaf count stays <= (N + L) / 2 <= maxSamples / 2 < maxNodes.
     if ((int64_t)g->N + g->L > g->dg.maxSamples) return MDAS_ERR_CAPACITY;
     // one CTA iteration per tile of MDAS_TILE_LEAVES leaves
-    const int64_t tiles = ((int64_t)g->L + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
+    const int64_t tiles = ((int64_t)g->L + 256 * g->dg.tileK - 1) / (256 * g->dg.tileK);
     const int gridDecide = grid_for(g, MDAS_K_DECIDE, tiles * 256);
     const int gridPlace = grid_for(g, MDAS_K_ADAPTIVE, g->L);  // one thread per accepted leaf (<= L)
     g->dg.priority = g->learned && g->lPredVersion == g->version ? g->lPred : nullptr;
@@ -1076,6 +1077,7 @@ struct mdas_batch {
     cudaStream_t stream = nullptr, captureStream = nullptr, bodyStream = nullptr;
     cudaGraphExec_t exec = nullptr;
     int tune[4] = {4, 4, 4, 8};  // persistent CTAs per SM: errors, decide, place, integrate/integrand
+    int tileK = MDAS_LEAVES_PER_THREAD;  // leaves per thread of decide (tiles of 256 * tileK leaves)
     uint64_t launches = 0;
     bool anyLearned = false;     // some image takes the learned acceptance
     unsigned* status = nullptr;  // bounded waits of the batched learned kernels
@@ -1149,7 +1151,8 @@ int build_batch_graph(mdas_batch* b) {
     }
     if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_reset, b->d_imgs, b->n, 1, bs);
     for (const auto& gr : b->groups)
-        if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_decide, b->d_imgs + gr.offset, gr.count, gr.D, gDec, bs);
+        if (eb == cudaSuccess)
+            eb = MDAS_ARITH_CALL(b, batch_decide, b->d_imgs + gr.offset, gr.count, gr.D, b->tileK, gDec, bs);
     if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_scan, b->d_imgs, b->n, bs);
     for (const auto& gr : b->groups)
         if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_place, b->d_imgs + gr.offset, gr.count, gr.D, gPl, bs);
@@ -1314,46 +1317,96 @@ int mdas_batch_render(mdas_batch* b, mdas_render_stats* stats) {
     return status;
 }
 
-int mdas_batch_set_tuning(mdas_batch* b, const int* ctasPerSm4) {
-    if (!b || !ctasPerSm4) return MDAS_ERR_INVALID;
+int mdas_batch_set_tiling(mdas_batch* b, const int* ctasPerSm4, int leavesPerTile) {
+    if (!b || !ctasPerSm4 || (leavesPerTile != 1024 && leavesPerTile != 2048)) return MDAS_ERR_INVALID;
     for (int k = 0; k < 4; ++k)
         if (ctasPerSm4[k] < 1 || ctasPerSm4[k] > 32) return MDAS_ERR_INVALID;
     for (int k = 0; k < 4; ++k) b->tune[k] = ctasPerSm4[k];
+    const int K = leavesPerTile / 256;
+    if (K != b->tileK) {
+        // every image's decide tiles (the grid's own passes keep theirs)
+        b->tileK = K;
+        for (auto& im : b->himgs) im.g.tileK = K;
+        if (cudaMemcpy(b->d_imgs, b->himgs.data(), sizeof(MdasBatchImage) * b->himgs.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess)
+            return MDAS_ERR_CUDA;
+    }
     return build_batch_graph(b);
 }
 
-int mdas_batch_autotune(mdas_batch* b, int repeats, int* best4, double* bestMs) {
+int mdas_batch_set_tuning(mdas_batch* b, const int* ctasPerSm4) {
+    if (!b) return MDAS_ERR_INVALID;
+    return mdas_batch_set_tiling(b, ctasPerSm4, 256 * b->tileK);
+}
+
+namespace {
+// one render of the batch's graph after a warm one, `repeats` times: ms per render
+int batch_time(mdas_batch* b, int repeats, cudaEvent_t e0, cudaEvent_t e1, double* ms) {
+    if (cudaGraphLaunch(b->exec, b->stream) != cudaSuccess) return MDAS_ERR_CUDA;  // warm
+    cudaEventRecord(e0, b->stream);
+    for (int r = 0; r < repeats; ++r) cudaGraphLaunch(b->exec, b->stream);
+    cudaEventRecord(e1, b->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) return MDAS_ERR_CUDA;
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, e0, e1);
+    b->launches += repeats + 1;
+    *ms = t / repeats;
+    return MDAS_OK;
+}
+}  // namespace
+
+int mdas_batch_autotune_ex(mdas_batch* b, int repeats, int* best4, int* bestLeavesPerTile, double* bestMs,
+                           int* evaluated) {
     if (!b || repeats < 1) return MDAS_ERR_INVALID;
-    // candidate persistent-grid sizes (CTAs per SM) for errors, decide, place, integrate/integrand
-    static const int cand[][4] = {{2, 2, 2, 4}, {4, 4, 4, 8}, {6, 6, 4, 8}, {8, 8, 4, 16}, {4, 8, 2, 8},
-                                  {6, 8, 3, 12}};
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return MDAS_ERR_CUDA;
+    // coordinate descent from the default: the decide tile size, then each stage's
+    // persistent grid (CTAs per SM) in turn, keeping every improvement
+    int cur[4] = {4, 4, 4, 8}, curTile = MDAS_TILE_LEAVES;
     double best = 1e30;
-    int bi = 1;
-    for (int c = 0; c < (int)(sizeof(cand) / sizeof(cand[0])); ++c) {
-        int rc = mdas_batch_set_tuning(b, cand[c]);
-        if (rc) return rc;
-        cudaGraphLaunch(b->exec, b->stream);  // warm
-        cudaEventRecord(e0, b->stream);
-        for (int r = 0; r < repeats; ++r) cudaGraphLaunch(b->exec, b->stream);
-        cudaEventRecord(e1, b->stream);
-        if (cudaEventSynchronize(e1) != cudaSuccess) return MDAS_ERR_CUDA;
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        b->launches += repeats + 1;
-        if (ms / repeats < best) {
-            best = ms / repeats;
-            bi = c;
+    int evals = 0, rc = MDAS_OK;
+    auto eval = [&](const int* t4, int tile, double* ms) {
+        int r = mdas_batch_set_tiling(b, t4, tile);
+        if (!r) r = batch_time(b, repeats, e0, e1, ms);
+        ++evals;
+        return r;
+    };
+    for (int tile : {MDAS_TILE_LEAVES, MDAS_TILE_LEAVES_MIN}) {
+        double ms = 0.0;
+        if ((rc = eval(cur, tile, &ms))) break;
+        if (ms < best) {
+            best = ms;
+            curTile = tile;
+        }
+    }
+    static const int choices[4][3] = {{2, 4, 8}, {2, 4, 8}, {2, 4, 6}, {4, 8, 16}};
+    for (int k = 0; k < 4 && !rc; ++k) {
+        for (int v : choices[k]) {
+            if (v == cur[k]) continue;
+            int t4[4] = {cur[0], cur[1], cur[2], cur[3]};
+            t4[k] = v;
+            double ms = 0.0;
+            if ((rc = eval(t4, curTile, &ms))) break;
+            if (ms < best) {
+                best = ms;
+                cur[k] = v;
+            }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    int rc = mdas_batch_set_tuning(b, cand[bi]);
+    if (rc) return rc;
+    rc = mdas_batch_set_tiling(b, cur, curTile);
     if (best4)
-        for (int k = 0; k < 4; ++k) best4[k] = cand[bi][k];
+        for (int k = 0; k < 4; ++k) best4[k] = cur[k];
+    if (bestLeavesPerTile) *bestLeavesPerTile = curTile;
     if (bestMs) *bestMs = best;
+    if (evaluated) *evaluated = evals;
     return rc;
+}
+
+int mdas_batch_autotune(mdas_batch* b, int repeats, int* best4, double* bestMs) {
+    return mdas_batch_autotune_ex(b, repeats, best4, nullptr, bestMs, nullptr);
 }
 
 int mdas_render_host(mdas_grid* g, mdas_scene* s, const float* hostPrims, int budget, float* hostPixels, int width,

@@ -96,6 +96,8 @@ struct MdasDeviceGrid {
     // leaf the last split-children errors pass recomputed, in its item order
     // (nullptr: not written)
     float* featRaw;
+    // leaves per thread of decide (4 or 8): its tiles are 256 * tileK leaves
+    int tileK;
 };
 
 // One image of a batched render (device-side descriptor).
@@ -109,9 +111,12 @@ struct MdasBatchImage {
     const void* mlp;        // packed weights of a learned image (g.priority set), nullptr: plain acceptance
 };
 
-// Leaves per thread and per tile of the adaptive pass.
+// Leaves per thread and per tile of the adaptive pass (the default; the
+// batched renders may take 4 per thread: MdasDeviceGrid::tileK), and the
+// smallest tile, which sizes the per-tile scratch.
 #define MDAS_LEAVES_PER_THREAD 8
 #define MDAS_TILE_LEAVES (256 * MDAS_LEAVES_PER_THREAD)
+#define MDAS_TILE_LEAVES_MIN 1024
 
 #define MDAS_OK 0
 #define MDAS_ERR_INVALID 1
@@ -139,7 +144,7 @@ struct MdasBatchImage {
     cudaError_t batch_set_counts(const MdasBatchImage* imgs, int n, cudaStream_t s);                         \
     cudaError_t batch_errors(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s);            \
     cudaError_t batch_reset(const MdasBatchImage* imgs, int n, int which, cudaStream_t s);                   \
-    cudaError_t batch_decide(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s);            \
+    cudaError_t batch_decide(const MdasBatchImage* imgs, int n, int D, int K, int grid, cudaStream_t s);     \
     cudaError_t batch_scan(const MdasBatchImage* imgs, int n, cudaStream_t s);                               \
     cudaError_t batch_place(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s);             \
     cudaError_t batch_condition(const MdasBatchImage* imgs, int n, cudaGraphConditionalHandle h,             \

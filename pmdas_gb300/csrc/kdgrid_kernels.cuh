@@ -484,23 +484,31 @@ __device__ __forceinline__ float learned_ratio(const MdasDeviceGrid& g, int leaf
 // decide, one tile: acceptance of the tile's leaves, final seeds, the tile's
 // counts and its compacted accepted list (shared by the single-image and the
 // batched kernels).
-template <int D>
+// K: leaves per thread (4 or 8): a tile is 256 K leaves (g.tileK must be K).
+template <int D, int K>
 __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, int L, float gError, unsigned jumpA,
                                             unsigned jumpC, unsigned* s_warp, float& keptMax, unsigned& gathered) {
     constexpr int kMaxNodeSize = 4;  // KDGrid ctor: maxNodeSize(4), kdgrid.cu:611
-    constexpr int K = MDAS_LEAVES_PER_THREAD;
-    constexpr int TILE = MDAS_TILE_LEAVES;
-    static_assert(TILE == 256 * K && TILE <= 2048, "tile = 256 threads x K leaves, local index in 11 bits");
+    constexpr int TILE = 256 * K;
+    static_assert((K == 4 || K == 8) && TILE <= 2048, "tile = 256 threads x K leaves, local index in 11 bits");
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int i0 = tile * TILE + threadIdx.x * K;
     const bool full = i0 + K <= L;
-    static_assert(K == 8, "the sample counts of a thread's leaves are one 8-byte load");
     float err[K];
     unsigned sd[K];
     int lc[K];
     if (full) {
-        const uint2 c8 = *reinterpret_cast<const uint2*>(g.leafCounts + i0);
+        // the sample counts of a thread's leaves: one 8- or 4-byte load
+        unsigned cw[2];
+        if constexpr (K == 8) {
+            const uint2 c8 = *reinterpret_cast<const uint2*>(g.leafCounts + i0);
+            cw[0] = c8.x;
+            cw[1] = c8.y;
+        } else {
+            cw[0] = *reinterpret_cast<const unsigned*>(g.leafCounts + i0);
+            cw[1] = 0u;
+        }
 #pragma unroll
         for (int q = 0; q < K; q += 4) {
             const float4 e4 = *reinterpret_cast<const float4*>(g.errors + i0 + q);
@@ -509,10 +517,7 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
             sd[q] = s4.x; sd[q + 1] = s4.y; sd[q + 2] = s4.z; sd[q + 3] = s4.w;
         }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            lc[j] = (int)((c8.x >> (8 * j)) & 0xffu);
-            lc[4 + j] = (int)((c8.y >> (8 * j)) & 0xffu);
-        }
+        for (int j = 0; j < K; ++j) lc[j] = (int)((cw[j >> 2] >> (8 * (j & 3))) & 0xffu);
     } else {
 #pragma unroll
         for (int j = 0; j < K; ++j) {
@@ -571,7 +576,8 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
             c8[j >> 2] |= nc << (8 * (j & 3));
         }
         if (full) {
-            *reinterpret_cast<uint2*>(g.leafCounts + i0) = make_uint2(c8[0], c8[1]);
+            if constexpr (K == 8) *reinterpret_cast<uint2*>(g.leafCounts + i0) = make_uint2(c8[0], c8[1]);
+            else *reinterpret_cast<unsigned*>(g.leafCounts + i0) = c8[0];
         } else {
 #pragma unroll
             for (int j = 0; j < K; ++j)
@@ -632,17 +638,17 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
     __syncthreads();  // s_warp is reused by the next tile
 }
 
-template <int D>
+template <int D, int K>
 __global__ void __launch_bounds__(256) k_adaptive_decide(MdasDeviceGrid g, unsigned jumpA, unsigned jumpC) {
     pdl_launch_dependents();
     __shared__ unsigned s_warp[8];
     const int L = g.counts->L;
     const float gError = __uint_as_float(g.counts->gerr);
-    const int ntiles = (L + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
+    const int ntiles = (L + 256 * K - 1) / (256 * K);
     float keptMax = 0.0f;   // max error of the leaves this CTA does not split
     unsigned gathered = 0;  // sample coordinates read
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
-        decide_tile<D>(g, tile, L, gError, jumpA, jumpC, s_warp, keptMax, gathered);
+        decide_tile<D, K>(g, tile, L, gError, jumpA, jumpC, s_warp, keptMax, gathered);
     unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(keptMax));
     unsigned c = __reduce_add_sync(0xffffffffu, gathered);
     if ((threadIdx.x & 31) == 0) {
@@ -656,7 +662,8 @@ __global__ void __launch_bounds__(256) k_adaptive_decide(MdasDeviceGrid g, unsig
 __device__ __forceinline__ void scan_image(const MdasDeviceGrid& g, unsigned* s_sel, unsigned* s_split) {
     const int N = g.counts->N;
     const int L = g.counts->L;
-    const int ntiles = (L + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
+    const int tileLeaves = 256 * g.tileK;
+    const int ntiles = (L + tileLeaves - 1) / tileLeaves;
     const int per = (ntiles + 1023) / 1024;
     const int t0 = threadIdx.x * per;
     const int t1 = min(t0 + per, ntiles);
@@ -732,7 +739,7 @@ __global__ void __launch_bounds__(1024) k_adaptive_scan(MdasDeviceGrid g) {
 template <int D>
 __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, int r, uint2 pre, int N, int L) {
     constexpr int kMaxNodeSize = 4;
-    constexpr int TILE = MDAS_TILE_LEAVES;
+    const int TILE = 256 * g.tileK;
     constexpr int NB = NbLayout<D>::FLOATS;
     (void)kMaxNodeSize;
     const uint2 e = g.accepted[(size_t)tile * TILE + r];
@@ -892,7 +899,7 @@ __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, i
 // the first tile of its 256-entry chunk.
 template <int D>
 __device__ __forceinline__ void place_rank(const MdasDeviceGrid& g, int k, int N, int L) {
-    const int ntiles = (L + MDAS_TILE_LEAVES - 1) / MDAS_TILE_LEAVES;
+    const int ntiles = (L + 256 * g.tileK - 1) / (256 * g.tileK);
     int tile = g.chunkTile[k >> 8];
     uint2 pre = g.tilePrefix[tile];
     while (tile + 1 < ntiles) {
@@ -1288,7 +1295,11 @@ cudaError_t adaptive_sampling(const MdasDeviceGrid& g, int gridDecide, int gridP
     if (e != cudaSuccess) return e;
     unsigned A, C;
     lcg_jump((unsigned)(g.candidatesNum * g.D), &A, &C);
-    MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD><<<gridDecide, 256, 0, s>>>(g, A, C)));
+    if (g.tileK == 4) {
+        MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD, 4><<<gridDecide, 256, 0, s>>>(g, A, C)));
+    } else {
+        MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD, 8><<<gridDecide, 256, 0, s>>>(g, A, C)));
+    }
     e = launch_pdl(k_adaptive_scan, 1, 1024, s, g);
     if (e != cudaSuccess) return e;
     MDAS_SWITCH_D(g.D, (e = launch_pdl(k_adaptive_place<DD>, gridPlace, 256, s, g)));
@@ -1366,7 +1377,7 @@ int max_blocks_per_sm(int D, int which) {
             MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_integrate<DD>, 256, 0)));
             break;
         case MDAS_K_DECIDE:
-            MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adaptive_decide<DD>, 256, 0)));
+            MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adaptive_decide<DD, 8>, 256, 0)));
             break;
         default:
             MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_initial_sampling<DD>, 256, 0)));

@@ -523,8 +523,24 @@ class Batch:
         a = (C.c_int * 4)(*ctas_per_sm)
         N.check(self._lib.mdas_batch_set_tuning(self._h, a), "mdas_batch_set_tuning")
 
+    def set_tiling(self, ctas_per_sm, leaves_per_tile: int):
+        """Per-stage CTAs per SM plus the decide tile size (1024 or 2048 leaves)."""
+        a = (C.c_int * 4)(*ctas_per_sm)
+        N.check(self._lib.mdas_batch_set_tiling(self._h, a, int(leaves_per_tile)), "mdas_batch_set_tiling")
+
     def autotune(self, repeats: int = 2):
         a = (C.c_int * 4)()
         ms = C.c_double()
         N.check(self._lib.mdas_batch_autotune(self._h, repeats, a, C.byref(ms)), "mdas_batch_autotune")
         return list(a), ms.value
+
+    def autotune_ex(self, repeats: int = 2):
+        """Coordinate-descent autotune over the decide tile size and every stage's
+        CTAs per SM: returns (ctas_per_sm, leaves_per_tile, ms_per_render, evaluated)."""
+        a = (C.c_int * 4)()
+        tile = C.c_int()
+        ms = C.c_double()
+        ev = C.c_int()
+        N.check(self._lib.mdas_batch_autotune_ex(self._h, repeats, a, C.byref(tile), C.byref(ms), C.byref(ev)),
+                "mdas_batch_autotune_ex")
+        return list(a), tile.value, ms.value, ev.value
