@@ -64,6 +64,10 @@ def parse_args():
     ap.add_argument("--learned-host", action="store_true",
                     help="render the learned-vs-plain ladders through the host loop (mdas_render) instead of graphs")
     ap.add_argument("--no-configs", action="store_true", help="skip the other benchmark configurations")
+    ap.add_argument("--batch-images", type=int, default=64,
+                    help="batch64: render only the first N images of the set (a smaller case for profilers)")
+    ap.add_argument("--stepped", action="store_true",
+                    help="batch64: the pass loop on the host (every kernel visible to a profiler), default tuning")
     ap.add_argument("--ncu-traffic", default=None, metavar="CSV",
                     help="print the per-stage DRAM traffic of an ncu launch list (gpu__time_duration.sum, "
                          "dram__bytes_read.sum, dram__bytes_write.sum; --csv) of this bench, and exit")
@@ -222,6 +226,40 @@ def reduce_across_ranks(mdas_ms: float, wall_ms: float, samples: int, world: int
 
 
 # ---- the GB300 arm ------------------------------------------------------------------
+def output_block(grid, pixels, W: int, H: int, peak: float, reps: int = 20) -> dict:
+    """The image outputs of the last render (kdgrid.cu:822-846), timed after the
+    render: ConvertToBytes (16 bytes read, 4 written per pixel) and the sampling
+    density on device memory (each sample's two image coordinates read, a float4
+    atomic per sample into an image that stays in L2, the image cleared and its
+    alpha set)."""
+    import torch
+
+    import pmdas_gb300._native as N
+    lib = N.load()
+    out = {}
+    byt = torch.zeros(H, W, 4, dtype=torch.uint8, device="cuda")
+    dens = torch.zeros(H, W, 4, device="cuda")
+    n = grid.GetNumberOfSamples()
+    cases = {
+        "convert_to_bytes": (lambda: grid.ConvertToBytes(pixels, byt, W, H), 20 * W * H),
+        "sampling_density": (lambda: N.check(lib.mdas_sampling_density_device(grid.handle, dens.data_ptr(), W, H),
+                                             "sampling_density_device"), 8 * n + 32 * W * H),
+    }
+    for name, (fn, nbytes) in cases.items():
+        fn()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / reps
+        gbs = nbytes / (ms / 1e3) / 1e9
+        out[name] = {"ms": round(ms, 4), "algorithmic_bytes": int(nbytes), "gbs": round(gbs, 1),
+                     "frac": round(gbs / peak, 4)}
+    return out
+
+
 def run_gb300(args, rank: int, world: int, local_rank: int):
     import numpy as np
     import torch
@@ -383,6 +421,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
                "includes": "primitive upload, culling masks, initial sampling, every pass, integrand, "
                            "reconstruction, one counter read, image copy (page-locked host buffers)"}
 
+    output = output_block(grid, pixels, W, H, peak)
     order = None if args.no_order else order_block(grid, wl, peak)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -412,6 +451,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         "e2e": e2e,
         "quality": quality,
         "leaf_order": order,
+        "output": output,
         "gpu_launches": int(launches),
         "clocks": clk,
     }
@@ -876,7 +916,7 @@ def run_batch(args, rank: int, world: int, local_rank: int) -> dict:
     from pmdas_gb300.workloads import batch_workloads
 
     torch.cuda.set_device(local_rank)
-    wls = batch_workloads(200 + 64 * rank, 64)
+    wls = batch_workloads(200 + 64 * rank, 64)[:max(1, min(64, args.batch_images))]
     grids, scenes, pix = [], [], []
     for wl in wls:
         grids.append(P.KDGrid(wl.dim, wl.maxSamples, wl.candidatesNum, wl.bitsPerDim, wl.extraImgBits, wl.alpha,
@@ -885,9 +925,15 @@ def run_batch(args, rank: int, world: int, local_rank: int) -> dict:
                               wl.height))
         pix.append(torch.zeros(wl.height, wl.width, 4, device="cuda"))
     batch = P.Batch(grids, scenes, [w.budget for w in wls], pix, [w.width for w in wls], [w.height for w in wls])
-    best, tile, tuned_ms, evaluated = batch.autotune_ex(repeats=1)
+    if args.stepped:  # default tuning, host-driven pass loop
+        best, tile, tuned_ms, evaluated = [4, 4, 4, 8], 2048, None, 0
+        render = batch.render_stepped
+    else:
+        best, tile, tuned_ms, evaluated = batch.autotune_ex(repeats=1)
+        render = batch.render
+    stats = None
     for _ in range(args.warmup):
-        stats = batch.render()
+        stats = render()
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -897,7 +943,7 @@ def run_batch(args, rank: int, world: int, local_rank: int) -> dict:
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(args.steps):
-        stats = batch.render()
+        stats = render()
     e1.record()
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -920,11 +966,13 @@ def run_batch(args, rank: int, world: int, local_rank: int) -> dict:
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded analytic integrands)",
-        "config": {"workload": "batch64: 64 images, resolution in {256^2, 512^2, 1280x720, 1920x1080}, spp in "
-                               "{4, 8, 16, 32}, 3-D motion blur or 4-D depth of field, seeds 200-263",
-                   "total_samples": samples, "timing": "whole batched render incl. integrand (one CUDA graph)",
+        "config": {"workload": (("batch64: 64 images," if len(wls) == 64 else f"batch64, its first {len(wls)} images:")
+                                + " resolution in {256^2, 512^2, 1280x720, 1920x1080}, spp in {4, 8, 16, 32}, "
+                                "3-D motion blur or 4-D depth of field, seeds 200-263"),
+                   "total_samples": samples, "timing": "whole batched render incl. integrand, CUDA events",
                    "autotuned_ctas_per_sm": best, "autotuned_decide_tile_leaves": tile,
-                   "autotune_candidates": evaluated, "autotune_ms": round(tuned_ms, 3)},
+                   "autotune_candidates": evaluated, "autotune_ms": round(tuned_ms, 3) if tuned_ms else None,
+                   "loop": "host-stepped passes (profiling)" if args.stepped else "device-side (CUDA graph)"},
         "per_image_ms": round(ms / len(wls), 4),
         "sequential_single_image_ms": round(t_single, 3),
         "batch_speedup_vs_sequential": round(t_single / ms, 3),

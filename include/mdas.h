@@ -277,11 +277,17 @@ int mdas_batch_create(mdas_batch** out, int n, mdas_grid* const* grids, mdas_sce
 int mdas_batch_destroy(mdas_batch* b);
 /* Renders every image; stats (n entries, caller order) may be NULL. */
 int mdas_batch_render(mdas_batch* b, mdas_render_stats* stats);
+/* The same render with the loop over passes on the host: the same kernels
+ * launched on the stream one pass at a time (one 4-byte read of the loop's
+ * verdict per pass) instead of the graph's device-side loop.  Same results;
+ * for tools that cannot look inside a graph's conditional node (profilers). */
+int mdas_batch_render_stepped(mdas_batch* b, mdas_render_stats* stats);
 /* Persistent CTAs per SM of the errors, decide, place and integrate/integrand
  * launches (rebuilds the graph). */
 int mdas_batch_set_tuning(mdas_batch* b, const int* ctasPerSm4);
 /* mdas_batch_set_tuning plus the tile size of the adaptive pass's decide
- * kernel (leavesPerTile: 1024 or 2048 leaves per 256-thread tile). */
+ * kernel (leavesPerTile: 1024 or 2048 leaves per 256-thread tile).  The
+ * results do not depend on it. */
 int mdas_batch_set_tiling(mdas_batch* b, const int* ctasPerSm4, int leavesPerTile);
 /* The batch's autotuner: times candidate tunings on this batch (`repeats`
  * renders each after a warm one) by coordinate descent from the default — the

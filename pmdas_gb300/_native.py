@@ -107,6 +107,7 @@ SIGNATURES = {
                                C.POINTER(_I), C.POINTER(_I)]),
     "mdas_batch_destroy": (_I, [_P]),
     "mdas_batch_render": (_I, [_P, C.POINTER(RenderStats)]),
+    "mdas_batch_render_stepped": (_I, [_P, C.POINTER(RenderStats)]),
     "mdas_batch_set_tuning": (_I, [_P, C.POINTER(_I)]),
     "mdas_batch_autotune": (_I, [_P, _I, C.POINTER(_I), C.POINTER(C.c_double)]),
     "mdas_batch_set_tiling": (_I, [_P, C.POINTER(_I), _I]),

@@ -329,8 +329,10 @@ __global__ void __launch_bounds__(256, 4) k_batch_place(const MdasBatchImage* __
 }
 
 // ---- loop condition over all images of the batch (one CTA of 256 threads)
+// anyOut: where the host-driven loop reads the verdict (nullptr: the graph's
+// conditional handle h takes it).
 __global__ void __launch_bounds__(256) k_batch_condition(const MdasBatchImage* __restrict__ imgs, int n,
-                                                          cudaGraphConditionalHandle h, int maxPasses) {
+                                                          cudaGraphConditionalHandle h, int maxPasses, int* anyOut) {
     __shared__ int s_any[8];
     int act = 0;
     if (threadIdx.x < (unsigned)n) {
@@ -348,7 +350,8 @@ __global__ void __launch_bounds__(256) k_batch_condition(const MdasBatchImage* _
     if (threadIdx.x == 0) {
         int a = 0;
         for (int w = 0; w < 8; ++w) a |= s_any[w];
-        cudaGraphSetConditional(h, a ? 1u : 0u);
+        if (anyOut) *anyOut = a;
+        else cudaGraphSetConditional(h, a ? 1u : 0u);
     }
 }
 
@@ -440,8 +443,8 @@ cudaError_t batch_place(const MdasBatchImage* imgs, int n, int D, int grid, cuda
 }
 
 cudaError_t batch_condition(const MdasBatchImage* imgs, int n, cudaGraphConditionalHandle h, int maxPasses,
-                            cudaStream_t s) {
-    k_batch_condition<<<1, 256, 0, s>>>(imgs, n, h, maxPasses);
+                            int* anyOut, cudaStream_t s) {
+    k_batch_condition<<<1, 256, 0, s>>>(imgs, n, h, maxPasses, anyOut);
     return cudaGetLastError();
 }
 

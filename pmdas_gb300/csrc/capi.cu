@@ -62,7 +62,7 @@ struct mdas_grid {
     cudaStream_t stream = nullptr;
     int device = 0;
     int numSMs = 1;
-    int occ[5] = {1, 1, 1, 1, 1};
+    int occ[MDAS_K_COUNT] = {1, 1, 1, 1, 1};
     int N = 0, L = 0, newN = 0, newL = 0;
     bool initialized = false;
     // errorsClean: every leaf error is >= 0 (an errors pass ran since the last change).
@@ -334,7 +334,7 @@ int mdas_create_ex(mdas_grid** out, int dim, int maxSamples, int candidatesNum, 
         delete g;
         return MDAS_ERR_CUDA;
     }
-    for (int k = 0; k < 5; ++k)
+    for (int k = 0; k < MDAS_K_COUNT; ++k)
         g->occ[k] = arith == MDAS_ARITH_IEEE ? mdas_ieee::max_blocks_per_sm(dim, k) : mdas_fast::max_blocks_per_sm(dim, k);
 
     MdasDeviceGrid& d = g->dg;
@@ -1088,17 +1088,64 @@ namespace {
 #define MDAS_ARITH_CALL(b, FN, ...) \
     ((b)->arith == MDAS_ARITH_IEEE ? mdas_ieee::FN(__VA_ARGS__) : mdas_fast::FN(__VA_ARGS__))
 
-// Graph of one batched render: initial sampling and integrand of every image,
-// then a device-side loop of passes over the still-active images, then
-// reconstruction.  Every stage is one launch per point dimension present.
+// The stages of one batched render.  Every stage is one launch per point
+// dimension present.  prologue: initial sampling and integrand of every image;
+// body: one pass over the still-active images, ending in the loop's verdict
+// (into the graph's conditional handle, or into anyOut when the host drives
+// the loop); epilogue: reconstruction.
+cudaError_t enqueue_batch_prologue(mdas_batch* b, cudaStream_t s) {
+    const int gInt = b->numSMs * b->tune[3];
+    cudaError_t e = cudaSuccess;
+    for (const auto& gr : b->groups)
+        if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_init, b->d_imgs + gr.offset, gr.count, gr.D, gInt, s);
+    if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_set_counts, b->d_imgs, b->n, s);
+    for (const auto& gr : b->groups)
+        if (e == cudaSuccess) e = mdas_launch_evaluate_batch(b->d_scenes + gr.offset, gr.count, gr.D, 1, gInt, s);
+    return e;
+}
+
+cudaError_t enqueue_batch_body(mdas_batch* b, cudaGraphConditionalHandle handle, int* anyOut, cudaStream_t s) {
+    const int gErr = b->numSMs * b->tune[0], gDec = b->numSMs * b->tune[1], gPl = b->numSMs * b->tune[2];
+    const int gInt = b->numSMs * b->tune[3];
+    cudaError_t e = MDAS_ARITH_CALL(b, batch_reset, b->d_imgs, b->n, 0, s);
+    for (const auto& gr : b->groups)
+        if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_errors, b->d_imgs + gr.offset, gr.count, gr.D, gErr, s);
+    if (e == cudaSuccess && b->anyLearned) {
+        // learned images: priorities of the leaves whose error was recomputed, then the judge
+        e = MDAS_ARITH_CALL(b, batch_reset, b->d_imgs, b->n, 2, s);
+        for (const auto& gr : b->groups)
+            if (e == cudaSuccess) e = mdas_mlp::batch_predict(b->d_imgs + gr.offset, gr.count, gr.D, b->status, s);
+        if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_learned_judge, b->d_imgs, b->n, b->numSMs * 4, s);
+    }
+    if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_reset, b->d_imgs, b->n, 1, s);
+    for (const auto& gr : b->groups)
+        if (e == cudaSuccess)
+            e = MDAS_ARITH_CALL(b, batch_decide, b->d_imgs + gr.offset, gr.count, gr.D, b->tileK, gDec, s);
+    if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_scan, b->d_imgs, b->n, s);
+    for (const auto& gr : b->groups)
+        if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_place, b->d_imgs + gr.offset, gr.count, gr.D, gPl, s);
+    for (const auto& gr : b->groups)
+        if (e == cudaSuccess) e = mdas_launch_evaluate_batch(b->d_scenes + gr.offset, gr.count, gr.D, 0, gInt, s);
+    if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_condition, b->d_imgs, b->n, handle, kMaxGraphPasses, anyOut, s);
+    return e;
+}
+
+cudaError_t enqueue_batch_epilogue(mdas_batch* b, cudaStream_t s) {
+    const int gInt = b->numSMs * b->tune[3];
+    cudaError_t e = MDAS_ARITH_CALL(b, batch_clear_pixels, b->d_imgs, b->n, s);
+    for (const auto& gr : b->groups)
+        if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_integrate, b->d_imgs + gr.offset, gr.count, gr.D, gInt, s);
+    return e;
+}
+
+// Graph of one batched render: the prologue, a device-side loop (a conditional
+// WHILE node) over the body, the epilogue.
 int build_batch_graph(mdas_batch* b) {
     if (b->exec) {
         cudaGraphExecDestroy(b->exec);
         b->exec = nullptr;
     }
     cudaStream_t cs = b->captureStream, bs = b->bodyStream;
-    const int gErr = b->numSMs * b->tune[0], gDec = b->numSMs * b->tune[1], gPl = b->numSMs * b->tune[2];
-    const int gInt = b->numSMs * b->tune[3];
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
     if (e != cudaSuccess) return MDAS_ERR_CUDA;
     auto fail = [&]() {
@@ -1108,16 +1155,7 @@ int build_batch_graph(mdas_batch* b) {
         cudaGetLastError();
         return MDAS_ERR_CUDA;
     };
-    for (const auto& gr : b->groups) {
-        e = MDAS_ARITH_CALL(b, batch_init, b->d_imgs + gr.offset, gr.count, gr.D, gInt, cs);
-        if (e != cudaSuccess) return fail();
-    }
-    e = MDAS_ARITH_CALL(b, batch_set_counts, b->d_imgs, b->n, cs);
-    if (e != cudaSuccess) return fail();
-    for (const auto& gr : b->groups) {
-        e = mdas_launch_evaluate_batch(b->d_scenes + gr.offset, gr.count, gr.D, 1, gInt, cs);
-        if (e != cudaSuccess) return fail();
-    }
+    if (enqueue_batch_prologue(b, cs) != cudaSuccess) return fail();
     cudaStreamCaptureStatus status;
     cudaGraph_t capGraph = nullptr;
     const cudaGraphNode_t* deps = nullptr;
@@ -1139,33 +1177,11 @@ int build_batch_graph(mdas_batch* b) {
         return fail();
     if (cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess)
         return fail();
-    cudaError_t eb = MDAS_ARITH_CALL(b, batch_reset, b->d_imgs, b->n, 0, bs);
-    for (const auto& gr : b->groups)
-        if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_errors, b->d_imgs + gr.offset, gr.count, gr.D, gErr, bs);
-    if (eb == cudaSuccess && b->anyLearned) {
-        // learned images: priorities of the leaves whose error was recomputed, then the judge
-        eb = MDAS_ARITH_CALL(b, batch_reset, b->d_imgs, b->n, 2, bs);
-        for (const auto& gr : b->groups)
-            if (eb == cudaSuccess) eb = mdas_mlp::batch_predict(b->d_imgs + gr.offset, gr.count, gr.D, b->status, bs);
-        if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_learned_judge, b->d_imgs, b->n, b->numSMs * 4, bs);
-    }
-    if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_reset, b->d_imgs, b->n, 1, bs);
-    for (const auto& gr : b->groups)
-        if (eb == cudaSuccess)
-            eb = MDAS_ARITH_CALL(b, batch_decide, b->d_imgs + gr.offset, gr.count, gr.D, b->tileK, gDec, bs);
-    if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_scan, b->d_imgs, b->n, bs);
-    for (const auto& gr : b->groups)
-        if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_place, b->d_imgs + gr.offset, gr.count, gr.D, gPl, bs);
-    for (const auto& gr : b->groups)
-        if (eb == cudaSuccess) eb = mdas_launch_evaluate_batch(b->d_scenes + gr.offset, gr.count, gr.D, 0, gInt, bs);
-    if (eb == cudaSuccess) eb = MDAS_ARITH_CALL(b, batch_condition, b->d_imgs, b->n, handle, kMaxGraphPasses, bs);
+    const cudaError_t eb = enqueue_batch_body(b, handle, nullptr, bs);
     cudaGraph_t bodyOut = nullptr;
     e = cudaStreamEndCapture(bs, &bodyOut);
     if (eb != cudaSuccess || e != cudaSuccess) return fail();
-    e = MDAS_ARITH_CALL(b, batch_clear_pixels, b->d_imgs, b->n, cs);
-    for (const auto& gr : b->groups)
-        if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_integrate, b->d_imgs + gr.offset, gr.count, gr.D, gInt, cs);
-    if (e != cudaSuccess) return fail();
+    if (enqueue_batch_epilogue(b, cs) != cudaSuccess) return fail();
     cudaGraph_t graph = nullptr;
     if (cudaStreamEndCapture(cs, &graph) != cudaSuccess) return MDAS_ERR_CUDA;
     e = cudaGraphInstantiate(&b->exec, graph, 0);
@@ -1287,12 +1303,9 @@ int mdas_batch_destroy(mdas_batch* b) {
     return MDAS_OK;
 }
 
-int mdas_batch_render(mdas_batch* b, mdas_render_stats* stats) {
-    if (!b || !b->exec) return MDAS_ERR_INVALID;
-    cudaError_t e = cudaGraphLaunch(b->exec, b->stream);
-    b->launches += 1;
-    if (e != cudaSuccess) return MDAS_ERR_CUDA;
-    if (cudaStreamSynchronize(b->stream) != cudaSuccess) return MDAS_ERR_CUDA;
+namespace {
+// After a batched render: the status, every grid's counts and the stats.
+int batch_finish(mdas_batch* b, mdas_render_stats* stats) {
     int status = MDAS_OK;
     if (b->anyLearned) {
         unsigned st = 0;
@@ -1315,6 +1328,41 @@ int mdas_batch_render(mdas_batch* b, mdas_render_stats* stats) {
         }
     }
     return status;
+}
+}  // namespace
+
+int mdas_batch_render(mdas_batch* b, mdas_render_stats* stats) {
+    if (!b || !b->exec) return MDAS_ERR_INVALID;
+    cudaError_t e = cudaGraphLaunch(b->exec, b->stream);
+    b->launches += 1;
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess) return MDAS_ERR_CUDA;
+    return batch_finish(b, stats);
+}
+
+int mdas_batch_render_stepped(mdas_batch* b, mdas_render_stats* stats) {
+    if (!b || !b->exec) return MDAS_ERR_INVALID;
+    int* any = nullptr;  // the loop's verdict, read by the host after every pass
+    if (cudaMallocHost(&any, sizeof(int)) != cudaSuccess) return MDAS_ERR_ALLOC;
+    int* dAny = nullptr;
+    cudaError_t e = cudaMalloc(&dAny, sizeof(int));
+    if (e == cudaSuccess) e = enqueue_batch_prologue(b, b->stream);
+    bool more = b->anyActive;
+    for (int pass = 0; e == cudaSuccess && more && pass < kMaxGraphPasses; ++pass) {
+        e = enqueue_batch_body(b, cudaGraphConditionalHandle{}, dAny, b->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(any, dAny, sizeof(int), cudaMemcpyDeviceToHost, b->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+        more = *any != 0;
+    }
+    if (e == cudaSuccess) e = enqueue_batch_epilogue(b, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    cudaFree(dAny);
+    cudaFreeHost(any);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return MDAS_ERR_CUDA;
+    }
+    return batch_finish(b, stats);
 }
 
 int mdas_batch_set_tiling(mdas_batch* b, const int* ctasPerSm4, int leavesPerTile) {

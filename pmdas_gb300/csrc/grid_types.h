@@ -148,7 +148,7 @@ struct MdasBatchImage {
     cudaError_t batch_scan(const MdasBatchImage* imgs, int n, cudaStream_t s);                               \
     cudaError_t batch_place(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s);             \
     cudaError_t batch_condition(const MdasBatchImage* imgs, int n, cudaGraphConditionalHandle h,             \
-                                int maxPasses, cudaStream_t s);                                              \
+                                int maxPasses, int* anyOut, cudaStream_t s);                                 \
     cudaError_t batch_integrate(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s);         \
     cudaError_t batch_clear_pixels(const MdasBatchImage* imgs, int n, cudaStream_t s);                       \
     unsigned batch_jump(int candidatesNum, int D, unsigned* C);                                              \
@@ -162,4 +162,11 @@ struct MdasBatchImage {
 MDAS_DECLARE_LAUNCHERS(mdas_fast)
 MDAS_DECLARE_LAUNCHERS(mdas_ieee)
 
-enum { MDAS_K_INIT = 0, MDAS_K_ERRORS = 1, MDAS_K_ADAPTIVE = 2, MDAS_K_INTEGRATE = 3, MDAS_K_DECIDE = 4 };
+enum {
+    MDAS_K_INIT = 0,
+    MDAS_K_ERRORS = 1,
+    MDAS_K_ADAPTIVE = 2,
+    MDAS_K_INTEGRATE = 3,
+    MDAS_K_DECIDE = 4,
+    MDAS_K_COUNT = 5
+};

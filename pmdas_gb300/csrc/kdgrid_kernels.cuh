@@ -495,7 +495,9 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
     const int warp = threadIdx.x >> 5;
     const int i0 = tile * TILE + threadIdx.x * K;
     const bool full = i0 + K <= L;
-    float err[K];
+    // learned acceptance unless the judge sent this pass back to the plain one
+    const bool learned = g.priority != nullptr && !g.learned->usePlain;
+    float err[K], pr[K];
     unsigned sd[K];
     int lc[K];
     if (full) {
@@ -515,6 +517,12 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
             const uint4 s4 = *reinterpret_cast<const uint4*>(g.seeds + i0 + q);
             err[q] = e4.x; err[q + 1] = e4.y; err[q + 2] = e4.z; err[q + 3] = e4.w;
             sd[q] = s4.x; sd[q + 1] = s4.y; sd[q + 2] = s4.z; sd[q + 3] = s4.w;
+            if (learned) {
+                const float4 p4 = *reinterpret_cast<const float4*>(g.priority + i0 + q);
+                pr[q] = p4.x; pr[q + 1] = p4.y; pr[q + 2] = p4.z; pr[q + 3] = p4.w;
+            } else {
+                pr[q] = pr[q + 1] = pr[q + 2] = pr[q + 3] = 0.0f;
+            }
         }
 #pragma unroll
         for (int j = 0; j < K; ++j) lc[j] = (int)((cw[j >> 2] >> (8 * (j & 3))) & 0xffu);
@@ -525,10 +533,9 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
             err[j] = v ? g.errors[i0 + j] : 0.0f;
             sd[j] = v ? g.seeds[i0 + j] : 0u;
             lc[j] = v ? (int)g.leafCounts[i0 + j] : 0;
+            pr[j] = v && learned ? g.priority[i0 + j] : 0.0f;
         }
     }
-    // learned acceptance unless the judge sent this pass back to the plain one
-    const bool learned = g.priority != nullptr && !g.learned->usePlain;
     const float predMax = learned ? mdas_float_unorder(g.learned->predMax) : 0.0f;
     unsigned accMask = 0;
     unsigned seedAcc[K];
@@ -540,7 +547,7 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
         bool a = false;
         if (leaf < L) {
             if (!learned) a = mdas_pow(err[j] / gError, g.alpha) >= rnd(seed);
-            else a = mdas_pow(learned_ratio(g, leaf, predMax), g.alpha) >= rnd(seed);
+            else a = mdas_pow(learned_ratio_of(pr[j], predMax, g.priorityScale), g.alpha) >= rnd(seed);
         }
         seedAcc[j] = seed;
         sd[j] = a ? jumpA * seed + jumpC : seed;  // the seed after the candidate draws

@@ -519,6 +519,12 @@ class Batch:
         N.check(self._lib.mdas_batch_render(self._h, st), "mdas_batch_render")
         return list(st)
 
+    def render_stepped(self):
+        """The same render with the pass loop on the host (kernels visible to profilers)."""
+        st = (N.RenderStats * self.n)()
+        N.check(self._lib.mdas_batch_render_stepped(self._h, st), "mdas_batch_render_stepped")
+        return list(st)
+
     def set_tuning(self, ctas_per_sm):
         a = (C.c_int * 4)(*ctas_per_sm)
         N.check(self._lib.mdas_batch_set_tuning(self._h, a), "mdas_batch_set_tuning")

@@ -149,12 +149,13 @@ def test_batch_equals_single_renders(cuda, arith):
         pix.append(torch.zeros(H, W, 4, device="cuda"))
         budgets.append(budget)
     batch = P.Batch(grids, scenes, budgets, pix, [sp[2] for sp in specs], [sp[3] for sp in specs])
-    for rnd in range(4):
+    for rnd in range(5):
         if rnd == 2:
             batch.set_tuning([2, 3, 1, 5])
         if rnd == 3:  # decide tiles of 1024 leaves: same results
             batch.set_tiling([3, 2, 2, 4], 1024)
-        stats = batch.render()
+        # the last round with the pass loop on the host
+        stats = batch.render_stepped() if rnd == 4 else batch.render()
         for i, (want, img, passes) in enumerate(singles):
             assert stats[i].passes == passes, (rnd, i)
             assert_states_equal(grids[i].dump_state(), want,

@@ -365,8 +365,9 @@ def test_learned_batch_equals_single_renders(cuda, arith):
         pix.append(torch.zeros(H_, W, 4, device="cuda"))
         budgets.append(budget)
     batch = P.Batch(grids, scenes, budgets, pix, [sp[2] for sp in specs], [sp[3] for sp in specs])
-    for rnd in range(2):
-        stats = batch.render()
+    for rnd in range(3):
+        # the last round with the pass loop on the host
+        stats = batch.render_stepped() if rnd == 2 else batch.render()
         for i, (want, img, passes, judged) in enumerate(singles):
             assert stats[i].passes == passes, (rnd, i)
             assert_states_equal(grids[i].dump_state(), want,
