@@ -64,6 +64,10 @@ def parse_args():
     ap.add_argument("--learned-host", action="store_true",
                     help="render the learned-vs-plain ladders through the host loop (mdas_render) instead of graphs")
     ap.add_argument("--no-configs", action="store_true", help="skip the other benchmark configurations")
+    ap.add_argument("--learned-only", default=None, metavar="WORKLOAD",
+                    help="only the learned-vs-plain comparison on WORKLOAD (mbdof1080 or dl4k), e.g. for profilers")
+    ap.add_argument("--ladder", default=None, metavar="SPP,...",
+                    help="with --learned-only: the spp ladder (default: the comparison's own)")
     ap.add_argument("--batch-images", type=int, default=64,
                     help="batch64: render only the first N images of the set (a smaller case for profilers)")
     ap.add_argument("--stepped", action="store_true",
@@ -1119,6 +1123,11 @@ def main():
     if world > 1:
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     from pmdas_gb300 import build as B  # noqa: F401  (the library must already be built)
+    if args.learned_only:
+        if rank == 0:
+            kw = {"ladder": tuple(float(x) for x in args.ladder.split(","))} if args.ladder else {}
+            print(json.dumps(learned_block({}, args.learned_only, host=args.learned_host, **kw)), flush=True)
+        return
     if args.workload == "batch64":
         line = run_batch(args, rank, world, local_rank)
         if rank == 0:

@@ -401,6 +401,9 @@ int mdas_learned_predict(mdas_grid* g);
  * pointer optional). */
 int mdas_learned_stats(mdas_grid* g, int* judgedPasses, int* plainPasses, int* lastPlain, double* unrefinedLearned,
                        double* unrefinedPlain);
+/* The largest priority the last update scaled the acceptance by (the maximum
+ * over every leaf's current prediction). */
+int mdas_learned_pred_max(mdas_grid* g, float* predMax);
 /* Host copies of the FP32 parameters (MDAS_MLP_PARAMS floats). */
 int mdas_learned_get_params(mdas_grid* g, float* params);
 int mdas_learned_set_params(mdas_grid* g, const float* params);

@@ -130,6 +130,7 @@ SIGNATURES = {
     "mdas_mlp_adam": (_I, [_P, _P, _P, _P, _I, _F, _P]),
     "mdas_learned_get_params": (_I, [_P, _P]),
     "mdas_learned_set_params": (_I, [_P, _P]),
+    "mdas_learned_pred_max": (_I, [_P, C.POINTER(C.c_float)]),
     "mdas_learned_predictions": (_I, [_P, _P]),
     "mdas_leaf_features": (_I, [_P, _P]),
     "mdas_mlp_forward": (_I, [_P, _P, _I, _P, _P]),

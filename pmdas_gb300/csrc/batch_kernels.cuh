@@ -114,7 +114,9 @@ __global__ void k_batch_reset(const MdasBatchImage* __restrict__ imgs, int n, in
         c->gerrNext = 0u;
     } else if (imgs[i].mlp) {
         MdasLearnedStats* st = imgs[i].g.learned;
-        st->predMax = 0u;
+        // after the first pass the predictions cover only the split children:
+        // the largest priority starts from that of the leaves the last pass kept
+        st->predMax = c->passes > 0 ? st->keptMax : 0u;
         st->blocksDone = 0u;
         st->usePlain = 0;
         st->unrefinedLearned = 0.0;
@@ -122,11 +124,12 @@ __global__ void k_batch_reset(const MdasBatchImage* __restrict__ imgs, int n, in
     }
 }
 
-// ---- learned images: the largest priority (phase 0), then the plain errors
-// each schedule leaves unrefined (phase 1), over chunks of 256 leaves across the
-// active learned images.  A block keeps its partial results while its chunks
-// stay in one image and adds them to that image's statistics when it moves on
-// (a few atomics per block and image); the verdicts follow in k_batch_verdict.
+// ---- learned images: the plain errors each schedule leaves unrefined, over
+// chunks of 256 leaves across the active learned images (the largest priority
+// came with the predictions).  A block keeps its partial results while its
+// chunks stay in one image and adds them to that image's statistics when it
+// moves on (a few atomics per block and image); the verdicts follow in
+// k_batch_verdict.
 // Compensated FP32 sum (Kahan): a thread's unrefined errors over any number of
 // leaves within about an ulp, without a per-leaf FP64 add (a slow pipe).
 struct KahanF {
@@ -140,49 +143,37 @@ struct KahanF {
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
-__device__ __forceinline__ void flush_learned(MdasLearnedStats* st, int phase, unsigned best, double ul, double up) {
-    if (phase == 0) {
-        best = __reduce_max_sync(0xffffffffu, best);
-        if ((threadIdx.x & 31) == 0 && best) atomicMax(&st->predMax, best);
-    } else {
+__device__ __forceinline__ void flush_learned(MdasLearnedStats* st, double ul, double up) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            ul += __shfl_xor_sync(0xffffffffu, ul, o);
-            up += __shfl_xor_sync(0xffffffffu, up, o);
-        }
-        if ((threadIdx.x & 31) == 0) {
-            if (ul != 0.0) atomicAdd(&st->unrefinedLearned, ul);
-            if (up != 0.0) atomicAdd(&st->unrefinedPlain, up);
-        }
+    for (int o = 16; o > 0; o >>= 1) {
+        ul += __shfl_xor_sync(0xffffffffu, ul, o);
+        up += __shfl_xor_sync(0xffffffffu, up, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (ul != 0.0) atomicAdd(&st->unrefinedLearned, ul);
+        if (up != 0.0) atomicAdd(&st->unrefinedPlain, up);
     }
 }
 
-__global__ void __launch_bounds__(256) k_batch_learned_reduce(const MdasBatchImage* __restrict__ imgs, int n,
-                                                              int phase) {
+__global__ void __launch_bounds__(256) k_batch_learned_reduce(const MdasBatchImage* __restrict__ imgs, int n) {
     __shared__ int s_pre[MDAS_MAX_BATCH + 1];
     __shared__ unsigned s_warp[8];
     const int total = batch_prefix(n, s_pre, s_warp, [&](int i) {
         return imgs[i].mlp && imgs[i].g.counts->active ? ceil_div(imgs[i].g.counts->L, 256) : 0;
     });
     int cur = -1;  // the image the block's partial results belong to (uniform across the block)
-    unsigned best = 0u;
     KahanF ul, up;
     for (int ch = blockIdx.x; ch < total; ch += gridDim.x) {
         const int img = batch_image_of(s_pre, n, ch);
         if (img != cur) {
-            if (cur >= 0) flush_learned(imgs[cur].g.learned, phase, best, ul.value(), up.value());
+            if (cur >= 0) flush_learned(imgs[cur].g.learned, ul.value(), up.value());
             cur = img;
-            best = 0u;
             ul = KahanF();
             up = KahanF();
         }
         const MdasDeviceGrid& g = imgs[img].g;
         const int i = (ch - s_pre[img]) * 256 + threadIdx.x;
         if (i >= g.counts->L) continue;
-        if (phase == 0) {
-            best = max(best, mdas_float_order(g.priority[i]));
-            continue;
-        }
         const float gError = __uint_as_float(g.counts->gerr);
         const float predMax = mdas_float_unorder(g.learned->predMax);
         const float e = g.errors[i];
@@ -192,7 +183,7 @@ __global__ void __launch_bounds__(256) k_batch_learned_reduce(const MdasBatchIma
         if (!(mdas_pow(e / gError, g.alpha) >= r)) up.add(e);
         if (!(mdas_pow(learned_ratio(g, i, predMax), g.alpha) >= r)) ul.add(e);
     }
-    if (cur >= 0) flush_learned(imgs[cur].g.learned, phase, best, ul.value(), up.value());
+    if (cur >= 0) flush_learned(imgs[cur].g.learned, ul.value(), up.value());
 }
 
 // One thread per image: the verdict of a learned image's pass.
@@ -204,6 +195,7 @@ __global__ void k_batch_verdict(const MdasBatchImage* __restrict__ imgs, int n) 
     st->usePlain = revert;
     st->plainPasses += revert;
     st->judgedPasses += 1;
+    st->keptMax = 0u;  // taken by this pass's predMax; the adaptive pass sets it anew
 }
 
 // ---- errors: full on an image's first pass, its split children after
@@ -229,24 +221,24 @@ __global__ void __launch_bounds__(256) k_batch_errors(const MdasBatchImage* __re
         const int k = (ch - s_pre[i]) * 256 + threadIdx.x;
         float maxError = dirty ? __uint_as_float(cnt->gerrNext) : 0.0f;
         unsigned recomputed = 0;
-        if (k < items && dirty && !g.featRaw) {
-            // split children from the splitting pass's lists (no leaf record read)
+        if (k < items && dirty) {
+            // split children from the splitting pass's lists (no leaf record read);
+            // learned images also complete the child's raw feature row
             const bool left = k < newL;
             const int4 sp = left ? g.splitL[k] : g.splitR[k - newL];
             const int nodeIndex = left ? sp.z : firstRight + (k - newL);
+            MdasLumStats lum;
             const float error = node_error<D>(g, make_int4(sp.x, sp.y, left ? ~D : sp.z, ~D), __int_as_float(sp.w),
-                                              nullptr);
+                                              g.featRaw ? &lum : nullptr);
+            if (g.featRaw) mdas_raw_store_stats(g.featRaw + (size_t)k * MDAS_RAW_FLOATS, lum, error);
             g.errors[nodeIndex] = error;
             recomputed = 1;
             maxError = fmaxf(maxError, error);
         } else if (k < items) {
-            const int nodeIndex = dirty ? (k < newL ? g.dirty[k] : firstRight + (k - newL)) : k;
-            // split children: -1 by construction (not read); learned images also
-            // leave the item's raw feature row for the prediction
-            float error = dirty ? -1.0f : g.errors[nodeIndex];
+            float error = g.errors[k];
             if (error < 0.0f) {
-                error = leaf_error<D>(g, nodeIndex, dirty && g.featRaw ? g.featRaw + (size_t)k * MDAS_RAW_FLOATS : nullptr);
-                g.errors[nodeIndex] = error;
+                error = leaf_error<D>(g, k);
+                g.errors[k] = error;
                 recomputed = 1;
             }
             maxError = fmaxf(maxError, error);
@@ -288,13 +280,16 @@ __global__ void __launch_bounds__(256) k_batch_decide(const MdasBatchImage* __re
         const int L = g.counts->L;
         const float gError = __uint_as_float(g.counts->gerr);
         float keptMax = 0.0f;
-        unsigned gathered = 0;
-        decide_tile<D, K>(g, t - s_pre[i], L, gError, imgs[i].jumpA, imgs[i].jumpC, s_warp, keptMax, gathered);
+        unsigned gathered = 0, keptPrio = 0;
+        decide_tile<D, K>(g, t - s_pre[i], L, gError, imgs[i].jumpA, imgs[i].jumpC, s_warp, keptMax, gathered,
+                          keptPrio);
         const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(keptMax));
         const unsigned c = __reduce_add_sync(0xffffffffu, gathered);
+        const unsigned kp = __reduce_max_sync(0xffffffffu, keptPrio);
         if ((threadIdx.x & 31) == 0) {
             if (m) atomicMax(&g.counts->gerrNext, m);
             if (c) atomicAdd(&g.counts->gathered, c);
+            if (kp) atomicMax(&g.learned->keptMax, kp);
         }
     }
 }
@@ -413,8 +408,7 @@ cudaError_t batch_reset(const MdasBatchImage* imgs, int n, int which, cudaStream
 }
 
 cudaError_t batch_learned_judge(const MdasBatchImage* imgs, int n, int grid, cudaStream_t s) {
-    k_batch_learned_reduce<<<grid, 256, 0, s>>>(imgs, n, 0);  // the largest priority of every image first
-    k_batch_learned_reduce<<<grid, 256, 0, s>>>(imgs, n, 1);
+    k_batch_learned_reduce<<<grid, 256, 0, s>>>(imgs, n);
     k_batch_verdict<<<(n + 255) / 256, 256, 0, s>>>(imgs, n);
     return cudaGetLastError();
 }

@@ -109,6 +109,7 @@ struct mdas_grid {
     float* lPred = nullptr;             // [maxNodes] predicted log2(error) / MDAS_MLP_TARGET_SCALE
     float* lRaw = nullptr;              // [maxNodes * MDAS_RAW_FLOATS] raw feature rows of the split-children errors pass
     bool rawValid = false;              // the last errors pass wrote lRaw for the leaves it recomputed
+    bool extentsValid = false;          // the last adaptive pass wrote the box extents of its split children's rows
     MdasLearnedStats* lStats = nullptr;
     uint64_t lPredVersion = ~0ull;      // grid version the predictions (and the verdict) belong to
     bool lastErrorsDirty = false;       // the last errors pass visited only the split children
@@ -437,6 +438,7 @@ int mdas_initial_sampling(mdas_grid* g) {
     g->initialized = true;
     g->errorsClean = false;
     g->dirtyValid = false;
+    g->extentsValid = false;
     if (g->log) {
         const double t = last_stage_ms(g, 0);
         *g->log << "INITIAL SAMPLES\n" << g->N << std::endl;
@@ -455,7 +457,7 @@ int mdas_compute_errors(mdas_grid* g) {
     if (rc) return rc;
     g->errorsClean = true;
     g->lastErrorsDirty = dirty;
-    g->rawValid = dirty && g->dg.featRaw != nullptr;
+    g->rawValid = dirty && g->dg.featRaw != nullptr && g->extentsValid;
     if (g->log) *g->log << "COMPUTE ERRORS TIME\n" << last_stage_ms(g, 1) << std::endl;
     return MDAS_OK;
 }
@@ -479,6 +481,7 @@ int mdas_adaptive_sampling(mdas_grid* g) {
     int rc = timed(g, 2, [&]() { return launch_adaptive(g, gridDecide, gridPlace); });
     g->dg.priority = nullptr;
     g->dirtyValid = g->errorsClean;
+    g->extentsValid = g->dg.featRaw != nullptr;
     g->errorsClean = false;
     g->launches += 3;
     if (rc) {
@@ -683,6 +686,7 @@ int mdas_load_state(mdas_grid* g, int numberOfSamples, int numberOfNodes, const 
     g->initialized = true;
     g->errorsClean = false;
     g->dirtyValid = false;
+    g->extentsValid = false;
     return MDAS_OK;
 }
 
@@ -1038,6 +1042,7 @@ int render_graph_finish(mdas_grid* g, mdas_render_stats* stats) {
     g->initialized = true;
     g->errorsClean = false;
     g->dirtyValid = g->hcounts->passes > 0;
+    g->extentsValid = g->dirtyValid && g->dg.featRaw != nullptr;
     if (stats) {
         stats->numberOfSamples = g->N;
         stats->numberOfNodes = g->L;
@@ -1319,6 +1324,7 @@ int batch_finish(mdas_batch* b, mdas_render_stats* stats) {
         g->initialized = true;
         g->errorsClean = false;
         g->dirtyValid = g->hcounts->passes > 0;
+        g->extentsValid = g->dirtyValid && g->dg.featRaw != nullptr;
         if (stats) {
             stats[i].numberOfSamples = g->N;
             stats[i].numberOfNodes = g->L;
@@ -1776,7 +1782,7 @@ cudaError_t learned_queue(mdas_grid* g, int L, cudaStream_t s) {
     if (e == cudaSuccess)
         e = g->arith == MDAS_ARITH_IEEE ? mdas_ieee::learned_judge(dg, L, grid, s)
                                         : mdas_fast::learned_judge(dg, L, grid, s);
-    g->launches += 3;
+    g->launches += 2;
     return e;
 }
 
@@ -1795,6 +1801,7 @@ int mdas_learned_enable(mdas_grid* g, const mdas_learned_config* cfg) {
         g->dg.learned = nullptr;
         g->dg.featRaw = nullptr;
         g->rawValid = false;
+        g->extentsValid = false;
         return MDAS_OK;
     }
     if (!(cfg->tolerance >= 0.0f)) return MDAS_ERR_INVALID;
@@ -1820,6 +1827,7 @@ int mdas_learned_enable(mdas_grid* g, const mdas_learned_config* cfg) {
     g->dg.learned = g->lStats;
     g->dg.featRaw = g->lRaw;
     g->rawValid = false;
+    g->extentsValid = false;
     g->learned = true;
     return MDAS_OK;
 }
@@ -1842,7 +1850,7 @@ int mdas_learned_predict(mdas_grid* g) {
     if (!g->initialized) return MDAS_ERR_STATE;
     cudaError_t e = mdas_mlp::predict_leaves(g->dg, g->L, 0, g->lPacked, g->lPred, &g->lStats->predMax,
                                              learned_status(g), g->stream);
-    g->launches += 2;
+    g->launches += 1;
     unsigned st = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&st, learned_status(g), sizeof(st), cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
@@ -1862,6 +1870,16 @@ int mdas_learned_stats(mdas_grid* g, int* judgedPasses, int* plainPasses, int* l
     if (lastPlain) *lastPlain = h.usePlain;
     if (unrefinedLearned) *unrefinedLearned = h.unrefinedLearned;
     if (unrefinedPlain) *unrefinedPlain = h.unrefinedPlain;
+    return MDAS_OK;
+}
+
+int mdas_learned_pred_max(mdas_grid* g, float* predMax) {
+    if (!g || !g->lStats || !predMax) return MDAS_ERR_INVALID;
+    unsigned bits = 0;
+    cudaError_t e = cudaMemcpyAsync(&bits, &g->lStats->predMax, sizeof(bits), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return MDAS_ERR_CUDA;
+    *predMax = mdas_float_unorder(bits);
     return MDAS_OK;
 }
 

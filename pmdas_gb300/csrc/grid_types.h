@@ -34,6 +34,11 @@ struct MdasLearnedStats {
     double unrefinedPlain;       // the same for the plain schedule
     float tolerance;             // revert when unrefinedLearned > (1 + tolerance) * unrefinedPlain
     int judgedPasses;
+    // order-preserving bits of the largest priority of the leaves the last
+    // adaptive pass did not split (their priorities carry over to the next
+    // pass, whose predictions of the split children complete predMax); set by
+    // decide, cleared by the judge once the predictions have taken it
+    unsigned keptMax;
 };
 
 // Order-preserving unsigned image of a float (for atomicMax over floats of any sign).

@@ -358,16 +358,11 @@ __device__ __forceinline__ float node_error(const MdasDeviceGrid& g, const int4 
     return error;
 }
 
-// raw (may be null): the leaf's row of raw feature inputs (learned mode).
 template <int D>
-__device__ __forceinline__ float leaf_error(const MdasDeviceGrid& g, int nodeIndex, float* raw = nullptr) {
+__device__ __forceinline__ float leaf_error(const MdasDeviceGrid& g, int nodeIndex) {
     float mn[D], mx[D];
     const int4 node = nb_load<D, 64>(g.nb + (size_t)nodeIndex * NbLayout<D>::FLOATS, mn, mx);
-    const float volume = box_volume<D>(mn, mx);
-    MdasLumStats lum;
-    const float error = node_error<D>(g, node, volume, raw ? &lum : nullptr);
-    if (raw) mdas_raw_store<D>(raw, mn, mx, lum, error);
-    return error;
+    return node_error<D>(g, node, box_volume<D>(mn, mx), nullptr);
 }
 
 // MODE 0: full, 1: dirty, 2: dirty unless no adaptive pass ran since the
@@ -388,30 +383,28 @@ __global__ void __launch_bounds__(256, 6) k_compute_errors(MdasDeviceGrid g) {
         items = g.counts->L;
     }
     unsigned recomputed = 0;
-    if (DIRTY && !g.featRaw) {
+    if (DIRTY) {
         // the split children's sample lists, slots and box volumes, as the
-        // splitting pass left them (no leaf record read)
+        // splitting pass left them (no leaf record read); learned mode also
+        // completes each child's raw feature row (item k is row k)
         for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < items; k += gridDim.x * blockDim.x) {
             const bool left = k < newL;
             const int4 sp = left ? g.splitL[k] : g.splitR[k - newL];
             const int nodeIndex = left ? sp.z : firstRight + (k - newL);
             const int4 node = make_int4(sp.x, sp.y, left ? ~D : sp.z, ~D);
-            const float error = node_error<D>(g, node, __int_as_float(sp.w), nullptr);
+            MdasLumStats lum;
+            const float error = node_error<D>(g, node, __int_as_float(sp.w), g.featRaw ? &lum : nullptr);
+            if (g.featRaw) mdas_raw_store_stats(g.featRaw + (size_t)k * MDAS_RAW_FLOATS, lum, error);
             g.errors[nodeIndex] = error;
             recomputed++;
             maxError = fmaxf(maxError, error);
         }
     } else {
         for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < items; k += gridDim.x * blockDim.x) {
-            const int nodeIndex = DIRTY ? (k < newL ? g.dirty[k] : firstRight + (k - newL)) : k;
-            // the last pass set the error of both children of each split to -1 (decide
-            // the left one, place the right one), so a dirty item is never read
-            float error = DIRTY ? -1.0f : g.errors[nodeIndex];
+            float error = g.errors[k];
             if (error < 0.0f) {
-                // learned mode: the item's row of raw feature inputs for the prediction
-                error = leaf_error<D>(g, nodeIndex,
-                                      DIRTY && g.featRaw ? g.featRaw + (size_t)k * MDAS_RAW_FLOATS : nullptr);
-                g.errors[nodeIndex] = error;
+                error = leaf_error<D>(g, k);
+                g.errors[k] = error;
                 recomputed++;
             }
             maxError = fmaxf(maxError, error);
@@ -485,9 +478,12 @@ __device__ __forceinline__ float learned_ratio(const MdasDeviceGrid& g, int leaf
 // counts and its compacted accepted list (shared by the single-image and the
 // batched kernels).
 // K: leaves per thread (4 or 8): a tile is 256 K leaves (g.tileK must be K).
+// keptPrio: the order bits of the largest priority of the leaves not split
+// (learned mode, whichever acceptance the pass takes).
 template <int D, int K>
 __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, int L, float gError, unsigned jumpA,
-                                            unsigned jumpC, unsigned* s_warp, float& keptMax, unsigned& gathered) {
+                                            unsigned jumpC, unsigned* s_warp, float& keptMax, unsigned& gathered,
+                                            unsigned& keptPrio) {
     constexpr int kMaxNodeSize = 4;  // KDGrid ctor: maxNodeSize(4), kdgrid.cu:611
     constexpr int TILE = 256 * K;
     static_assert((K == 4 || K == 8) && TILE <= 2048, "tile = 256 threads x K leaves, local index in 11 bits");
@@ -496,7 +492,8 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
     const int i0 = tile * TILE + threadIdx.x * K;
     const bool full = i0 + K <= L;
     // learned acceptance unless the judge sent this pass back to the plain one
-    const bool learned = g.priority != nullptr && !g.learned->usePlain;
+    const bool havePrio = g.priority != nullptr;
+    const bool learned = havePrio && !g.learned->usePlain;
     float err[K], pr[K];
     unsigned sd[K];
     int lc[K];
@@ -517,7 +514,7 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
             const uint4 s4 = *reinterpret_cast<const uint4*>(g.seeds + i0 + q);
             err[q] = e4.x; err[q + 1] = e4.y; err[q + 2] = e4.z; err[q + 3] = e4.w;
             sd[q] = s4.x; sd[q + 1] = s4.y; sd[q + 2] = s4.z; sd[q + 3] = s4.w;
-            if (learned) {
+            if (havePrio) {
                 const float4 p4 = *reinterpret_cast<const float4*>(g.priority + i0 + q);
                 pr[q] = p4.x; pr[q + 1] = p4.y; pr[q + 2] = p4.z; pr[q + 3] = p4.w;
             } else {
@@ -533,7 +530,7 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
             err[j] = v ? g.errors[i0 + j] : 0.0f;
             sd[j] = v ? g.seeds[i0 + j] : 0u;
             lc[j] = v ? (int)g.leafCounts[i0 + j] : 0;
-            pr[j] = v && learned ? g.priority[i0 + j] : 0.0f;
+            pr[j] = v && havePrio ? g.priority[i0 + j] : 0.0f;
         }
     }
     const float predMax = learned ? mdas_float_unorder(g.learned->predMax) : 0.0f;
@@ -561,7 +558,10 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
     for (int j = 0; j < K; ++j) {
         gathered += (unsigned)cnt[j];
         if (cnt[j] >= kMaxNodeSize) splitMask |= 1u << j;
-        if (i0 + j < L && !((splitMask >> j) & 1u)) keptMax = fmaxf(keptMax, err[j]);
+        if (i0 + j < L && !((splitMask >> j) & 1u)) {
+            keptMax = fmaxf(keptMax, err[j]);
+            if (havePrio) keptPrio = max(keptPrio, mdas_float_order(pr[j]));
+        }
     }
     if (full) {
 #pragma unroll
@@ -654,13 +654,16 @@ __global__ void __launch_bounds__(256) k_adaptive_decide(MdasDeviceGrid g, unsig
     const int ntiles = (L + 256 * K - 1) / (256 * K);
     float keptMax = 0.0f;   // max error of the leaves this CTA does not split
     unsigned gathered = 0;  // sample coordinates read
+    unsigned keptPrio = 0;  // max priority of those leaves (learned mode)
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
-        decide_tile<D, K>(g, tile, L, gError, jumpA, jumpC, s_warp, keptMax, gathered);
+        decide_tile<D, K>(g, tile, L, gError, jumpA, jumpC, s_warp, keptMax, gathered, keptPrio);
     unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(keptMax));
     unsigned c = __reduce_add_sync(0xffffffffu, gathered);
+    unsigned kp = __reduce_max_sync(0xffffffffu, keptPrio);
     if ((threadIdx.x & 31) == 0) {
         if (m) atomicMax(&g.counts->gerrNext, m);
         if (c) atomicAdd(&g.counts->gathered, c);
+        if (kp) atomicMax(&g.learned->keptMax, kp);
     }
 }
 
@@ -888,6 +891,12 @@ __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, i
             for (int i = 0; i < D; ++i) lmx[i] = (i == axis) ? splitPosition : mx[i];
             g.splitL[rank_] = make_int4(l0, l1, nodeIndex, __float_as_int(box_volume<D>(mn, lmx)));
             g.splitR[rank_] = make_int4(r0, r1, r2, __float_as_int(box_volume<D>(rmn, mx)));
+            // learned mode: the children's box extents, the first half of their
+            // raw feature rows (the errors pass writes the second)
+            if (g.featRaw) {
+                mdas_raw_store_extents<D>(g.featRaw + (size_t)rank_ * MDAS_RAW_FLOATS, mn, lmx);
+                mdas_raw_store_extents<D>(g.featRaw + (size_t)(g.counts->newL + rank_) * MDAS_RAW_FLOATS, rmn, mx);
+            }
         }
         // a new slot starts without a seed: the reference's seed buffer is zeroed
         // once at InitialSampling (kdgrid.cu:637), and a slot's first draw starts
@@ -1213,6 +1222,7 @@ __global__ void __launch_bounds__(256) k_learned_judge(MdasDeviceGrid g, int Lho
         st->plainPasses += revert;
         st->judgedPasses += 1;
         st->blocksDone = 0;
+        st->keptMax = 0u;  // taken by this pass's predMax; the adaptive pass sets it anew
     }
 }
 

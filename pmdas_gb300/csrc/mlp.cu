@@ -139,13 +139,19 @@ __host__ __device__ __forceinline__ int core_off(int r, int k, int KB) {
 __device__ __forceinline__ uint16_t bf16_bits(float x) { return __bfloat16_as_ushort(__float2bfloat16_rn(x)); }
 __device__ __forceinline__ float bf16_val(uint16_t b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
 
+// two floats as BF16 (round to nearest even), the first in the low half
+__device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
 // 8 consecutive K-elements of row r (one core-matrix row, 16 bytes)
 __device__ __forceinline__ void st_row8(uint8_t* tile, int r, int kb, int KB, const float* v) {
     uint4 q;
-    q.x = (uint32_t)bf16_bits(v[0]) | ((uint32_t)bf16_bits(v[1]) << 16);
-    q.y = (uint32_t)bf16_bits(v[2]) | ((uint32_t)bf16_bits(v[3]) << 16);
-    q.z = (uint32_t)bf16_bits(v[4]) | ((uint32_t)bf16_bits(v[5]) << 16);
-    q.w = (uint32_t)bf16_bits(v[6]) | ((uint32_t)bf16_bits(v[7]) << 16);
+    q.x = bf16x2_bits(v[0], v[1]);
+    q.y = bf16x2_bits(v[2], v[3]);
+    q.z = bf16x2_bits(v[4], v[5]);
+    q.w = bf16x2_bits(v[6], v[7]);
     *reinterpret_cast<uint4*>(tile + 2 * core_off(r, kb * 8, KB)) = q;
 }
 __device__ __forceinline__ void ld_row8(const uint8_t* tile, int r, int kb, int KB, float* v) {
@@ -270,8 +276,9 @@ __device__ __forceinline__ void tmem_row(const Ctx& c, float (&acc)[kH]) {
     tmem_wait_ld();
 }
 
-// Issue `steps` MMAs over K (16 each) of A at aOff (KB K-blocks) x B at bOff, then wait.
-__device__ __forceinline__ void run_mma(Ctx& c, int aOff, int bOff, int KB, int steps) {
+// Issue `steps` MMAs over K (16 each) of A at aOff (KB K-blocks) x B at bOff
+// (after the CTA's shared-memory writes); mma_wait completes them.
+__device__ __forceinline__ void mma_issue(Ctx& c, int aOff, int bOff, int KB, int steps) {
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -283,32 +290,40 @@ __device__ __forceinline__ void run_mma(Ctx& c, int aOff, int bOff, int KB, int 
                      s > 0 ? 1u : 0u);
         mma_commit(c.bar);
     }
+}
+
+__device__ __forceinline__ void run_mma(Ctx& c, int aOff, int bOff, int KB, int steps) {
+    mma_issue(c, aOff, bOff, KB, steps);
     mma_wait(c);
 }
 
 // Forward of the tile whose features this thread wrote as row threadIdx.x of SM_X:
-// z2 = the layer-2 pre-activations (b2 added).  between() runs after layer 1's
-// MMA completed and before layer 2's is issued (loads for the next tile).
-template <typename Between>
-__device__ __forceinline__ void tile_forward(Ctx& c, float (&z2)[kH], Between between) {
+// z2 = the layer-2 pre-activations (b2 added).  during1() and during2() run
+// while layer 1's and layer 2's MMAs execute (global loads for the next tile
+// into registers; they touch neither the operand tiles nor tensor memory).
+template <typename During1, typename During2>
+__device__ __forceinline__ void tile_forward(Ctx& c, float (&z2)[kH], During1 during1, During2 during2) {
     const float* b1 = reinterpret_cast<const float*>(c.sm + SM_VEC);
     const float* b2 = b1 + kH;
-    run_mma(c, SM_X, SM_W1, 2, 1);
-    between();
+    mma_issue(c, SM_X, SM_W1, 2, 1);
+    during1();
+    mma_wait(c);
     float acc[kH];
     tmem_row(c, acc);
 #pragma unroll
     for (int i = 0; i < kH; ++i) acc[i] = fmaxf(acc[i] + b1[i], 0.0f);
 #pragma unroll
     for (int kb = 0; kb < kH / 8; ++kb) st_row8(c.sm + SM_H, threadIdx.x, kb, 8, acc + 8 * kb);
-    run_mma(c, SM_H, SM_W2, 8, kH / 16);
+    mma_issue(c, SM_H, SM_W2, 8, kH / 16);
+    during2();
+    mma_wait(c);
     tmem_row(c, z2);
 #pragma unroll
     for (int i = 0; i < kH; ++i) z2[i] += b2[i];
 }
 
 __device__ __forceinline__ void tile_forward(Ctx& c, float (&z2)[kH]) {
-    tile_forward(c, z2, [] {});
+    tile_forward(c, z2, [] {}, [] {});
 }
 
 __device__ __forceinline__ float head(const Ctx& c, const float (&z2)[kH]) {
@@ -333,7 +348,10 @@ __device__ __forceinline__ void put_features(const Ctx& c, const float (&f)[kIn]
 // errors of the four neighbouring leaf slots (slot +-1, +-2: initial cells in
 // Morton order, split children next to the children of neighbouring parents),
 // log2(error) / 32.
-__device__ __forceinline__ float log2_err(float e) { return log2f(fmaxf(e, 1e-30f)) * (1.0f / MDAS_MLP_TARGET_SCALE); }
+// (The features use the hardware base-2 logarithm, MUFU.LG2 via __log2f: its
+// arguments here are normal numbers >= 1e-30, and its relative error of about
+// 2^-22 is far below what the BF16 inputs of the network resolve.)
+__device__ __forceinline__ float log2_err(float e) { return __log2f(fmaxf(e, 1e-30f)) * (1.0f / MDAS_MLP_TARGET_SCALE); }
 
 // The raw inputs of a leaf's features (leaf_raw.h), gathered from its record
 // and sample values.
@@ -396,23 +414,23 @@ __device__ void feats_of_raw(const MdasDeviceGrid& g, const float (&raw)[MDAS_RA
 #pragma unroll
     for (int j = 0; j < D; ++j) {
         float e = raw[j];
-        if (j == 0) e /= g.scaleX;
-        if (j == 1) e /= g.scaleY;
-        const float l = log2f(fmaxf(e, 1e-30f));
+        if (j == 0) e = __fdividef(e, g.scaleX);
+        if (j == 1) e = __fdividef(e, g.scaleY);
+        const float l = __log2f(fmaxf(e, 1e-30f));
         if (j < 5) f[j] = l * (1.0f / 16.0f);
         depth += -(float)(g.bitsPerDim + (j < 2 ? g.extraImgBits : 0)) - l;
     }
 #pragma unroll
     for (int j = D; j < 5; ++j) f[j] = 0.0f;
     const float n = raw[6];
-    const float inv = n > 0.0f ? 1.0f / n : 0.0f;
+    const float inv = n > 0.0f ? __frcp_rn(n) : 0.0f;
     const float mean = raw[7] * inv;
     const float var = fmaxf(raw[8] * inv - mean * mean, 0.0f);
     f[5] = n * 0.25f;
-    f[6] = log2f(1.0f + fabsf(mean));
-    f[7] = log2f(1.0f + sqrtf(var));
-    f[8] = n > 0.0f ? log2f(1.0f + fabsf(raw[9])) : 0.0f;
-    f[9] = n > 0.0f ? log2f(1.0f + fabsf(raw[10])) : 0.0f;
+    f[6] = __log2f(1.0f + fabsf(mean));
+    f[7] = __log2f(1.0f + sqrtf(var));
+    f[8] = n > 0.0f ? __log2f(1.0f + fabsf(raw[9])) : 0.0f;
+    f[9] = n > 0.0f ? __log2f(1.0f + fabsf(raw[10])) : 0.0f;
     f[10] = log2_err(raw[11]);
     f[11] = depth * (1.0f / 32.0f);
 #pragma unroll
@@ -459,14 +477,20 @@ __global__ void __launch_bounds__(kThreads) k_forward_rows(const Packed* __restr
 // errors pass wrote (g.featRaw); 2: as 3 (as 1 without rows), or every leaf
 // before the first adaptive pass.  Lhost < 0: the leaf count in the device
 // counters.
+// predMax (may be null): receives the largest priority over all leaves: the
+// largest of the rows predicted here, and for the split children only, that
+// of the leaves the last adaptive pass kept (*keptMax).
 template <int D>
 __global__ void __launch_bounds__(kThreads, 4) k_predict_leaves(MdasDeviceGrid g, int Lhost, int mode,
                                                              const Packed* __restrict__ w, float* __restrict__ pred,
+                                                             unsigned* predMax, const unsigned* keptMax,
                                                              unsigned* status) {
     Ctx c;
     ctx_open(c, w, status);
     const int L = Lhost >= 0 ? Lhost : g.counts->L;
     const bool dirty = mode == 1 || mode == 3 || (mode == 2 && g.counts->passes > 0);
+    unsigned best = 0u;  // order bits of this thread's largest prediction
+    if (predMax && dirty && keptMax && blockIdx.x == 0 && threadIdx.x == 0 && *keptMax) atomicMax(predMax, *keptMax);
     const bool rows_raw = dirty && g.featRaw && mode != 1;
     const int newL = g.counts->newL;
     const int rows = dirty ? 2 * newL : L;
@@ -474,8 +498,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_predict_leaves(MdasDeviceGrid g
     auto leaf_of = [&](int r) { return !dirty ? r : (r < newL ? g.dirty[r] : (L - newL) + (r - newL)); };
     if (rows_raw) {
         // The rows of the errors pass: the next tile's row and leaf index are
-        // loaded while this tile's layer-1 MMA runs, its neighbours' errors
-        // after it, so a tile's inputs are at hand when its features are formed.
+        // loaded while this tile's layer-1 MMA runs, the errors of that leaf's
+        // neighbours while its layer-2 MMA runs, so a tile's inputs are at hand
+        // when its features are formed.
         int tile = blockIdx.x;
         int r = tile * kRows + threadIdx.x;
         float raw[MDAS_RAW_FLOATS], ne[4];
@@ -494,24 +519,37 @@ __global__ void __launch_bounds__(kThreads, 4) k_predict_leaves(MdasDeviceGrid g
             put_features(c, f);
             const int rNext = (tile + gridDim.x) * kRows + threadIdx.x;
             const bool more = tile + gridDim.x < tiles && rNext < rows;
-            float rawNext[MDAS_RAW_FLOATS];
+            float rawNext[MDAS_RAW_FLOATS], neNext[4];
             int leafNext = 0;
             float z2[kH];
-            tile_forward(c, z2, [&] {
-                if (more) {
-                    load_raw(g.featRaw + (size_t)rNext * MDAS_RAW_FLOATS, rawNext);
-                    leafNext = leaf_of(rNext);
-                }
-            });
+            tile_forward(
+                c, z2,
+                [&] {
+                    if (more) {
+                        load_raw(g.featRaw + (size_t)rNext * MDAS_RAW_FLOATS, rawNext);
+                        leafNext = leaf_of(rNext);
+                    }
+                },
+                [&] {
+                    if (more) nbr_errors(g, leafNext, L, rawNext[11], neNext);
+                });
             const float p = head(c, z2);
-            if (r < rows) pred[leaf] = f[10] + p;
+            if (r < rows) {
+                pred[leaf] = f[10] + p;
+                best = max(best, mdas_float_order(f[10] + p));
+            }
             if (more) {
 #pragma unroll
                 for (int i = 0; i < MDAS_RAW_FLOATS; ++i) raw[i] = rawNext[i];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) ne[q] = neNext[q];
                 leaf = leafNext;
-                nbr_errors(g, leaf, L, raw[11], ne);
             }
             r = rNext;
+        }
+        if (predMax) {
+            best = __reduce_max_sync(0xffffffffu, best);
+            if ((threadIdx.x & 31) == 0 && best) atomicMax(predMax, best);
         }
         ctx_close(c);
         return;
@@ -532,12 +570,21 @@ __global__ void __launch_bounds__(kThreads, 4) k_predict_leaves(MdasDeviceGrid g
         float z2[kH];
         tile_forward(c, z2);
         const float p = head(c, z2);
-        if (r < rows) pred[leaf] = f[10] + p;
+        if (r < rows) {
+            pred[leaf] = f[10] + p;
+            best = max(best, mdas_float_order(f[10] + p));
+        }
+    }
+    if (predMax) {
+        best = __reduce_max_sync(0xffffffffu, best);
+        if ((threadIdx.x & 31) == 0 && best) atomicMax(predMax, best);
     }
     ctx_close(c);
 }
 
-// Batched: the learned images' priorities in one launch (one dimension).
+// Batched: the learned images' priorities in one launch (one dimension), and
+// into each image's predMax the largest (which k_batch_reset started from the
+// leaves the last pass kept).
 // Tiles of 128 rows are enumerated across the images (each image's rows as in
 // mode 2 above); a CTA reloads the weights when its tile belongs to an image
 // with other weights.
@@ -595,37 +642,15 @@ __global__ void __launch_bounds__(kThreads, 4) k_batch_predict(const MdasBatchIm
         float z2[kH];
         tile_forward(c, z2);
         const float p = head(c, z2);
-        if (r < rows) const_cast<float*>(g.priority)[leaf] = f[10] + p;
+        unsigned best = 0u;
+        if (r < rows) {
+            const_cast<float*>(g.priority)[leaf] = f[10] + p;
+            best = mdas_float_order(f[10] + p);
+        }
+        best = __reduce_max_sync(0xffffffffu, best);  // the tile is one image's
+        if ((threadIdx.x & 31) == 0 && best) atomicMax(&g.learned->predMax, best);
     }
     ctx_close(c);
-}
-
-// The largest priority over all leaves (order-preserving bits into *out).
-__global__ void __launch_bounds__(256) k_priority_max(const MdasDeviceGrid g, int Lhost, const float* __restrict__ pred,
-                                                      unsigned* out) {
-    const int L = Lhost >= 0 ? Lhost : g.counts->L;
-    unsigned best = 0u;
-    // 16-byte loads, two in flight per thread (pred is 256-byte aligned)
-    const int L4 = L >> 2;
-    const float4* p4 = reinterpret_cast<const float4*>(pred);
-    const int stride = gridDim.x * blockDim.x;
-    int v = blockIdx.x * blockDim.x + threadIdx.x;
-    for (; v + stride < L4; v += 2 * stride) {
-        const float4 a = p4[v], b = p4[v + stride];
-        best = max(best, max(max(mdas_float_order(a.x), mdas_float_order(a.y)),
-                             max(mdas_float_order(a.z), mdas_float_order(a.w))));
-        best = max(best, max(max(mdas_float_order(b.x), mdas_float_order(b.y)),
-                             max(mdas_float_order(b.z), mdas_float_order(b.w))));
-    }
-    if (v < L4) {
-        const float4 a = p4[v];
-        best = max(best, max(max(mdas_float_order(a.x), mdas_float_order(a.y)),
-                             max(mdas_float_order(a.z), mdas_float_order(a.w))));
-    }
-    for (int i = 4 * L4 + blockIdx.x * blockDim.x + threadIdx.x; i < L; i += stride)
-        best = max(best, mdas_float_order(pred[i]));
-    best = __reduce_max_sync(0xffffffffu, best);
-    if ((threadIdx.x & 31) == 0 && best) atomicMax(out, best);
 }
 
 template <int D>
@@ -880,18 +905,15 @@ cudaError_t predict_leaves(const MdasDeviceGrid& g, int L, int mode, const Packe
     if (L == 0) return cudaSuccess;
     const int tiles = L > 0 && mode == 0 ? (L + kRows - 1) / kRows : sm_count() * 4;
     const int grid = tiles < sm_count() * 4 ? tiles : sm_count() * 4;
-    cudaError_t e = cudaSuccess;
+    cudaError_t e = predMax ? cudaMemsetAsync(predMax, 0, sizeof(unsigned), s) : cudaSuccess;
+    if (e != cudaSuccess) return e;
+    const unsigned* kept = g.learned ? &g.learned->keptMax : nullptr;
     MLP_SWITCH_D(g.D, (e = set_smem(k_predict_leaves<DD>, kFwdSmem),
                        e == cudaSuccess ? (k_predict_leaves<DD><<<grid, kThreads, kFwdSmem, s>>>(g, L, mode, w, pred,
-                                                                                               status),
+                                                                                               predMax, kept, status),
                                            0)
                                         : 0));
     if (e != cudaSuccess) return e;
-    if (predMax) {
-        e = cudaMemsetAsync(predMax, 0, sizeof(unsigned), s);
-        if (e != cudaSuccess) return e;
-        k_priority_max<<<sm_count() * 4, 256, 0, s>>>(g, L, pred, predMax);
-    }
     return cudaGetLastError();
 }
 

@@ -56,8 +56,10 @@ cudaError_t forward(const Packed* w, const float* features, int m, float* pred, 
 // correction, for every leaf (mode 0), the leaves whose error the last errors
 // pass recomputed (1: features gathered; 3: from the raw rows that pass wrote
 // to g.featRaw), or as 3 unless no adaptive pass ran yet (2; as 1 if
-// g.featRaw is null); L < 0: the leaf count in the device counters.  Then the largest priority over all
-// leaves into *predMax (order-preserving bits; skipped if null).
+// g.featRaw is null); L < 0: the leaf count in the device counters.  The largest priority over all
+// leaves goes to *predMax (order-preserving bits; skipped if null): the largest
+// prediction made, and where only the split children were predicted, that of
+// the leaves the last adaptive pass kept (g.learned->keptMax, from its decide).
 cudaError_t predict_leaves(const MdasDeviceGrid& g, int L, int mode, const Packed* w, float* pred, unsigned* predMax,
                            unsigned* status, cudaStream_t s);
 // Batched: the priorities of the active learned images of a batch (all of one

@@ -303,6 +303,12 @@ class KDGrid:
         assert q.size == N.MLP_PARAMS
         N.check(self._lib.mdas_learned_set_params(self._h, _ptr(q)), "learned_set_params")
 
+    def LearnedPredMax(self) -> float:
+        """The largest priority the last learned update used."""
+        v = C.c_float()
+        N.check(self._lib.mdas_learned_pred_max(self._h, C.byref(v)), "learned_pred_max")
+        return v.value
+
     def LearnedPredictions(self):
         import torch
         n = self.GetNumberOfNodes()

@@ -222,6 +222,28 @@ def test_incremental_predictions_from_error_rows(cuda):
     assert torch.equal(pred[idx], again[idx])
 
 
+@pytest.mark.parametrize("tolerance", [0.05, 1.0e6])
+def test_pred_max_is_the_max_over_every_leaf(cuda, tolerance):
+    """The largest priority of an incremental update (the kept leaves' maximum
+    from the adaptive pass, the split children's from their predictions) equals
+    the maximum over all current predictions, pass after pass, whichever
+    acceptance the judge picked."""
+    torch = cuda
+    g, sc = _grid(torch, seed=17)
+    g.LearnedEnable(seed=5, tolerance=tolerance)
+    g.InitialSampling()
+    sc.evaluate(g, 0, g.GetNumberOfSamples())
+    for k in range(8):
+        g.ComputeErrors()
+        g.LearnedUpdate()              # every leaf first, then the split children only
+        pred = g.LearnedPredictions()
+        assert g.LearnedPredMax() == float(pred.max()), k
+        g.AdaptiveSampling()
+        a, b = g.GetNumberOfSamples(), g.GetNewSamples()
+        sc.evaluate(g, a - b, b)
+    assert g.LearnedStats()["judged"] == 8
+
+
 def test_true_errors_match_oracle_integrand(cuda):
     torch = cuda
     from oracle import pyoracle as O
