@@ -43,20 +43,23 @@ constexpr int SM_W2 = 22528;     // 64 x 64 BF16 (B of layer 2: n = output, k = 
 constexpr int SM_W2T = 30720;    // 64 x 64 BF16 (B of dH1: n = input, k = output)
 constexpr int SM_VEC = 38912;    // b1, b2, w3 (64 floats each), b3
 constexpr int SM_BAR = 39744;    // mbarrier (8 B), TMEM address slot (4 B)
-constexpr int SM_FWD = 39808;    // end of what the forward needs
+// b1 and b2 as 16 chunks of 4 columns each, every chunk one core matrix of
+// 8 identical 16-byte rows: the sources of the accumulators' bias copies
+constexpr int SM_BIAS = 39808;
+constexpr int SM_FWD = SM_BIAS + 2 * 16 * 128;  // end of what the forward needs
 // training only
-constexpr int SM_Z2F = 39936;                    // dZ2, FP32 [128][65]
+constexpr int SM_Z2F = 44032;                    // dZ2, FP32 [128][65]
 constexpr int SM_D = SM_Z2F + kRows * 65 * 4;    // dZ2, BF16 core matrices (A of dH1)
 constexpr int SM_Z1F = SM_D + kRows * kH * 2;    // dZ1, FP32 [128][65]
 constexpr int SM_G = SM_Z1F + kRows * 65 * 4;    // per-CTA gradient, FP32 [MDAS_MLP_PARAMS]
 constexpr int SM_RED = SM_G + ((MDAS_MLP_PARAMS * 4 + 127) / 128) * 128;  // [3][4 warps][64] partial sums
 constexpr int SM_TRAIN = SM_RED + 3 * 4 * kH * 4;
-constexpr int kFwdSmem = 40960 + 1024;           // also bounds residency: <= 5 CTAs x 64 TMEM columns per SM
+constexpr int kFwdSmem = SM_FWD + 1024;          // (+ alignment of the base) <= 5 CTAs x 64 TMEM columns per SM
 constexpr int kTrainSmem = SM_TRAIN + 1024;
 
 static_assert(SM_W2T + kH * kH * 2 == SM_VEC, "map");
 static_assert(SM_VEC + (3 * kH + 4) * 4 <= SM_BAR, "map");
-static_assert(SM_FWD <= SM_Z2F, "map");
+static_assert(SM_FWD <= SM_Z2F && SM_BIAS >= SM_BAR + 16 && SM_BIAS % 128 == 0, "map");
 
 // ---- PTX wrappers ---------------------------------------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -112,6 +115,12 @@ __device__ __forceinline__ void mma_bf16_id(uint32_t d, uint64_t a, uint64_t b, 
 }
 __device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t accumulate) {
     mma_bf16_id(d, a, b, kIdesc, accumulate);
+}
+// A 32-row x 128-bit matrix from shared memory into the tensor-memory columns
+// taddr .. taddr + 3 of all four 32-lane quarters (asynchronous; ordered with
+// the issuing thread's MMAs).
+__device__ __forceinline__ void tmem_cp_32x128b_x4(uint32_t taddr, uint64_t sdesc) {
+    asm volatile("tcgen05.cp.cta_group::1.32x128b.warpx4 [%0], %1;" ::"r"(taddr), "l"(sdesc) : "memory");
 }
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
@@ -194,7 +203,8 @@ __device__ __forceinline__ uint8_t* aligned_smem() {
     return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dyn) + 1023) & ~(uintptr_t)1023);
 }
 
-// weights: W1, W2, W2^T tiles and the vectors (Packed keeps them contiguous)
+// weights: W1, W2, W2^T tiles and the vectors (Packed keeps them contiguous),
+// and the bias chunks (row r of chunk j of b: b[4j .. 4j + 3], every r)
 __device__ __forceinline__ void copy_weights(uint8_t* sm, const Packed* w) {
     const uint4* src = reinterpret_cast<const uint4*>(w);
     uint4* dst = reinterpret_cast<uint4*>(sm + SM_W1);
@@ -202,6 +212,11 @@ __device__ __forceinline__ void copy_weights(uint8_t* sm, const Packed* w) {
     static_assert(sizeof(Packed) % 16 == 0, "Packed is copied in 16-byte pieces");
     static_assert(SM_W1 + (int)sizeof(Packed) <= SM_BAR, "Packed fits before the barrier");
     for (int i = threadIdx.x; i < n16; i += kThreads) dst[i] = src[i];
+    uint4* bias = reinterpret_cast<uint4*>(sm + SM_BIAS);
+    for (int i = threadIdx.x; i < 2 * 16 * 8; i += kThreads) {  // (layer, chunk, row)
+        const float* b = (i >> 7) ? w->b2 : w->b1;
+        bias[i] = reinterpret_cast<const uint4*>(b)[(i >> 3) & 15];
+    }
 }
 
 // cols: tensor-memory columns of the CTA (a power of 2, >= 32)
@@ -277,17 +292,22 @@ __device__ __forceinline__ void tmem_row(const Ctx& c, float (&acc)[kH]) {
 }
 
 // Issue `steps` MMAs over K (16 each) of A at aOff (KB K-blocks) x B at bOff
-// (after the CTA's shared-memory writes); mma_wait completes them.
-__device__ __forceinline__ void mma_issue(Ctx& c, int aOff, int bOff, int KB, int steps) {
+// (after the CTA's shared-memory writes); mma_wait completes them.  biasOff >=
+// 0: the accumulators start from that bias (its 16 chunks copied into the 64
+// columns first; a chunk's descriptor has zero strides, so its one 8-row core
+// matrix stands for all 32 rows), else from zero.
+__device__ __forceinline__ void mma_issue(Ctx& c, int aOff, int bOff, int KB, int steps, int biasOff = -1) {
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     if (threadIdx.x == 0) {
         tc_fence_after();
+        if (biasOff >= 0)
+            for (int j = 0; j < kH / 4; ++j) tmem_cp_32x128b_x4(c.tmem + 4 * j, smem_desc(c.base + biasOff + 128 * j, 0, 0));
         const uint32_t sbo = (uint32_t)KB * 128u;
         for (int s = 0; s < steps; ++s)
             mma_bf16(c.tmem, smem_desc(c.base + aOff + 256 * s, 128, sbo), smem_desc(c.base + bOff + 256 * s, 128, sbo),
-                     s > 0 ? 1u : 0u);
+                     s > 0 || biasOff >= 0 ? 1u : 0u);
         mma_commit(c.bar);
     }
 }
@@ -301,25 +321,23 @@ __device__ __forceinline__ void run_mma(Ctx& c, int aOff, int bOff, int KB, int 
 // z2 = the layer-2 pre-activations (b2 added).  during1() and during2() run
 // while layer 1's and layer 2's MMAs execute (global loads for the next tile
 // into registers; they touch neither the operand tiles nor tensor memory).
+// The biases enter as the accumulators' initial values (copied into tensor
+// memory ahead of each layer's MMAs).
 template <typename During1, typename During2>
 __device__ __forceinline__ void tile_forward(Ctx& c, float (&z2)[kH], During1 during1, During2 during2) {
-    const float* b1 = reinterpret_cast<const float*>(c.sm + SM_VEC);
-    const float* b2 = b1 + kH;
-    mma_issue(c, SM_X, SM_W1, 2, 1);
+    mma_issue(c, SM_X, SM_W1, 2, 1, SM_BIAS);
     during1();
     mma_wait(c);
     float acc[kH];
     tmem_row(c, acc);
 #pragma unroll
-    for (int i = 0; i < kH; ++i) acc[i] = fmaxf(acc[i] + b1[i], 0.0f);
+    for (int i = 0; i < kH; ++i) acc[i] = fmaxf(acc[i], 0.0f);
 #pragma unroll
     for (int kb = 0; kb < kH / 8; ++kb) st_row8(c.sm + SM_H, threadIdx.x, kb, 8, acc + 8 * kb);
-    mma_issue(c, SM_H, SM_W2, 8, kH / 16);
+    mma_issue(c, SM_H, SM_W2, 8, kH / 16, SM_BIAS + 16 * 128);
     during2();
     mma_wait(c);
     tmem_row(c, z2);
-#pragma unroll
-    for (int i = 0; i < kH; ++i) z2[i] += b2[i];
 }
 
 __device__ __forceinline__ void tile_forward(Ctx& c, float (&z2)[kH]) {
@@ -398,12 +416,12 @@ __device__ __forceinline__ void load_raw(const float* __restrict__ row, float (&
     }
 }
 
-// The errors of the leaf's slot neighbours (slot -2, -1, +1, +2; the leaf's own
-// where a neighbour does not exist).
-__device__ __forceinline__ void nbr_errors(const MdasDeviceGrid& g, int leaf, int L, float e0, float (&ne)[4]) {
+// The errors of the leaf's slot neighbours (slot -2, -1, +1, +2; a NaN where a
+// neighbour does not exist: feats_of_raw then takes the leaf's own error).
+__device__ __forceinline__ void nbr_errors(const MdasDeviceGrid& g, int leaf, int L, float (&ne)[4]) {
     const int nbr[4] = {leaf - 2, leaf - 1, leaf + 1, leaf + 2};
 #pragma unroll
-    for (int q = 0; q < 4; ++q) ne[q] = nbr[q] >= 0 && nbr[q] < L ? g.errors[nbr[q]] : e0;
+    for (int q = 0; q < 4; ++q) ne[q] = nbr[q] >= 0 && nbr[q] < L ? g.errors[nbr[q]] : __int_as_float(0x7fffffff);
 }
 
 // Features from the raw inputs and the neighbours' errors.
@@ -434,14 +452,14 @@ __device__ void feats_of_raw(const MdasDeviceGrid& g, const float (&raw)[MDAS_RA
     f[10] = log2_err(raw[11]);
     f[11] = depth * (1.0f / 32.0f);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) f[12 + q] = log2_err(ne[q]);
+    for (int q = 0; q < 4; ++q) f[12 + q] = log2_err(ne[q] != ne[q] ? raw[11] : ne[q]);
 }
 
 template <int D>
 __device__ void leaf_feats(const MdasDeviceGrid& g, int leaf, int L, float (&f)[kIn], float* err) {
     float raw[MDAS_RAW_FLOATS], ne[4];
     leaf_raw<D>(g, leaf, raw);
-    nbr_errors(g, leaf, L, raw[11], ne);
+    nbr_errors(g, leaf, L, ne);
     feats_of_raw<D>(g, raw, ne, f);
     if (err) *err = raw[11];
 }
@@ -497,42 +515,44 @@ __global__ void __launch_bounds__(kThreads, 4) k_predict_leaves(MdasDeviceGrid g
     const int tiles = (rows + kRows - 1) / kRows;
     auto leaf_of = [&](int r) { return !dirty ? r : (r < newL ? g.dirty[r] : (L - newL) + (r - newL)); };
     if (rows_raw) {
-        // The rows of the errors pass: the next tile's row and leaf index are
-        // loaded while this tile's layer-1 MMA runs, the errors of that leaf's
-        // neighbours while its layer-2 MMA runs, so a tile's inputs are at hand
-        // when its features are formed.
+        // The rows of the errors pass.  While a tile's layer-1 MMA runs, the
+        // next tile's row and its neighbours' errors are loaded (that leaf's
+        // index came a tile earlier) and the index of the tile after it, so
+        // every load has a whole tile's work to arrive.
+        const int G = gridDim.x;
         int tile = blockIdx.x;
         int r = tile * kRows + threadIdx.x;
         float raw[MDAS_RAW_FLOATS], ne[4];
-        int leaf = 0;
+        int leaf = 0, leafNext = 0;
         if (tile < tiles && r < rows) {
             load_raw(g.featRaw + (size_t)r * MDAS_RAW_FLOATS, raw);
             leaf = leaf_of(r);
-            nbr_errors(g, leaf, L, raw[11], ne);
+            nbr_errors(g, leaf, L, ne);
         }
-        for (; tile < tiles; tile += gridDim.x) {
+        if (tile + G < tiles && r + G * kRows < rows) leafNext = leaf_of(r + G * kRows);
+        for (; tile < tiles; tile += G) {
             float f[kIn];
             if (r < rows) feats_of_raw<D>(g, raw, ne, f);
             else
 #pragma unroll
                 for (int i = 0; i < kIn; ++i) f[i] = 0.0f;
             put_features(c, f);
-            const int rNext = (tile + gridDim.x) * kRows + threadIdx.x;
-            const bool more = tile + gridDim.x < tiles && rNext < rows;
+            const int rNext = r + G * kRows, rNext2 = rNext + G * kRows;
+            const bool more = tile + G < tiles && rNext < rows;
+            const bool more2 = tile + 2 * G < tiles && rNext2 < rows;
             float rawNext[MDAS_RAW_FLOATS], neNext[4];
-            int leafNext = 0;
+            int leafNext2 = 0;
             float z2[kH];
             tile_forward(
                 c, z2,
                 [&] {
                     if (more) {
                         load_raw(g.featRaw + (size_t)rNext * MDAS_RAW_FLOATS, rawNext);
-                        leafNext = leaf_of(rNext);
+                        nbr_errors(g, leafNext, L, neNext);
                     }
+                    if (more2) leafNext2 = leaf_of(rNext2);
                 },
-                [&] {
-                    if (more) nbr_errors(g, leafNext, L, rawNext[11], neNext);
-                });
+                [] {});
             const float p = head(c, z2);
             if (r < rows) {
                 pred[leaf] = f[10] + p;
@@ -544,6 +564,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_predict_leaves(MdasDeviceGrid g
 #pragma unroll
                 for (int q = 0; q < 4; ++q) ne[q] = neNext[q];
                 leaf = leafNext;
+                leafNext = leafNext2;
             }
             r = rNext;
         }
@@ -561,7 +582,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_predict_leaves(MdasDeviceGrid g
         if (r < rows) {
             float raw[MDAS_RAW_FLOATS], ne[4];
             leaf_raw<D>(g, leaf, raw);
-            nbr_errors(g, leaf, L, raw[11], ne);
+            nbr_errors(g, leaf, L, ne);
             feats_of_raw<D>(g, raw, ne, f);
         } else
 #pragma unroll
@@ -633,7 +654,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_batch_predict(const MdasBatchIm
             float raw[MDAS_RAW_FLOATS], ne[4];  // the batched errors pass's row, or gathered
             if (dirty && g.featRaw) load_raw(g.featRaw + (size_t)r * MDAS_RAW_FLOATS, raw);
             else leaf_raw<D>(g, leaf, raw);
-            nbr_errors(g, leaf, L, raw[11], ne);
+            nbr_errors(g, leaf, L, ne);
             feats_of_raw<D>(g, raw, ne, f);
         } else
 #pragma unroll
