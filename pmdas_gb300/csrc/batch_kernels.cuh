@@ -265,8 +265,9 @@ __global__ void __launch_bounds__(256) k_batch_errors(const MdasBatchImage* __re
 }
 
 // ---- adaptive pass: decide
-template <int D, int K>
-__global__ void __launch_bounds__(256) k_batch_decide(const MdasBatchImage* __restrict__ imgs, int n) {
+// LEARNED: some image of the batch is learned (else the lean plain kernel).
+template <int D, int K, bool LEARNED>
+__global__ void __launch_bounds__(256, 3) k_batch_decide(const MdasBatchImage* __restrict__ imgs, int n) {
     pdl_launch_dependents();
     __shared__ int s_pre[MDAS_MAX_BATCH + 1];
     __shared__ unsigned s_warp[8];
@@ -281,15 +282,17 @@ __global__ void __launch_bounds__(256) k_batch_decide(const MdasBatchImage* __re
         const float gError = __uint_as_float(g.counts->gerr);
         float keptMax = 0.0f;
         unsigned gathered = 0, keptPrio = 0;
-        decide_tile<D, K>(g, t - s_pre[i], L, gError, imgs[i].jumpA, imgs[i].jumpC, s_warp, keptMax, gathered,
-                          keptPrio);
+        decide_tile<D, K, LEARNED>(g, t - s_pre[i], L, gError, imgs[i].jumpA, imgs[i].jumpC, s_warp, keptMax,
+                                   gathered, keptPrio);
         const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(keptMax));
         const unsigned c = __reduce_add_sync(0xffffffffu, gathered);
-        const unsigned kp = __reduce_max_sync(0xffffffffu, keptPrio);
         if ((threadIdx.x & 31) == 0) {
             if (m) atomicMax(&g.counts->gerrNext, m);
             if (c) atomicAdd(&g.counts->gathered, c);
-            if (kp) atomicMax(&g.learned->keptMax, kp);
+        }
+        if constexpr (LEARNED) {
+            const unsigned kp = __reduce_max_sync(0xffffffffu, keptPrio);
+            if ((threadIdx.x & 31) == 0 && kp) atomicMax(&g.learned->keptMax, kp);
         }
     }
 }
@@ -414,11 +417,16 @@ cudaError_t batch_learned_judge(const MdasBatchImage* imgs, int n, int grid, cud
 }
 
 // K: leaves per thread of decide (4 or 8); every image of the group has tileK == K.
-cudaError_t batch_decide(const MdasBatchImage* imgs, int n, int D, int K, int grid, cudaStream_t s) {
-    if (K == 4) {
-        MDAS_BATCH_SWITCH_D(D, (k_batch_decide<DD, 4><<<grid, 256, 0, s>>>(imgs, n)));
+// learned: some image of the batch takes the learned acceptance.
+cudaError_t batch_decide(const MdasBatchImage* imgs, int n, int D, int K, bool learned, int grid, cudaStream_t s) {
+    if (learned && K == 4) {
+        MDAS_BATCH_SWITCH_D(D, (k_batch_decide<DD, 4, true><<<grid, 256, 0, s>>>(imgs, n)));
+    } else if (learned) {
+        MDAS_BATCH_SWITCH_D(D, (k_batch_decide<DD, 8, true><<<grid, 256, 0, s>>>(imgs, n)));
+    } else if (K == 4) {
+        MDAS_BATCH_SWITCH_D(D, (k_batch_decide<DD, 4, false><<<grid, 256, 0, s>>>(imgs, n)));
     } else {
-        MDAS_BATCH_SWITCH_D(D, (k_batch_decide<DD, 8><<<grid, 256, 0, s>>>(imgs, n)));
+        MDAS_BATCH_SWITCH_D(D, (k_batch_decide<DD, 8, false><<<grid, 256, 0, s>>>(imgs, n)));
     }
     return cudaGetLastError();
 }

@@ -1125,7 +1125,8 @@ cudaError_t enqueue_batch_body(mdas_batch* b, cudaGraphConditionalHandle handle,
     if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_reset, b->d_imgs, b->n, 1, s);
     for (const auto& gr : b->groups)
         if (e == cudaSuccess)
-            e = MDAS_ARITH_CALL(b, batch_decide, b->d_imgs + gr.offset, gr.count, gr.D, b->tileK, gDec, s);
+            e = MDAS_ARITH_CALL(b, batch_decide, b->d_imgs + gr.offset, gr.count, gr.D, b->tileK, b->anyLearned, gDec,
+                                s);
     if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_scan, b->d_imgs, b->n, s);
     for (const auto& gr : b->groups)
         if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_place, b->d_imgs + gr.offset, gr.count, gr.D, gPl, s);

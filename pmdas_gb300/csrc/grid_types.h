@@ -149,7 +149,8 @@ struct MdasBatchImage {
     cudaError_t batch_set_counts(const MdasBatchImage* imgs, int n, cudaStream_t s);                         \
     cudaError_t batch_errors(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s);            \
     cudaError_t batch_reset(const MdasBatchImage* imgs, int n, int which, cudaStream_t s);                   \
-    cudaError_t batch_decide(const MdasBatchImage* imgs, int n, int D, int K, int grid, cudaStream_t s);     \
+    cudaError_t batch_decide(const MdasBatchImage* imgs, int n, int D, int K, bool learned, int grid,        \
+                             cudaStream_t s);                                                                 \
     cudaError_t batch_scan(const MdasBatchImage* imgs, int n, cudaStream_t s);                               \
     cudaError_t batch_place(const MdasBatchImage* imgs, int n, int D, int grid, cudaStream_t s);             \
     cudaError_t batch_condition(const MdasBatchImage* imgs, int n, cudaGraphConditionalHandle h,             \

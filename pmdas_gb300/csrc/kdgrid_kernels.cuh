@@ -478,9 +478,10 @@ __device__ __forceinline__ float learned_ratio(const MdasDeviceGrid& g, int leaf
 // counts and its compacted accepted list (shared by the single-image and the
 // batched kernels).
 // K: leaves per thread (4 or 8): a tile is 256 K leaves (g.tileK must be K).
-// keptPrio: the order bits of the largest priority of the leaves not split
-// (learned mode, whichever acceptance the pass takes).
-template <int D, int K>
+// LEARNED: the grid has priorities (g.priority set; a plain grid's kernels
+// carry none of their code).  keptPrio: the order bits of the largest priority
+// of the leaves not split (whichever acceptance the pass takes).
+template <int D, int K, bool LEARNED>
 __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, int L, float gError, unsigned jumpA,
                                             unsigned jumpC, unsigned* s_warp, float& keptMax, unsigned& gathered,
                                             unsigned& keptPrio) {
@@ -492,7 +493,7 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
     const int i0 = tile * TILE + threadIdx.x * K;
     const bool full = i0 + K <= L;
     // learned acceptance unless the judge sent this pass back to the plain one
-    const bool havePrio = g.priority != nullptr;
+    const bool havePrio = LEARNED && g.priority != nullptr;
     const bool learned = havePrio && !g.learned->usePlain;
     float err[K], pr[K];
     unsigned sd[K];
@@ -645,7 +646,7 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
     __syncthreads();  // s_warp is reused by the next tile
 }
 
-template <int D, int K>
+template <int D, int K, bool LEARNED>
 __global__ void __launch_bounds__(256) k_adaptive_decide(MdasDeviceGrid g, unsigned jumpA, unsigned jumpC) {
     pdl_launch_dependents();
     __shared__ unsigned s_warp[8];
@@ -656,14 +657,16 @@ __global__ void __launch_bounds__(256) k_adaptive_decide(MdasDeviceGrid g, unsig
     unsigned gathered = 0;  // sample coordinates read
     unsigned keptPrio = 0;  // max priority of those leaves (learned mode)
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
-        decide_tile<D, K>(g, tile, L, gError, jumpA, jumpC, s_warp, keptMax, gathered, keptPrio);
+        decide_tile<D, K, LEARNED>(g, tile, L, gError, jumpA, jumpC, s_warp, keptMax, gathered, keptPrio);
     unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(keptMax));
     unsigned c = __reduce_add_sync(0xffffffffu, gathered);
-    unsigned kp = __reduce_max_sync(0xffffffffu, keptPrio);
     if ((threadIdx.x & 31) == 0) {
         if (m) atomicMax(&g.counts->gerrNext, m);
         if (c) atomicAdd(&g.counts->gathered, c);
-        if (kp) atomicMax(&g.learned->keptMax, kp);
+    }
+    if constexpr (LEARNED) {
+        const unsigned kp = __reduce_max_sync(0xffffffffu, keptPrio);
+        if ((threadIdx.x & 31) == 0 && kp) atomicMax(&g.learned->keptMax, kp);
     }
 }
 
@@ -1312,10 +1315,14 @@ cudaError_t adaptive_sampling(const MdasDeviceGrid& g, int gridDecide, int gridP
     if (e != cudaSuccess) return e;
     unsigned A, C;
     lcg_jump((unsigned)(g.candidatesNum * g.D), &A, &C);
-    if (g.tileK == 4) {
-        MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD, 4><<<gridDecide, 256, 0, s>>>(g, A, C)));
+    if (g.priority && g.tileK == 4) {
+        MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD, 4, true><<<gridDecide, 256, 0, s>>>(g, A, C)));
+    } else if (g.priority) {
+        MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD, 8, true><<<gridDecide, 256, 0, s>>>(g, A, C)));
+    } else if (g.tileK == 4) {
+        MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD, 4, false><<<gridDecide, 256, 0, s>>>(g, A, C)));
     } else {
-        MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD, 8><<<gridDecide, 256, 0, s>>>(g, A, C)));
+        MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD, 8, false><<<gridDecide, 256, 0, s>>>(g, A, C)));
     }
     e = launch_pdl(k_adaptive_scan, 1, 1024, s, g);
     if (e != cudaSuccess) return e;
@@ -1394,7 +1401,8 @@ int max_blocks_per_sm(int D, int which) {
             MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_integrate<DD>, 256, 0)));
             break;
         case MDAS_K_DECIDE:
-            MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adaptive_decide<DD, 8>, 256, 0)));
+            MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adaptive_decide<DD, 8, false>,
+                                                                                 256, 0)));
             break;
         default:
             MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_initial_sampling<DD>, 256, 0)));
