@@ -70,6 +70,8 @@ def parse_args():
                     help="with --learned-only: the spp ladder (default: the comparison's own)")
     ap.add_argument("--batch-images", type=int, default=64,
                     help="batch64: render only the first N images of the set (a smaller case for profilers)")
+    ap.add_argument("--batch-learned", action="store_true",
+                    help="batch64: every image with the learned acceptance (the mbdof1080 weights)")
     ap.add_argument("--stepped", action="store_true",
                     help="batch64: the pass loop on the host (every kernel visible to a profiler), default tuning")
     ap.add_argument("--ncu-traffic", default=None, metavar="CSV",
@@ -962,6 +964,12 @@ def run_batch(args, rank: int, world: int, local_rank: int) -> dict:
         scenes.append(P.Scene(wl.scene_kind, wl.scene_seed, wl.scene_count, wl.scaleX, wl.scaleY, wl.width,
                               wl.height))
         pix.append(torch.zeros(wl.height, wl.width, 4, device="cuda"))
+    if args.batch_learned:
+        params, _ = _weights("mbdof1080")
+        if params is None:
+            raise SystemExit("no trained weights for mbdof1080")
+        for g in grids:
+            g.LearnedEnable(params=params)
     batch = P.Batch(grids, scenes, [w.budget for w in wls], pix, [w.width for w in wls], [w.height for w in wls])
     if args.stepped:  # default tuning, host-driven pass loop
         best, tile, tuned_ms, evaluated = [4, 4, 4, 8], 2048, None, 0
@@ -1010,7 +1018,8 @@ def run_batch(args, rank: int, world: int, local_rank: int) -> dict:
                    "total_samples": samples, "timing": "whole batched render incl. integrand, CUDA events",
                    "autotuned_ctas_per_sm": best, "autotuned_decide_tile_leaves": tile,
                    "autotune_candidates": evaluated, "autotune_ms": round(tuned_ms, 3) if tuned_ms else None,
-                   "loop": "host-stepped passes (profiling)" if args.stepped else "device-side (CUDA graph)"},
+                   "loop": "host-stepped passes (profiling)" if args.stepped else "device-side (CUDA graph)",
+                   "acceptance": "learned (mbdof1080 weights)" if args.batch_learned else "plain"},
         "per_image_ms": round(ms / len(wls), 4),
         "sequential_single_image_ms": round(t_single, 3),
         "batch_speedup_vs_sequential": round(t_single / ms, 3),

@@ -158,8 +158,10 @@ __device__ __forceinline__ void flush_learned(MdasLearnedStats* st, double ul, d
 __global__ void __launch_bounds__(256) k_batch_learned_reduce(const MdasBatchImage* __restrict__ imgs, int n) {
     __shared__ int s_pre[MDAS_MAX_BATCH + 1];
     __shared__ unsigned s_warp[8];
+    // chunks of 1024 leaves: four per thread, 16-byte loads of errors, seeds and
+    // priorities (all 256-byte aligned)
     const int total = batch_prefix(n, s_pre, s_warp, [&](int i) {
-        return imgs[i].mlp && imgs[i].g.counts->active ? ceil_div(imgs[i].g.counts->L, 256) : 0;
+        return imgs[i].mlp && imgs[i].g.counts->active ? ceil_div(imgs[i].g.counts->L, 1024) : 0;
     });
     int cur = -1;  // the image the block's partial results belong to (uniform across the block)
     KahanF ul, up;
@@ -172,16 +174,38 @@ __global__ void __launch_bounds__(256) k_batch_learned_reduce(const MdasBatchIma
             up = KahanF();
         }
         const MdasDeviceGrid& g = imgs[img].g;
-        const int i = (ch - s_pre[img]) * 256 + threadIdx.x;
-        if (i >= g.counts->L) continue;
+        const int L = g.counts->L;
+        const int i0 = (ch - s_pre[img]) * 1024 + 4 * (int)threadIdx.x;
+        if (i0 >= L) continue;
         const float gError = __uint_as_float(g.counts->gerr);
         const float predMax = mdas_float_unorder(g.learned->predMax);
-        const float e = g.errors[i];
-        unsigned seed = g.seeds[i];
-        if (seed == 0) seed = tea4((unsigned)i, 0);
-        const float r = rnd(seed);
-        if (!(mdas_pow(e / gError, g.alpha) >= r)) up.add(e);
-        if (!(mdas_pow(learned_ratio(g, i, predMax), g.alpha) >= r)) ul.add(e);
+        float e[4], p[4];
+        unsigned sd[4];
+        const int m = L - i0 < 4 ? L - i0 : 4;
+        if (m == 4) {
+            const float4 e4 = *reinterpret_cast<const float4*>(g.errors + i0);
+            const uint4 s4 = *reinterpret_cast<const uint4*>(g.seeds + i0);
+            const float4 p4 = *reinterpret_cast<const float4*>(g.priority + i0);
+            e[0] = e4.x; e[1] = e4.y; e[2] = e4.z; e[3] = e4.w;
+            sd[0] = s4.x; sd[1] = s4.y; sd[2] = s4.z; sd[3] = s4.w;
+            p[0] = p4.x; p[1] = p4.y; p[2] = p4.z; p[3] = p4.w;
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                e[j] = j < m ? g.errors[i0 + j] : 0.0f;
+                sd[j] = j < m ? g.seeds[i0 + j] : 0u;
+                p[j] = j < m ? g.priority[i0 + j] : 0.0f;
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (j >= m) break;
+            unsigned seed = sd[j];
+            if (seed == 0) seed = tea4((unsigned)(i0 + j), 0);
+            const float r = rnd(seed);
+            if (!(mdas_pow(e[j] / gError, g.alpha) >= r)) up.add(e[j]);
+            if (!(mdas_pow(learned_ratio_of(p[j], predMax, g.priorityScale), g.alpha) >= r)) ul.add(e[j]);
+        }
     }
     if (cur >= 0) flush_learned(imgs[cur].g.learned, ul.value(), up.value());
 }

@@ -470,9 +470,6 @@ __device__ __forceinline__ unsigned acc_pack(unsigned local, unsigned splitRank,
 __device__ __forceinline__ float learned_ratio_of(float priority, float predMax, float scale) {
     return exp2f((priority - predMax) * scale);
 }
-__device__ __forceinline__ float learned_ratio(const MdasDeviceGrid& g, int leaf, float predMax) {
-    return learned_ratio_of(g.priority[leaf], predMax, g.priorityScale);
-}
 
 // decide, one tile: acceptance of the tile's leaves, final seeds, the tile's
 // counts and its compacted accepted list (shared by the single-image and the

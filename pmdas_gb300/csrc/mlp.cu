@@ -627,14 +627,46 @@ __global__ void __launch_bounds__(kThreads, 4) k_batch_predict(const MdasBatchIm
     const Packed* loaded = nullptr;
     Ctx c;
     ctx_open(c, nullptr, status);
-    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    // A tile: its image, its row of that image's rows, and whether those rows
+    // come from the errors pass (split children after the first pass).
+    struct TileRows {
+        int img, r, rows, L, leaf;
+        bool fromRows;
+    };
+    auto tile_rows = [&](int t) {
         int lo = 0, hi = n - 1;  // the image whose tile range holds t
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
             if (s_pre[mid] <= t) lo = mid;
             else hi = mid - 1;
         }
-        const MdasBatchImage& im = imgs[lo];
+        const MdasDeviceGrid& g = imgs[lo].g;
+        TileRows tr;
+        tr.img = lo;
+        tr.L = g.counts->L;
+        const bool dirty = g.counts->passes > 0;
+        const int newL = g.counts->newL;
+        tr.rows = dirty ? 2 * newL : tr.L;
+        tr.r = (t - s_pre[lo]) * kRows + threadIdx.x;
+        tr.leaf = tr.r >= tr.rows ? 0 : !dirty ? tr.r : (tr.r < newL ? g.dirty[tr.r] : (tr.L - newL) + (tr.r - newL));
+        tr.fromRows = dirty && g.featRaw != nullptr;
+        return tr;
+    };
+    // the inputs of the CTA's current tile: rows are loaded while the previous
+    // tile's MMAs run (the leaf index and row under layer 1, the neighbours'
+    // errors under layer 2); gathered rows (an image's first pass) at the tile
+    float raw[MDAS_RAW_FLOATS], ne[4];
+    TileRows cur;
+    if ((int)blockIdx.x < total) {
+        cur = tile_rows(blockIdx.x);
+        const MdasDeviceGrid& g = imgs[cur.img].g;
+        if (cur.fromRows && cur.r < cur.rows) {
+            load_raw(g.featRaw + (size_t)cur.r * MDAS_RAW_FLOATS, raw);
+            nbr_errors(g, cur.leaf, cur.L, ne);
+        }
+    }
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        const MdasBatchImage& im = imgs[cur.img];
         const Packed* w = reinterpret_cast<const Packed*>(im.mlp);
         if (w != loaded) {  // no MMA is in flight between tiles
             __syncthreads();
@@ -643,33 +675,50 @@ __global__ void __launch_bounds__(kThreads, 4) k_batch_predict(const MdasBatchIm
             loaded = w;
         }
         const MdasDeviceGrid& g = im.g;
-        const int L = g.counts->L;
-        const bool dirty = g.counts->passes > 0;
-        const int newL = g.counts->newL;
-        const int rows = dirty ? 2 * newL : L;
-        const int r = (t - s_pre[lo]) * kRows + threadIdx.x;
-        const int leaf = !dirty ? r : (r < newL ? g.dirty[r] : (L - newL) + (r - newL));
         float f[kIn];
-        if (r < rows) {
-            float raw[MDAS_RAW_FLOATS], ne[4];  // the batched errors pass's row, or gathered
-            if (dirty && g.featRaw) load_raw(g.featRaw + (size_t)r * MDAS_RAW_FLOATS, raw);
-            else leaf_raw<D>(g, leaf, raw);
-            nbr_errors(g, leaf, L, ne);
+        if (cur.r < cur.rows) {
+            if (!cur.fromRows) {
+                leaf_raw<D>(g, cur.leaf, raw);
+                nbr_errors(g, cur.leaf, cur.L, ne);
+            }
             feats_of_raw<D>(g, raw, ne, f);
         } else
 #pragma unroll
             for (int i = 0; i < kIn; ++i) f[i] = 0.0f;
         put_features(c, f);
+        const bool more = t + (int)gridDim.x < total;
+        TileRows nxt = cur;
+        float rawNext[MDAS_RAW_FLOATS], neNext[4];
         float z2[kH];
-        tile_forward(c, z2);
+        tile_forward(
+            c, z2,
+            [&] {
+                if (more) {
+                    nxt = tile_rows(t + gridDim.x);
+                    if (nxt.fromRows && nxt.r < nxt.rows)
+                        load_raw(imgs[nxt.img].g.featRaw + (size_t)nxt.r * MDAS_RAW_FLOATS, rawNext);
+                }
+            },
+            [&] {
+                if (more && nxt.fromRows && nxt.r < nxt.rows) nbr_errors(imgs[nxt.img].g, nxt.leaf, nxt.L, neNext);
+            });
         const float p = head(c, z2);
         unsigned best = 0u;
-        if (r < rows) {
-            const_cast<float*>(g.priority)[leaf] = f[10] + p;
+        if (cur.r < cur.rows) {
+            const_cast<float*>(g.priority)[cur.leaf] = f[10] + p;
             best = mdas_float_order(f[10] + p);
         }
         best = __reduce_max_sync(0xffffffffu, best);  // the tile is one image's
         if ((threadIdx.x & 31) == 0 && best) atomicMax(&g.learned->predMax, best);
+        if (more) {
+            if (nxt.fromRows && nxt.r < nxt.rows) {
+#pragma unroll
+                for (int i = 0; i < MDAS_RAW_FLOATS; ++i) raw[i] = rawNext[i];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) ne[q] = neNext[q];
+            }
+            cur = nxt;
+        }
     }
     ctx_close(c);
 }
