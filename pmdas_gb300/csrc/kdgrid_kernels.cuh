@@ -120,12 +120,6 @@ __device__ __forceinline__ void store_point(float* __restrict__ p, const float (
     }
 }
 
-// Fetch `bytes` (a multiple of 16) from the 16-byte aligned global address p
-// into L2: a bulk prefetch, issued by the thread and not waited on.
-__device__ __forceinline__ void l2_prefetch(const void* p, unsigned bytes) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
-
 // ---- leaf storage ------------------------------------------------------------------
 // nb:  NbLayout<D>::FLOATS floats per leaf (a multiple of 32 bytes; 128 bytes,
 //      one L2 line, at D = 4):
@@ -779,12 +773,41 @@ __device__ __forceinline__ PlaceLoc place_locate(const MdasDeviceGrid& g, int k,
 }
 
 // place, one accepted leaf (entry r of `tile`, whose prefix is `pre`, entry
-// word `e`): best candidate, append or split.  With `next` (may be null), once
-// this leaf's record loads are under way, it also locates entry kn (the leaf
-// this thread places next) and fetches that leaf's record into L2.
+// word `e`): best candidate, append or split.  The leaf's record is read from
+// its chunks staged in shared memory at srec, or from global memory when srec
+// is null.
+// 16-byte chunks of a leaf record that the adaptive pass reads (node, box, padding, private copy)
+template <int D>
+struct RecChunks {
+    static constexpr int C = (NbLayout<D>::SC + 4 * D + 3) / 4;
+    static constexpr int CS = C | 1;  // shared-memory stride in chunks: odd, so lanes' chunks hit distinct banks
+};
+
+// The record read from its chunks in shared memory.
+template <int D>
+__device__ __forceinline__ int4 rec_from_chunks(const float4* __restrict__ ch, float (&mn)[D], float (&mx)[D],
+                                                float (&scv)[4 * D]) {
+    constexpr int C = RecChunks<D>::C;
+    constexpr int SC = NbLayout<D>::SC;
+    float v[4 * C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        const float4 t = ch[c];
+        v[4 * c] = t.x; v[4 * c + 1] = t.y; v[4 * c + 2] = t.z; v[4 * c + 3] = t.w;
+    }
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+        mn[i] = v[4 + i];
+        mx[i] = v[4 + D + i];
+    }
+#pragma unroll
+    for (int k = 0; k < 4 * D; ++k) scv[k] = v[SC + k];
+    return make_int4(__float_as_int(v[0]), __float_as_int(v[1]), __float_as_int(v[2]), __float_as_int(v[3]));
+}
+
 template <int D>
 __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, int r, uint2 pre, uint2 e, int N,
-                                            int L, PlaceLoc* next = nullptr, int kn = 0, int ntiles = 0) {
+                                            int L, const float4* srec = nullptr) {
     constexpr int kMaxNodeSize = 4;
     const int TILE = 256 * g.tileK;
     constexpr int NB = NbLayout<D>::FLOATS;
@@ -797,13 +820,14 @@ __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, i
     float* nb = g.nb + (size_t)nodeIndex * NB;
     float* sc = leaf_copy<D>(g.nb, (size_t)nodeIndex);
     float mn[D], mx[D];
-    // the whole record (no hint: measured as fast as .L2::128B, faster than 64B or 256B)
-    int4 node = nb_load<D>(nb, mn, mx);
+    int4 node;
     float scv[4 * D];
-    ld_floats<4 * D>(sc, scv);
-    if (next) {
-        *next = place_locate(g, kn, ntiles);
-        l2_prefetch(g.nb + ((size_t)next->tile * TILE + (next->e.x & 0x7ffu)) * NB, NB * 4);
+    if (srec) {
+        node = rec_from_chunks<D>(srec, mn, mx, scv);  // staged in shared memory by the warp
+    } else {
+        // the whole record (no hint: measured as fast as .L2::128B, faster than 64B or 256B)
+        node = nb_load<D>(nb, mn, mx);
+        ld_floats<4 * D>(sc, scv);
     }
     float samples[4][D];
 #pragma unroll
@@ -958,31 +982,125 @@ __device__ __forceinline__ void place_rank(const MdasDeviceGrid& g, int k, int N
     place_entry<D>(g, p.tile, p.r, p.pre, p.e, N, L);
 }
 
-// One thread per accepted leaf, in accepted-rank order.  Each thread finds
-// its next leaf's entry while it places the current one and fetches that
-// leaf's record into L2 (1 % faster than loading each record when its turn
-// comes).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// The warp's records of the leaves `leaf` (one per lane, -1: none) copied into
+// shared memory at srec (record of lane l at srec + l * CS chunks).
 template <int D>
-__global__ void __launch_bounds__(256, 4) k_adaptive_place(MdasDeviceGrid g) {
+__device__ __forceinline__ void stage_records(const float* __restrict__ nb, int leaf, float4* srec) {
+    constexpr int C = RecChunks<D>::C, CS = RecChunks<D>::CS, NB = NbLayout<D>::FLOATS;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int q = 0; q < C; ++q) {
+        const int idx = q * 32 + lane;
+        const int rr = idx / C, c = idx - rr * C;
+        const int src = __shfl_sync(0xffffffffu, leaf, rr);
+        if (src >= 0) cp_async16(srec + rr * CS + c, nb + (size_t)src * NB + 4 * c);
+    }
+}
+
+// The ranks kb + lane of a warp (kb a multiple of 32, so that all lie in one
+// 256-entry chunk): each lane's tile and the tile's prefix.  The warp reads the
+// prefixes of the 32 tiles from the chunk's first one in one coalesced load and
+// each lane searches them (5 shuffles); ranks beyond those 32 tiles walk on.
+// Every lane of the warp calls it; lanes with k >= accepted get a tile too
+// (unused).
+__device__ __forceinline__ void warp_locate(const MdasDeviceGrid& g, int kb, int k, int ntiles, int& tile,
+                                            uint2& pre) {
+    const int lane = threadIdx.x & 31;
+    const int t0 = g.chunkTile[kb >> 8];
+    const uint2 totals = make_uint2((unsigned)g.counts->newN, (unsigned)g.counts->newL);
+    const uint2 P = t0 + lane < ntiles ? g.tilePrefix[t0 + lane] : totals;
+    // largest j with P_j.x <= k (P_0.x <= kb <= k; P is non-decreasing in j)
+    int j = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+        const unsigned px = __shfl_sync(0xffffffffu, P.x, j + step);
+        if ((int)px <= k) j += step;
+    }
+    tile = t0 + j;
+    pre.x = __shfl_sync(0xffffffffu, P.x, j);
+    pre.y = __shfl_sync(0xffffffffu, P.y, j);
+    if (j == 31) {  // (only where 31 tiles in a row hold fewer than 32 accepted leaves)
+        while (tile + 1 < ntiles) {
+            const uint2 next = g.tilePrefix[tile + 1];
+            if ((int)next.x > k) break;
+            ++tile;
+            pre = next;
+        }
+    }
+}
+
+// One thread per accepted leaf, in accepted-rank order; each warp places 32
+// consecutive ranks per iteration, their records staged in shared memory:
+//   * every 16-byte copy instruction of the warp (cp.async) covers whole
+//     records (4 records of 128 bytes per instruction at D = 4) instead of one
+//     16-byte piece of 32 records;
+//   * double-buffered: while the warp places its current 32 leaves, the
+//     records of its next 32 are on their way into the other buffer;
+//   * a rank's tile comes from warp_locate (three dependent loads whatever the
+//     density of accepted leaves).
+// Three CTAs per SM at D <= 4 (two at D >= 5: 74-90 KB of buffers).  Measured
+// against one thread per leaf loading its record when its turn comes: adaptive
+// stage -4 % on dof1024, -18 % on mbdof1080.
+template <int D>
+__global__ void __launch_bounds__(256, D >= 5 ? 2 : 3) k_adaptive_place(MdasDeviceGrid g) {
+    constexpr int CS = RecChunks<D>::CS;
+    __shared__ __align__(16) float4 s_rec[2][8][32 * CS];
     pdl_wait();
     const int N = g.ctl->N0;
     const int L = g.ctl->L0;
     const int accepted = g.counts->newN;
-    const int ntiles = (L + 256 * g.tileK - 1) / (256 * g.tileK);
+    const int TILE = 256 * g.tileK;
+    const int ntiles = (L + TILE - 1) / TILE;
     const int stride = gridDim.x * 256;
-    int k = blockIdx.x * 256 + threadIdx.x;
-    if (k >= accepted) return;
-    PlaceLoc cur = place_locate(g, k, ntiles);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int kb = blockIdx.x * 256 + warp * 32;
+    if (kb >= accepted) return;
+    // the warp's ranks of one iteration, located: entry, tile, prefix
+    auto fetch = [&](int kbase, uint2& e, int& tile, uint2& pre) {
+        const int k = kbase + lane;
+        warp_locate(g, kbase, k, ntiles, tile, pre);
+        if (k < accepted) e = g.accepted[(size_t)tile * TILE + (k - (int)pre.x)];
+    };
+    uint2 e0 = make_uint2(0u, 0u), pre0;
+    int tile0;
+    fetch(kb, e0, tile0, pre0);
+    stage_records<D>(g.nb, kb + lane < accepted ? tile0 * TILE + (int)(e0.x & 0x7ffu) : -1, s_rec[0][warp]);
+    cp_async_commit();
+    int buf = 0;
     for (;;) {
-        const int kn = k + stride;
-        if (kn >= accepted) {
-            place_entry<D>(g, cur.tile, cur.r, cur.pre, cur.e, N, L);
-            break;
+        const int kn = kb + stride;
+        const bool more = kn < accepted;  // warp-uniform
+        uint2 e1 = make_uint2(0u, 0u), pre1;
+        int tile1 = 0;
+        if (more) {
+            fetch(kn, e1, tile1, pre1);
+            stage_records<D>(g.nb, kn + lane < accepted ? tile1 * TILE + (int)(e1.x & 0x7ffu) : -1,
+                             s_rec[buf ^ 1][warp]);
+            cp_async_commit();
+            cp_async_wait_group<1>();
+        } else {
+            cp_async_wait_group<0>();
         }
-        PlaceLoc nxt;
-        place_entry<D>(g, cur.tile, cur.r, cur.pre, cur.e, N, L, &nxt, kn, ntiles);
-        cur = nxt;
-        k = kn;
+        __syncwarp();
+        const int k = kb + lane;
+        if (k < accepted)
+            place_entry<D>(g, tile0, k - (int)pre0.x, pre0, e0, N, L, s_rec[buf][warp] + lane * CS);
+        __syncwarp();  // the buffer is refilled two iterations on
+        if (!more) break;
+        e0 = e1;
+        tile0 = tile1;
+        pre0 = pre1;
+        kb = kn;
+        buf ^= 1;
     }
 }
 
@@ -1356,6 +1474,19 @@ static void lcg_jump(unsigned n, unsigned* A, unsigned* C) {
     *C = c;
 }
 
+// The place kernel's shared-memory carveout: its double buffers take 56 KB per
+// CTA at D = 4, three CTAs per SM need the largest carveout.
+static cudaError_t place_prepare(int D) {
+    static bool done[7] = {};
+    if (D < 3 || D > 6) return cudaErrorInvalidValue;
+    if (done[D]) return cudaSuccess;
+    cudaError_t e = cudaSuccess;
+    MDAS_SWITCH_D(D, (e = cudaFuncSetAttribute(k_adaptive_place<DD>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                               (int)cudaSharedmemCarveoutMaxShared)));
+    if (e == cudaSuccess) done[D] = true;
+    return e;
+}
+
 cudaError_t adaptive_sampling(const MdasDeviceGrid& g, int gridDecide, int gridPlace, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(&g.counts->gathered, 0, 2 * sizeof(unsigned), s);  // + gerrNext
     if (e != cudaSuccess) return e;
@@ -1371,6 +1502,8 @@ cudaError_t adaptive_sampling(const MdasDeviceGrid& g, int gridDecide, int gridP
         MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD, 8, false><<<gridDecide, 256, 0, s>>>(g, A, C)));
     }
     e = launch_pdl(k_adaptive_scan, 1, 1024, s, g);
+    if (e != cudaSuccess) return e;
+    e = place_prepare(g.D);
     if (e != cudaSuccess) return e;
     MDAS_SWITCH_D(g.D, (e = launch_pdl(k_adaptive_place<DD>, gridPlace, 256, s, g)));
     if (e != cudaSuccess) return e;
@@ -1441,7 +1574,9 @@ int max_blocks_per_sm(int D, int which) {
                                                                                  0)));
             break;
         case MDAS_K_ADAPTIVE:
-            MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adaptive_place<DD>, 256, 0)));
+            e = place_prepare(D);
+            if (e == cudaSuccess)
+                MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adaptive_place<DD>, 256, 0)));
             break;
         case MDAS_K_INTEGRATE:
             MDAS_SWITCH_D(D, (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_integrate<DD>, 256, 0)));
