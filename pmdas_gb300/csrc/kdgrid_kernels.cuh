@@ -539,19 +539,43 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
     const float predMax = learned ? mdas_float_unorder(g.learned->predMax) : 0.0f;
     unsigned accMask = 0;
     unsigned seedAcc[K];
+    // the acceptance draw of leaf j (kdgrid.cu:323-326); seed: its stream, advanced
+    auto accept = [&](int j, unsigned& seed) {
+        if (!learned) return mdas_pow(err[j] / gError, g.alpha) >= rnd(seed);
+        return mdas_pow(learned_ratio_of(pr[j], predMax, g.priorityScale), g.alpha) >= rnd(seed);
+    };
+    // Almost always every leaf of the warp exists and has a drawn seed: that
+    // case takes a loop without the per-leaf tests (warp-uniform choice).
+    bool plain = full;
 #pragma unroll
-    for (int j = 0; j < K; ++j) {
-        const int leaf = i0 + j;
-        unsigned seed = sd[j];
-        if (seed == 0) seed = tea4((unsigned)leaf, 0);
-        bool a = false;
-        if (leaf < L) {
-            if (!learned) a = mdas_pow(err[j] / gError, g.alpha) >= rnd(seed);
-            else a = mdas_pow(learned_ratio_of(pr[j], predMax, g.priorityScale), g.alpha) >= rnd(seed);
+    for (int j = 0; j < K; ++j) plain = plain && sd[j] != 0u;
+    if (__all_sync(0xffffffffu, plain)) {
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            unsigned seed = sd[j];
+            const bool a = accept(j, seed);
+            seedAcc[j] = seed;
+            sd[j] = a ? jumpA * seed + jumpC : seed;  // the seed after the candidate draws
+            accMask |= (unsigned)a << j;
         }
-        seedAcc[j] = seed;
-        sd[j] = a ? jumpA * seed + jumpC : seed;  // the seed after the candidate draws
-        if (a) accMask |= 1u << j;
+    } else {
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            const int leaf = i0 + j;
+            unsigned seed = sd[j];
+            if (seed == 0) seed = tea4((unsigned)leaf, 0);
+            bool a = false;
+            if (leaf < L) a = accept(j, seed);
+            seedAcc[j] = seed;
+            sd[j] = a ? jumpA * seed + jumpC : seed;
+            if (a) accMask |= 1u << j;
+        }
+    }
+    unsigned validMask = (1u << K) - 1u;
+    if (!full) {
+        validMask = 0u;
+#pragma unroll
+        for (int j = 0; j < K; ++j) validMask |= (unsigned)(i0 + j < L) << j;
     }
     int cnt[K];
 #pragma unroll
@@ -560,11 +584,14 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
 #pragma unroll
     for (int j = 0; j < K; ++j) {
         gathered += (unsigned)cnt[j];
-        if (cnt[j] >= kMaxNodeSize) splitMask |= 1u << j;
-        if (i0 + j < L && !((splitMask >> j) & 1u)) {
-            keptMax = fmaxf(keptMax, err[j]);
-            if (havePrio) keptPrio = max(keptPrio, mdas_float_order(pr[j]));
-        }
+        splitMask |= (unsigned)(cnt[j] >= kMaxNodeSize) << j;
+    }
+    const unsigned keptMask = validMask & ~splitMask;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        // (errors are >= 0: a leaf not kept contributes 0)
+        keptMax = fmaxf(keptMax, ((keptMask >> j) & 1u) ? err[j] : 0.0f);
+        if (havePrio && ((keptMask >> j) & 1u)) keptPrio = max(keptPrio, mdas_float_order(pr[j]));
     }
     if (full) {
 #pragma unroll
@@ -636,20 +663,21 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
         uint2* acc = g.accepted + (size_t)tile * TILE;
 #pragma unroll
         for (int j = 0; j < K; ++j) {
-            if ((accMask >> j) & 1u) {
-                const unsigned sp = (splitMask >> j) & 1u;
-                acc[r] = make_uint2(acc_pack((unsigned)(threadIdx.x * K + j), rp, sp, (unsigned)cnt[j]), seedAcc[j]);
-                r++;
-                rp += sp;
-            }
+            const unsigned a = (accMask >> j) & 1u, sp = (splitMask >> j) & 1u;
+            if (a) acc[r] = make_uint2(acc_pack((unsigned)(threadIdx.x * K + j), rp, sp, (unsigned)cnt[j]), seedAcc[j]);
+            r += a;
+            rp += sp;
         }
     }
     if (threadIdx.x == 0) g.tileCounts[tile] = make_uint2(tileTotal & 0xffffu, tileTotal >> 16);
     __syncthreads();  // s_warp is reused by the next tile
 }
 
+// Plain decide at 4 CTAs per SM (63 registers; measured against 3 CTAs at 70:
+// adaptive stage -0.3 % on dof1024 and +2 % on mbdof1080 at 3).
 template <int D, int K, bool LEARNED>
-__global__ void __launch_bounds__(256) k_adaptive_decide(MdasDeviceGrid g, unsigned jumpA, unsigned jumpC) {
+__global__ void __launch_bounds__(256, LEARNED ? 1 : 4) k_adaptive_decide(MdasDeviceGrid g, unsigned jumpA,
+                                                                        unsigned jumpC) {
     pdl_launch_dependents();
     __shared__ unsigned s_warp[8];
     const int L = g.counts->L;
