@@ -458,6 +458,17 @@ int mdas_config_defaults(mdas_config* cfg);
  * message on failure. */
 int mdas_config_read(const char* path, mdas_config* cfg, char* err, int errBytes);
 
+/* ---- image files (replace sutil::saveImage in the sample apps,
+ *      SDK/optixMotionBlur/optixMotionBlur.cpp:795-840) ---- */
+#define MDAS_IMAGE_FLOAT4 0 /* float4 pixels (the film, the sampling density) -> PFM */
+#define MDAS_IMAGE_UCHAR4 1 /* uchar4 pixels (after mdas_convert_to_bytes)     -> PPM */
+
+/* Write width x height pixels from HOST memory, row-major from the top, to
+ * `path`: float4 as a Portable Float Map (RGB float32, little-endian; in place
+ * of the reference's OpenEXR output), uchar4 as a binary PPM (RGB).  Alpha is
+ * dropped.  MDAS_ERR_INVALID if the file cannot be written. */
+int mdas_save_image(const char* path, const void* pixels, int width, int height, int format);
+
 #ifdef __cplusplus
 }
 #endif

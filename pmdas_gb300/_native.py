@@ -27,6 +27,9 @@ SCENE_DISCS_DOF = 1
 SCENE_DISCS_MBDOF = 2
 SCENE_DIRECT_LIGHT = 3
 
+IMAGE_FLOAT4 = 0
+IMAGE_UCHAR4 = 1
+
 PRIM_STRIDE = 12
 
 
@@ -92,6 +95,7 @@ SIGNATURES = {
     "mdas_test_set_wait_limit": (_I, [_I]),
     "mdas_get_launch_count": (_I, [_P, C.POINTER(C.c_uint64)]),
     "mdas_get_pass_stats": (_I, [_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_int64)]),
+    "mdas_save_image": (_I, [C.c_char_p, _P, _I, _I, _I]),
     "mdas_status_string": (C.c_char_p, [_I]),
     "mdas_scene_create": (_I, [C.POINTER(_P), _I, C.c_uint64, _I, _F, _F, _I, _I]),
     "mdas_scene_destroy": (_I, [_P]),

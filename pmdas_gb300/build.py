@@ -42,7 +42,7 @@ UNITS = [
     ("order.cu", IEEE),
     ("mlp.cu", []),
 ]
-CXX_UNITS = ["env.cpp"]
+CXX_UNITS = ["env.cpp", "image_io.cpp"]
 HEADERS = ["grid_types.h", "ieee_math.h", "integrand.h", "kdgrid_kernels.cuh", "batch_kernels.cuh", "scene.h", "order.h", "mlp.h", "leaf_raw.h", "ld_hint.h"]
 
 

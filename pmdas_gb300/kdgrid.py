@@ -463,6 +463,49 @@ class Scene:
         N.check(self._lib.mdas_evaluate(grid.handle, self._h, offset, count), "mdas_evaluate")
 
 
+def save_image(path: str, pixels) -> None:
+    """Write an (H, W, 4) image held in host memory (numpy) or on the device
+    (torch; copied to the host first) to `path`: float32 as a Portable Float
+    Map, uint8 (after ConvertToBytes) as a binary PPM — the headless stand-ins
+    for the sample apps' EXR and PPM output (optixMotionBlur.cpp:795-840)."""
+    a = pixels.detach().cpu().numpy() if hasattr(pixels, "detach") else np.asarray(pixels)
+    if a.ndim != 3 or a.shape[2] != 4:
+        raise ValueError(f"expected an (H, W, 4) image, got shape {a.shape}")
+    if a.dtype == np.float32:
+        fmt = N.IMAGE_FLOAT4
+    elif a.dtype == np.uint8:
+        fmt = N.IMAGE_UCHAR4
+    else:
+        raise ValueError(f"expected float32 or uint8 pixels, got {a.dtype}")
+    a = np.ascontiguousarray(a)
+    N.check(N.load().mdas_save_image(path.encode(), a.ctypes.data, a.shape[1], a.shape[0], fmt), "mdas_save_image")
+
+
+def read_image(path: str) -> np.ndarray:
+    """Read a PFM (as (H, W, 3) float32, top row first) or a binary PPM (as
+    (H, W, 3) uint8) written by save_image."""
+    with open(path, "rb") as f:
+        data = f.read()
+    parts, pos = [], 0
+    while len(parts) < 4:  # magic, width, height, scale or maxval
+        while data[pos:pos + 1].isspace():
+            pos += 1
+        end = pos
+        while not data[end:end + 1].isspace():
+            end += 1
+        parts.append(data[pos:end].decode())
+        pos = end
+    pos += 1  # the single whitespace byte after the header
+    magic, w, h = parts[0], int(parts[1]), int(parts[2])
+    if magic == "PF":
+        dt = "<f4" if float(parts[3]) < 0 else ">f4"
+        img = np.frombuffer(data, dtype=dt, count=w * h * 3, offset=pos).reshape(h, w, 3)
+        return img[::-1].astype(np.float32)
+    if magic == "P6":
+        return np.frombuffer(data, dtype=np.uint8, count=w * h * 3, offset=pos).reshape(h, w, 3).copy()
+    raise ValueError(f"{path}: not a PFM or binary PPM file")
+
+
 def render(grid: KDGrid, scene: Scene, budget: int, pixels, width: int, height: int) -> N.RenderStats:
     """The headless budget loop of the sample apps (optixMotionBlur.cpp:768-793)."""
     st = N.RenderStats()
