@@ -1025,12 +1025,15 @@ template <int D>
 __device__ __forceinline__ void stage_records(const float* __restrict__ nb, int leaf, float4* srec) {
     constexpr int C = RecChunks<D>::C, CS = RecChunks<D>::CS, NB = NbLayout<D>::FLOATS;
     const int lane = threadIdx.x & 31;
+    // each record takes P lanes (P: C rounded up to a power of two), chunk = lane % P
+    constexpr int P = C <= 8 ? 8 : 16;
+    constexpr int RPQ = 32 / P;  // records per copy instruction
+    const int c = lane & (P - 1), r0 = lane / P;
 #pragma unroll
-    for (int q = 0; q < C; ++q) {
-        const int idx = q * 32 + lane;
-        const int rr = idx / C, c = idx - rr * C;
+    for (int q = 0; q < P; ++q) {
+        const int rr = q * RPQ + r0;
         const int src = __shfl_sync(0xffffffffu, leaf, rr);
-        if (src >= 0) cp_async16(srec + rr * CS + c, nb + (size_t)src * NB + 4 * c);
+        if (c < C && src >= 0) cp_async16(srec + rr * CS + c, nb + (size_t)src * NB + 4 * c);
     }
 }
 
