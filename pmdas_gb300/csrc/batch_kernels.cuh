@@ -88,31 +88,25 @@ __global__ void k_batch_set_counts(const MdasBatchImage* __restrict__ imgs, int 
     c->L = L;
     c->newN = 0;
     c->newL = 0;
-    c->gerr = 0u;
-    c->recomputed = 0;
+    c->gerr = c->gerrLast = 0u;
+    c->recomputed = c->recomputedLast = 0;
     c->status = 0;
     c->selected = 0;
     c->passes = 0;
-    c->gathered = 0u;
-    c->gerrNext = 0u;
+    c->gathered = c->gatheredLast = 0u;
+    c->gerrNext = c->gerrCarry = 0u;
     c->active = (N < imgs[i].budget && (long long)N + L <= imgs[i].g.maxSamples) ? 1 : 0;
 }
 
-// Clears the accumulators of the next stage of the active images:
-// which = 0 before the errors pass, 1 before the adaptive pass, 2 before the
-// learned images' predictions (their per-pass statistics).
+// Clears the per-pass statistics of the active learned images before their
+// predictions (which = 2; the pass accumulators of MdasCounts need no clearing:
+// each pass's scan clears them for the next pass).
 __global__ void k_batch_reset(const MdasBatchImage* __restrict__ imgs, int n, int which) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     MdasCounts* c = imgs[i].g.counts;
     if (!c->active) return;
-    if (which == 0) {
-        c->gerr = 0u;
-        c->recomputed = 0;
-    } else if (which == 1) {
-        c->gathered = 0u;
-        c->gerrNext = 0u;
-    } else if (imgs[i].mlp) {
+    if (which == 2 && imgs[i].mlp) {
         MdasLearnedStats* st = imgs[i].g.learned;
         // after the first pass the predictions cover only the split children:
         // the largest priority starts from that of the leaves the last pass kept
@@ -243,7 +237,7 @@ __global__ void __launch_bounds__(256) k_batch_errors(const MdasBatchImage* __re
         const int items = dirty ? 2 * newL : cnt->L;
         const int firstRight = cnt->L - newL;
         const int k = (ch - s_pre[i]) * 256 + threadIdx.x;
-        float maxError = dirty ? __uint_as_float(cnt->gerrNext) : 0.0f;
+        float maxError = dirty ? __uint_as_float(cnt->gerrCarry) : 0.0f;
         unsigned recomputed = 0;
         if (k < items && dirty) {
             // split children from the splitting pass's lists (no leaf record read);

@@ -29,13 +29,13 @@ __global__ void k_set_counts(MdasCounts* c, int N, int L) {
     c->L = L;
     c->newN = 0;
     c->newL = 0;
-    c->gerr = 0u;
-    c->recomputed = 0;
+    c->gerr = c->gerrLast = 0u;
+    c->recomputed = c->recomputedLast = 0;
     c->status = 0;
     c->selected = 0;
     c->passes = 0;
-    c->gathered = 0u;
-    c->gerrNext = 0u;
+    c->gathered = c->gatheredLast = 0u;
+    c->gerrNext = c->gerrCarry = 0u;
     c->active = 1;
 }
 
@@ -590,7 +590,8 @@ int mdas_get_gerror(mdas_grid* g, float* gError) {
     cudaError_t e = cudaMemcpyAsync(g->hcounts, g->dg.counts, sizeof(MdasCounts), cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     if (e != cudaSuccess) return MDAS_ERR_CUDA;
-    unsigned bits = g->hcounts->gerr;
+    // the last errors pass's: this pass's, or (after an adaptive pass) the last pass's
+    unsigned bits = g->errorsClean || g->hcounts->passes == 0 ? g->hcounts->gerr : g->hcounts->gerrLast;
     memcpy(gError, &bits, 4);
     return MDAS_OK;
 }
@@ -764,10 +765,10 @@ int mdas_get_stage_times_ex(mdas_grid* g, double* ms, int n, int reset) {
 
 int mdas_get_pass_stats(mdas_grid* g, int* recomputed, int* selected, int* splits, int64_t* gathered) {
     if (!g) return MDAS_ERR_INVALID;
-    if (recomputed) *recomputed = g->hcounts->recomputed;
+    if (recomputed) *recomputed = g->hcounts->recomputedLast;
     if (selected) *selected = g->hcounts->selected;
     if (splits) *splits = g->hcounts->newL;
-    if (gathered) *gathered = (int64_t)g->hcounts->gathered;
+    if (gathered) *gathered = (int64_t)g->hcounts->gatheredLast;
     return MDAS_OK;
 }
 
@@ -1112,7 +1113,9 @@ cudaError_t enqueue_batch_prologue(mdas_batch* b, cudaStream_t s) {
 cudaError_t enqueue_batch_body(mdas_batch* b, cudaGraphConditionalHandle handle, int* anyOut, cudaStream_t s) {
     const int gErr = b->numSMs * b->tune[0], gDec = b->numSMs * b->tune[1], gPl = b->numSMs * b->tune[2];
     const int gInt = b->numSMs * b->tune[3];
-    cudaError_t e = MDAS_ARITH_CALL(b, batch_reset, b->d_imgs, b->n, 0, s);
+    // (the accumulators of this pass were cleared by the last pass's scan, or
+    // when the counters were set)
+    cudaError_t e = cudaSuccess;
     for (const auto& gr : b->groups)
         if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_errors, b->d_imgs + gr.offset, gr.count, gr.D, gErr, s);
     if (e == cudaSuccess && b->anyLearned) {
@@ -1122,7 +1125,6 @@ cudaError_t enqueue_batch_body(mdas_batch* b, cudaGraphConditionalHandle handle,
             if (e == cudaSuccess) e = mdas_mlp::batch_predict(b->d_imgs + gr.offset, gr.count, gr.D, b->status, s);
         if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_learned_judge, b->d_imgs, b->n, b->numSMs * 4, s);
     }
-    if (e == cudaSuccess) e = MDAS_ARITH_CALL(b, batch_reset, b->d_imgs, b->n, 1, s);
     for (const auto& gr : b->groups)
         if (e == cudaSuccess)
             e = MDAS_ARITH_CALL(b, batch_decide, b->d_imgs + gr.offset, gr.count, gr.D, b->tileK, b->anyLearned, gDec,

@@ -7,19 +7,28 @@
 // Counters kept in device memory so that a pass never needs the host to know
 // how many leaves there are (the reference reads them back with
 // cudaMemcpyFromSymbol after every pass, kdgrid.cu:753-759).
+//
+// The accumulators of a pass need no memset before it: the adaptive pass's
+// scan, which runs once the pass's decide kernel is done, moves each to its
+// `...Last` copy (or, for gerrNext, to gerrCarry for the next errors pass) and
+// clears it for the next pass.
 struct MdasCounts {
     int N;          // samples
     int L;          // leaves
     int newN;       // samples added by the last adaptive pass
     int newL;       // leaves added by the last adaptive pass
-    unsigned gerr;   // bits of g_error, the max leaf error of the last errors pass
-    int recomputed;  // leaf errors recomputed by the last errors pass (reset with gerr)
+    unsigned gerr;   // bits of g_error, the max leaf error of the errors pass since the last adaptive pass
+    int recomputed;  // leaf errors recomputed by that errors pass
     int status;      // first device-side error (MDAS_ERR_*), 0 if none
     int selected;    // leaves selected by the last adaptive pass (== newN)
     int passes;      // adaptive passes since the initial sampling
-    unsigned gathered;  // sample coordinates read by the last adaptive pass
-    unsigned gerrNext;  // max error of the leaves the last adaptive pass did not split (reset with gathered)
+    unsigned gathered;  // sample coordinates read by the running adaptive pass
+    unsigned gerrNext;  // max error of the leaves the running adaptive pass does not split
     int active;         // batched rendering: 1 while this image still takes passes
+    unsigned gerrLast;      // gerr of the last adaptive pass
+    int recomputedLast;     // recomputed of the last adaptive pass
+    unsigned gatheredLast;  // gathered of the last adaptive pass
+    unsigned gerrCarry;     // gerrNext of the last adaptive pass (where the next errors pass starts)
 };
 
 // Learned acceptance, one pass: the largest prediction, and the judge's sums of

@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(256, 6) k_compute_errors(MdasDeviceGrid g) {
         newL = g.counts->newL;
         firstRight = g.counts->L - newL;
         items = 2 * newL;
-        maxError = __uint_as_float(g.counts->gerrNext);
+        maxError = __uint_as_float(g.counts->gerrCarry);
     } else {
         items = g.counts->L;
     }
@@ -766,7 +766,18 @@ __device__ __forceinline__ void scan_image(const MdasDeviceGrid& g, unsigned* s_
         g.counts->selected = (int)newN;
         g.counts->N = N + (int)newN;
         g.counts->L = L + (int)newL;
-        g.counts->passes += 1;
+        // the pass's accumulators: kept for the host and the next errors pass,
+        // cleared for the next pass (decide, their last writer, is done)
+        MdasCounts* c = g.counts;
+        c->gerrLast = c->gerr;
+        c->recomputedLast = c->recomputed;
+        c->gatheredLast = c->gathered;
+        c->gerrCarry = c->gerrNext;
+        c->gerr = 0u;
+        c->recomputed = 0;
+        c->gathered = 0u;
+        c->gerrNext = 0u;
+        c->passes += 1;
     }
 }
 
@@ -1459,9 +1470,8 @@ cudaError_t initial_sampling(const MdasDeviceGrid& g, int L, cudaStream_t s) {
 }
 
 cudaError_t compute_errors(const MdasDeviceGrid& g, int grid, bool dirty, cudaStream_t s) {
-    // g_error = 0 (kdgrid.cu:684-685) and the recomputed-leaf counter next to it
-    cudaError_t e = cudaMemsetAsync(&g.counts->gerr, 0, 2 * sizeof(unsigned), s);
-    if (e != cudaSuccess) return e;
+    // (g_error = 0, kdgrid.cu:684-685: cleared by the last pass's scan, or when
+    // the counters were set)
     if (dirty) {
         MDAS_SWITCH_D(g.D, (k_compute_errors<DD, 1><<<grid, 256, 0, s>>>(g)));
     } else {
@@ -1471,8 +1481,6 @@ cudaError_t compute_errors(const MdasDeviceGrid& g, int grid, bool dirty, cudaSt
 }
 
 cudaError_t compute_errors_auto(const MdasDeviceGrid& g, int grid, cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(&g.counts->gerr, 0, 2 * sizeof(unsigned), s);
-    if (e != cudaSuccess) return e;
     MDAS_SWITCH_D(g.D, (k_compute_errors<DD, 2><<<grid, 256, 0, s>>>(g)));
     return cudaGetLastError();
 }
@@ -1519,8 +1527,7 @@ static cudaError_t place_prepare(int D) {
 }
 
 cudaError_t adaptive_sampling(const MdasDeviceGrid& g, int gridDecide, int gridPlace, cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(&g.counts->gathered, 0, 2 * sizeof(unsigned), s);  // + gerrNext
-    if (e != cudaSuccess) return e;
+    cudaError_t e = cudaSuccess;
     unsigned A, C;
     lcg_jump((unsigned)(g.candidatesNum * g.D), &A, &C);
     if (g.priority && g.tileK == 4) {
