@@ -134,6 +134,8 @@ def test_batch_equals_single_renders(cuda, arith):
         (P.SCENE_DISCS_MB, 3, 128, 128, 4, 1, 4, 0.5, 2, 14, 64),
         (P.SCENE_DIRECT_LIGHT, 4, 80, 60, 32, 0, 5, 0.015625, 4, 15, 4),
         (P.SCENE_DISCS_DOF, 4, 32, 32, 2, 1, 3, 0.25, 4, 16, 16),  # budget below the initial grid: no pass
+        # a larger image (1280 x 1024) beside the small ones
+        (P.SCENE_DISCS_DOF, 4, 1280, 1024, 1, 0, 7, 0.25, 4, 17, 32),
     ]
     grids, scenes, pix, budgets, singles = [], [], [], [], []
     for kind, D, W, H, spp, bpd, eib, alpha, cand, seed, prims in specs:
@@ -162,7 +164,7 @@ def test_batch_equals_single_renders(cuda, arith):
                                 keys=("coords", "values", "nodes", "boxes", "errors", "seeds"), what=f"image {i}")
             ok, worst = rel_close(pix[i].cpu().numpy(), img)
             assert ok, (i, worst)
-    assert singles[-1][2] == 0 and singles[0][2] > 0
+    assert singles[-2][2] == 0 and singles[0][2] > 0 and singles[-1][2] > 0
     batch.close()
 
 
