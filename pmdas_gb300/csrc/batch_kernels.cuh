@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(256) k_batch_errors(const MdasBatchImage* __re
 // ---- adaptive pass: decide
 // LEARNED: some image of the batch is learned (else the lean plain kernel).
 template <int D, int K, bool LEARNED>
-__global__ void __launch_bounds__(256, 3) k_batch_decide(const MdasBatchImage* __restrict__ imgs, int n) {
+__global__ void __launch_bounds__(256, LEARNED ? 3 : 4) k_batch_decide(const MdasBatchImage* __restrict__ imgs, int n) {
     pdl_launch_dependents();
     __shared__ int s_pre[MDAS_MAX_BATCH + 1];
     __shared__ unsigned s_warp[8];
