@@ -388,13 +388,26 @@ __global__ void __launch_bounds__(256, 6) k_compute_errors(MdasDeviceGrid g) {
         // splitting pass left them (no leaf record read); learned mode also
         // completes each child's raw feature row (item k is row k)
         const int stride = gridDim.x * blockDim.x;
-        int k = blockIdx.x * blockDim.x + threadIdx.x;
-        int4 spNext = k < items ? (k < newL ? g.splitL[k] : g.splitR[k - newL]) : make_int4(0, 0, 0, 0);
-        for (; k < items; k += stride) {
+        // loop index m: the left (even m) and right (odd m) child of split m / 2
+        // in neighbouring lanes, which often read the same value sectors (errors
+        // stage -3.6 % on dof1024, -9 % on mbdof1080 against all left children
+        // first)
+        auto item = [&](int m) { return (m & 1) ? newL + (m >> 1) : (m >> 1); };
+        int m = blockIdx.x * blockDim.x + threadIdx.x;
+        int4 spNext = make_int4(0, 0, 0, 0);
+        if (m < items) {
+            const int kn = item(m);
+            spNext = kn < newL ? g.splitL[kn] : g.splitR[kn - newL];
+        }
+        for (; m < items; m += stride) {
+            const int k = item(m);
             const bool left = k < newL;
             const int4 sp = spNext;
             // the next item's entry, loaded while this one is computed
-            if (k + stride < items) spNext = k + stride < newL ? g.splitL[k + stride] : g.splitR[k + stride - newL];
+            if (m + stride < items) {
+                const int kn = item(m + stride);
+                spNext = kn < newL ? g.splitL[kn] : g.splitR[kn - newL];
+            }
             const int nodeIndex = left ? sp.z : firstRight + (k - newL);
             const int4 node = make_int4(sp.x, sp.y, left ? ~D : sp.z, ~D);
             MdasLumStats lum;
