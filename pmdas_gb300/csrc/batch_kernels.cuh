@@ -241,14 +241,17 @@ __global__ void __launch_bounds__(256) k_batch_errors(const MdasBatchImage* __re
         unsigned recomputed = 0;
         if (k < items && dirty) {
             // split children from the splitting pass's lists (no leaf record read);
-            // learned images also complete the child's raw feature row
-            const bool left = k < newL;
-            const int4 sp = left ? g.splitL[k] : g.splitR[k - newL];
-            const int nodeIndex = left ? sp.z : firstRight + (k - newL);
+            // learned images also complete the child's raw feature row.  The two
+            // children of a split in neighbouring lanes (item kk: left children
+            // first, then right ones, as the lists and rows are laid out)
+            const int kk = (k & 1) ? newL + (k >> 1) : (k >> 1);
+            const bool left = kk < newL;
+            const int4 sp = left ? g.splitL[kk] : g.splitR[kk - newL];
+            const int nodeIndex = left ? sp.z : firstRight + (kk - newL);
             MdasLumStats lum;
             const float error = node_error<D>(g, make_int4(sp.x, sp.y, left ? ~D : sp.z, ~D), __int_as_float(sp.w),
                                               g.featRaw ? &lum : nullptr);
-            if (g.featRaw) mdas_raw_store_stats(g.featRaw + (size_t)k * MDAS_RAW_FLOATS, lum, error);
+            if (g.featRaw) mdas_raw_store_stats(g.featRaw + (size_t)kk * MDAS_RAW_FLOATS, lum, error);
             g.errors[nodeIndex] = error;
             recomputed = 1;
             maxError = fmaxf(maxError, error);
