@@ -369,6 +369,7 @@ __device__ __forceinline__ float leaf_error(const MdasDeviceGrid& g, int nodeInd
 // initial sampling (the device-side budget loop, where passes alternate).
 template <int D, int MODE>
 __global__ void __launch_bounds__(256, 6) k_compute_errors(MdasDeviceGrid g) {
+    pdl_launch_dependents();  // decide may be scheduled; it waits for this grid
     __shared__ unsigned s_max[8];
     __shared__ unsigned s_cnt[8];
     const bool DIRTY = MODE == 1 || (MODE == 2 && g.counts->passes > 0);
@@ -691,6 +692,7 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
 template <int D, int K, bool LEARNED>
 __global__ void __launch_bounds__(256, LEARNED ? 1 : 4) k_adaptive_decide(MdasDeviceGrid g, unsigned jumpA,
                                                                         unsigned jumpC) {
+    pdl_wait();  // the errors pass (or the learned judge) before it has completed
     pdl_launch_dependents();
     __shared__ unsigned s_warp[8];
     const int L = g.counts->L;
@@ -1544,14 +1546,15 @@ cudaError_t adaptive_sampling(const MdasDeviceGrid& g, int gridDecide, int gridP
     unsigned A, C;
     lcg_jump((unsigned)(g.candidatesNum * g.D), &A, &C);
     if (g.priority && g.tileK == 4) {
-        MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD, 4, true><<<gridDecide, 256, 0, s>>>(g, A, C)));
+        MDAS_SWITCH_D(g.D, (e = launch_pdl(k_adaptive_decide<DD, 4, true>, gridDecide, 256, s, g, A, C)));
     } else if (g.priority) {
-        MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD, 8, true><<<gridDecide, 256, 0, s>>>(g, A, C)));
+        MDAS_SWITCH_D(g.D, (e = launch_pdl(k_adaptive_decide<DD, 8, true>, gridDecide, 256, s, g, A, C)));
     } else if (g.tileK == 4) {
-        MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD, 4, false><<<gridDecide, 256, 0, s>>>(g, A, C)));
+        MDAS_SWITCH_D(g.D, (e = launch_pdl(k_adaptive_decide<DD, 4, false>, gridDecide, 256, s, g, A, C)));
     } else {
-        MDAS_SWITCH_D(g.D, (k_adaptive_decide<DD, 8, false><<<gridDecide, 256, 0, s>>>(g, A, C)));
+        MDAS_SWITCH_D(g.D, (e = launch_pdl(k_adaptive_decide<DD, 8, false>, gridDecide, 256, s, g, A, C)));
     }
+    if (e != cudaSuccess) return e;
     e = launch_pdl(k_adaptive_scan, 1, 1024, s, g);
     if (e != cudaSuccess) return e;
     e = place_prepare(g.D);
