@@ -1085,7 +1085,9 @@ __device__ __forceinline__ void warp_locate(const MdasDeviceGrid& g, int kb, int
     tile = t0 + j;
     pre.x = __shfl_sync(0xffffffffu, P.x, j);
     pre.y = __shfl_sync(0xffffffffu, P.y, j);
-    if (j == 31) {  // (only where 31 tiles in a row hold fewer than 32 accepted leaves)
+    // (only where 31 tiles in a row hold fewer than 32 accepted leaves; not for
+    // the lanes past the last rank, which would walk to the last tile)
+    if (j == 31 && k < (int)totals.x) {
         while (tile + 1 < ntiles) {
             const uint2 next = g.tilePrefix[tile + 1];
             if ((int)next.x > k) break;
