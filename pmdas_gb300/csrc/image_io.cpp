@@ -18,13 +18,6 @@
 
 namespace {
 
-bool little_endian_host() {
-    const uint32_t one = 1u;
-    unsigned char b;
-    memcpy(&b, &one, 1);
-    return b == 1;
-}
-
 // float bits in little-endian byte order, whatever the host's
 void put_le(unsigned char* dst, float v) {
     uint32_t u;
@@ -48,7 +41,6 @@ extern "C" int mdas_save_image(const char* path, const void* pixels, int width, 
         ok = fprintf(f, "PF\n%d %d\n-1.0\n", width, height) > 0;
         const float* px = static_cast<const float*>(pixels);
         std::vector<unsigned char> row(12 * W);
-        (void)little_endian_host;  // the bytes are written explicitly little-endian
         for (size_t y = 0; y < H && ok; ++y) {
             const float* src = px + 4 * W * (H - 1 - y);  // PFM rows run bottom to top
             for (size_t x = 0; x < W; ++x)

@@ -1129,8 +1129,8 @@ __global__ void __launch_bounds__(256, D >= 5 ? 2 : 3) k_adaptive_place(MdasDevi
         warp_locate(g, kbase, k, ntiles, tile, pre);
         if (k < accepted) e = g.accepted[(size_t)tile * TILE + (k - (int)pre.x)];
     };
-    uint2 e0 = make_uint2(0u, 0u), pre0;
-    int tile0;
+    uint2 e0 = make_uint2(0u, 0u), pre0 = make_uint2(0u, 0u);
+    int tile0 = 0;
     fetch(kb, e0, tile0, pre0);
     stage_records<D>(g.nb, kb + lane < accepted ? tile0 * TILE + (int)(e0.x & 0x7ffu) : -1, s_rec[0][warp]);
     cp_async_commit();
@@ -1138,7 +1138,7 @@ __global__ void __launch_bounds__(256, D >= 5 ? 2 : 3) k_adaptive_place(MdasDevi
     for (;;) {
         const int kn = kb + stride;
         const bool more = kn < accepted;  // warp-uniform
-        uint2 e1 = make_uint2(0u, 0u), pre1;
+        uint2 e1 = make_uint2(0u, 0u), pre1 = make_uint2(0u, 0u);
         int tile1 = 0;
         if (more) {
             fetch(kn, e1, tile1, pre1);
@@ -1533,13 +1533,15 @@ static void lcg_jump(unsigned n, unsigned* A, unsigned* C) {
 // The place kernel's shared-memory carveout: its double buffers take 56 KB per
 // CTA at D = 4, three CTAs per SM need the largest carveout.
 static cudaError_t place_prepare(int D) {
-    static bool done[7] = {};
+    static bool done[64][7] = {};  // per device ordinal (a function attribute is set per device)
     if (D < 3 || D > 6) return cudaErrorInvalidValue;
-    if (done[D]) return cudaSuccess;
-    cudaError_t e = cudaSuccess;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < 64 && done[dev][D]) return cudaSuccess;
     MDAS_SWITCH_D(D, (e = cudaFuncSetAttribute(k_adaptive_place<DD>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                                (int)cudaSharedmemCarveoutMaxShared)));
-    if (e == cudaSuccess) done[D] = true;
+    if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev][D] = true;
     return e;
 }
 
