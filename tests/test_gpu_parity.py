@@ -486,3 +486,33 @@ def test_full_size_ieee_pass_matches_oracle(cuda, name):
     assert g.GetNewSamples() == o.newN > 0
     assert_states_equal(g.dump_state(), o.dump_state(), keys=("coords", "nodes", "boxes", "errors", "seeds"),
                         what=f"{name} full-size pass vs oracle")
+
+
+def test_pass_accumulators_without_memsets(cuda):
+    """No pass clears its accumulators with a memset: the adaptive pass's scan
+    keeps them for the host and clears them for the next pass.  g_error stays
+    the last errors pass's after the adaptive pass (as the reference's
+    __device__ g_error does), a repeated errors pass gives the same g_error,
+    and the pass tallies match the dumped state."""
+    g, sc, _, c = make("dof4d", P.ARITH_REFERENCE)
+    g.InitialSampling()
+    sc.evaluate(g, 0, g.GetNumberOfSamples())
+    for k in range(4):
+        g.ComputeErrors()
+        ge = g.GetGError()
+        st = g.dump_state()
+        assert ge == float(st["errors"].max())  # the max over every leaf
+        g.ComputeErrors()  # again, no adaptive pass between: the same value
+        assert g.GetGError() == ge
+        L0 = g.GetNumberOfNodes()
+        g.AdaptiveSampling()
+        assert g.GetGError() == ge  # still this pass's after the adaptive pass
+        ps = g.pass_stats()
+        assert ps["selected"] == g.GetNewSamples() > 0
+        assert ps["splits"] == g.GetNumberOfNodes() - L0
+        # every sample coordinate the accepted leaves held was read once
+        assert 0 < ps["gathered"] <= 4 * ps["selected"]
+        n2, nn = g.GetNumberOfSamples(), g.GetNewSamples()
+        sc.evaluate(g, n2 - nn, nn)
+        if k == 0:
+            assert ps["recomputed"] == L0  # the first errors pass visits every leaf
