@@ -687,12 +687,12 @@ __device__ __forceinline__ void decide_tile(const MdasDeviceGrid& g, int tile, i
     __syncthreads();  // s_warp is reused by the next tile
 }
 
-// Plain decide at 4 CTAs per SM (63 registers; measured against 3 CTAs at 70:
-// adaptive stage -0.3 % on dof1024 and +2 % on mbdof1080 at 3).
+// Plain decide at 4 CTAs per SM (63 registers); measured against 3 CTAs per
+// SM (70 registers): equal on dof1024, adaptive stage 2 % faster on mbdof1080.
 template <int D, int K, bool LEARNED>
 __global__ void __launch_bounds__(256, LEARNED ? 1 : 4) k_adaptive_decide(MdasDeviceGrid g, unsigned jumpA,
                                                                         unsigned jumpC) {
-    pdl_wait();  // the errors pass (or the learned judge) before it has completed
+    pdl_wait();  // until the kernel before it (the errors pass or the learned judge) has completed
     pdl_launch_dependents();
     __shared__ unsigned s_warp[8];
     const int L = g.counts->L;
@@ -826,10 +826,6 @@ __device__ __forceinline__ PlaceLoc place_locate(const MdasDeviceGrid& g, int k,
     return p;
 }
 
-// place, one accepted leaf (entry r of `tile`, whose prefix is `pre`, entry
-// word `e`): best candidate, append or split.  The leaf's record is read from
-// its chunks staged in shared memory at srec, or from global memory when srec
-// is null.
 // 16-byte chunks of a leaf record that the adaptive pass reads (node, box, padding, private copy)
 template <int D>
 struct RecChunks {
@@ -859,6 +855,10 @@ __device__ __forceinline__ int4 rec_from_chunks(const float4* __restrict__ ch, f
     return make_int4(__float_as_int(v[0]), __float_as_int(v[1]), __float_as_int(v[2]), __float_as_int(v[3]));
 }
 
+// place, one accepted leaf (entry r of `tile`, whose prefix is `pre`, entry
+// word `e`): best candidate, append or split.  The leaf's record is read from
+// its chunks staged in shared memory at srec, or from global memory when srec
+// is null.
 template <int D>
 __device__ __forceinline__ void place_entry(const MdasDeviceGrid& g, int tile, int r, uint2 pre, uint2 e, int N,
                                             int L, const float4* srec = nullptr) {
